@@ -1,0 +1,393 @@
+// C ABI of libiqgpu.so: contexts, errors, the resident training image and the per-operation
+// entry points (fastdistance, pick, graphcut, finddisabled, genpath). iq_simulate lives in
+// iq_sim.cu.
+#include <stdarg.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
+#include "iq_internal.h"
+
+static thread_local char g_err[1024] = "";
+
+int iq_set_error(int code, const char* fmt, ...) {
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(g_err, sizeof(g_err), fmt, ap);
+  va_end(ap);
+  return code;
+}
+
+extern "C" const char* iq_last_error(void) { return g_err; }
+
+extern "C" int iq_version(void) { return 100; }  // 0.1.0
+
+void* iq_scratch(iq_ctx* ctx, int slot, size_t bytes) {
+  if ((int)ctx->buf.size() <= slot) {
+    ctx->buf.resize(slot + 1, nullptr);
+    ctx->buf_bytes.resize(slot + 1, 0);
+  }
+  if (bytes == 0) bytes = 256;
+  if (ctx->buf_bytes[slot] >= bytes) return ctx->buf[slot];
+  if (ctx->buf[slot]) {
+    cudaStreamSynchronize(ctx->stream);
+    cudaFree(ctx->buf[slot]);
+    ctx->buf[slot] = nullptr;
+    ctx->buf_bytes[slot] = 0;
+  }
+  void* p = nullptr;
+  if (cudaMalloc(&p, bytes) != cudaSuccess) {
+    cudaGetLastError();
+    iq_set_error(IQ_ERR_ALLOC, "device allocation of %zu bytes failed", bytes);
+    return nullptr;
+  }
+  ctx->buf[slot] = p;
+  ctx->buf_bytes[slot] = bytes;
+  return p;
+}
+
+// ---- timers --------------------------------------------------------------------------
+void iq_timer_start(iq_ctx* ctx, const char* name) {
+  if (!ctx->prof) return;
+  IqTimer& t = ctx->timers[name];
+  if (t.ev.size() < 2 * (t.used + 1)) {
+    for (int i = 0; i < 2; ++i) {
+      cudaEvent_t e;
+      cudaEventCreate(&e);
+      t.ev.push_back(e);
+    }
+  }
+  cudaEventRecord(t.ev[2 * t.used], ctx->stream);
+}
+
+void iq_timer_stop(iq_ctx* ctx, const char* name) {
+  if (!ctx->prof) return;
+  IqTimer& t = ctx->timers[name];
+  cudaEventRecord(t.ev[2 * t.used + 1], ctx->stream);
+  t.used++;
+}
+
+extern "C" int iq_profile(iq_ctx* ctx, int32_t enable) {
+  if (!ctx) return iq_set_error(IQ_ERR_ARG, "null context");
+  cudaStreamSynchronize(ctx->stream);
+  for (auto& kv : ctx->timers) kv.second.used = 0;
+  ctx->prof = enable != 0;
+  return IQ_OK;
+}
+
+extern "C" int iq_profile_get(iq_ctx* ctx, const char* kernel, double* ms_total,
+                              int64_t* launches) {
+  if (!ctx || !kernel) return iq_set_error(IQ_ERR_ARG, "null argument");
+  IQ_CUDA_OK(cudaStreamSynchronize(ctx->stream));
+  double ms = 0;
+  int64_t n = 0;
+  auto it = ctx->timers.find(kernel);
+  if (it != ctx->timers.end()) {
+    for (size_t i = 0; i < it->second.used; ++i) {
+      float f = 0;
+      cudaEventElapsedTime(&f, it->second.ev[2 * i], it->second.ev[2 * i + 1]);
+      ms += f;
+    }
+    n = (int64_t)it->second.used;
+  }
+  if (ms_total) *ms_total = ms;
+  if (launches) *launches = n;
+  return IQ_OK;
+}
+
+// ---- contexts ------------------------------------------------------------------------
+extern "C" int iq_ctx_create(int device, iq_ctx** out) {
+  if (!out) return iq_set_error(IQ_ERR_ARG, "null output pointer");
+  *out = nullptr;
+  IQ_CUDA_OK(cudaSetDevice(device));
+  iq_ctx* c = new iq_ctx();
+  c->device = device;
+  if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    delete c;
+    return iq_set_error(IQ_ERR_CUDA, "stream creation failed");
+  }
+  if (cudaMalloc(&c->d_status, sizeof(int)) != cudaSuccess) {
+    cudaStreamDestroy(c->stream);
+    delete c;
+    return iq_set_error(IQ_ERR_ALLOC, "status word allocation failed");
+  }
+  cudaMemset(c->d_status, 0, sizeof(int));
+  *out = c;
+  return IQ_OK;
+}
+
+static void free_ti(iq_ctx* c) {
+  cudaFree(c->d_ti);
+  cudaFree(c->d_ti2ii);
+  cudaFree(c->d_nanii);
+  c->d_ti = nullptr;
+  c->d_ti2ii = nullptr;
+  c->d_nanii = nullptr;
+  c->has_ti = false;
+}
+
+extern "C" int iq_ctx_destroy(iq_ctx* ctx) {
+  if (!ctx) return IQ_OK;
+  cudaSetDevice(ctx->device);
+  cudaStreamSynchronize(ctx->stream);
+  free_ti(ctx);
+  for (void* p : ctx->buf) cudaFree(p);
+  for (auto& kv : ctx->timers)
+    for (auto e : kv.second.ev) cudaEventDestroy(e);
+  cudaFree(ctx->d_status);
+  cudaStreamDestroy(ctx->stream);
+  delete ctx;
+  return IQ_OK;
+}
+
+extern "C" void* iq_ctx_stream(iq_ctx* ctx) { return ctx ? (void*)ctx->stream : nullptr; }
+
+// ---- training image --------------------------------------------------------------------
+static int read_dims(int32_t ndim, const int64_t* size, Dim3& d) {
+  if (ndim < 1 || ndim > 3 || !size) return iq_set_error(IQ_ERR_ARG, "ndim must be 1, 2 or 3");
+  int64_t e[3] = {1, 1, 1};
+  for (int i = 0; i < ndim; ++i) {
+    if (size[i] <= 0) return iq_set_error(IQ_ERR_ARG, "extents must be positive");
+    if (size[i] > (1 << 20)) return iq_set_error(IQ_ERR_LIMIT, "extent above 2^20");
+    e[i] = size[i];
+  }
+  d = Dim3{e[0], e[1], e[2]};
+  return IQ_OK;
+}
+
+extern "C" int iq_set_ti(iq_ctx* ctx, const void* ti, int32_t dtype, int32_t ndim,
+                         const int64_t* size) {
+  if (!ctx || !ti) return iq_set_error(IQ_ERR_ARG, "null argument");
+  if (dtype != IQ_F32 && dtype != IQ_F64) return iq_set_error(IQ_ERR_ARG, "dtype must be F32 or F64");
+  Dim3 d;
+  int rc = read_dims(ndim, size, d);
+  if (rc) return rc;
+  IQ_CUDA_OK(cudaSetDevice(ctx->device));
+  const int64_t n = d.vol();
+  if (n >= (int64_t)1 << 31) return iq_set_error(IQ_ERR_LIMIT, "training image above 2^31 voxels");
+  const bool same = ctx->has_ti && ctx->ti.x == d.x && ctx->ti.y == d.y && ctx->ti.z == d.z;
+  if (!same) {
+    cudaStreamSynchronize(ctx->stream);
+    free_ti(ctx);
+    const int64_t nii = (d.x + 1) * (d.y + 1) * (d.z + 1);
+    if (cudaMalloc(&ctx->d_ti, sizeof(float) * n) != cudaSuccess ||
+        cudaMalloc(&ctx->d_ti2ii, sizeof(double) * nii) != cudaSuccess ||
+        cudaMalloc(&ctx->d_nanii, sizeof(int32_t) * nii) != cudaSuccess) {
+      cudaGetLastError();
+      free_ti(ctx);
+      return iq_set_error(IQ_ERR_ALLOC, "training image allocation failed");
+    }
+  }
+  ctx->has_ti = false;
+  uint8_t* nanm = (uint8_t*)iq_scratch(ctx, S_TMP0, (size_t)n);
+  if (!nanm) return IQ_ERR_ALLOC;
+  if (dtype == IQ_F32) {
+    IQ_CUDA_OK(cudaMemcpyAsync(ctx->d_ti, ti, sizeof(float) * n, cudaMemcpyDefault, ctx->stream));
+  } else {
+    double* tmp = (double*)iq_scratch(ctx, S_TMP1, sizeof(double) * n);
+    if (!tmp) return IQ_ERR_ALLOC;
+    IQ_CUDA_OK(cudaMemcpyAsync(tmp, ti, sizeof(double) * n, cudaMemcpyDefault, ctx->stream));
+    if ((rc = iq_launch_to_f32(ctx, tmp, ctx->d_ti, n))) return rc;
+  }
+  if ((rc = iq_launch_prepare(ctx, ctx->d_ti, n, nanm))) return rc;
+  if ((rc = iq_build_integrals(ctx, ctx->d_ti, d, ctx->d_ti2ii, ctx->d_nanii, nanm))) return rc;
+  int32_t total = 0;
+  IQ_CUDA_OK(cudaMemcpyAsync(&total, ctx->d_nanii + (d.x + 1) * (d.y + 1) * (d.z + 1) - 1,
+                             sizeof(int32_t), cudaMemcpyDeviceToHost, ctx->stream));
+  IQ_CUDA_OK(cudaStreamSynchronize(ctx->stream));
+  ctx->ti = d;
+  ctx->ndim = ndim;
+  ctx->ti_nan = total;
+  ctx->has_ti = true;
+  return IQ_OK;
+}
+
+// ---- fastdistance -----------------------------------------------------------------------
+extern "C" int iq_fastdistance(iq_ctx* ctx, const int64_t* tilesize, int32_t ntmpl,
+                               const float* tmpl, const uint8_t* weights, float* out) {
+  if (!ctx || !tilesize || !tmpl || !out || ntmpl <= 0)
+    return iq_set_error(IQ_ERR_ARG, "invalid argument");
+  if (!ctx->has_ti) return iq_set_error(IQ_ERR_STATE, "no training image set");
+  IQ_CUDA_OK(cudaSetDevice(ctx->device));
+  Dim3 t;
+  int rc = read_dims(ctx->ndim, tilesize, t);
+  if (rc) return rc;
+  if (t.x > ctx->ti.x || t.y > ctx->ti.y || t.z > ctx->ti.z)
+    return iq_set_error(IQ_ERR_ARG, "invalid tile size");
+  if (t.x >= 1024 || t.y >= 1024 || t.z >= 1024) return iq_set_error(IQ_ERR_LIMIT, "tile extent >= 1024");
+  const int64_t T = t.vol();
+  Dim3 od{ctx->ti.x - t.x + 1, ctx->ti.y - t.y + 1, ctx->ti.z - t.z + 1};
+  const int64_t P = od.vol();
+  // mask -> offset list (host)
+  std::vector<uint8_t> w(T, 1);
+  if (weights) IQ_CUDA_OK(cudaMemcpy(w.data(), weights, T, cudaMemcpyDefault));
+  std::vector<uint32_t> kl;
+  for (int64_t k = 0; k < T; ++k)
+    if (w[k]) kl.push_back(kpack(k % t.x, (k / t.x) % t.y, k / (t.x * t.y)));
+  const int K = (int)kl.size();
+  // A2 by integral image when the mask is all ones, else direct
+  const bool full = K == T;
+  const int rt = iq_register_tile(ntmpl);
+  const int rpad = ((ntmpl + rt - 1) / rt) * rt;
+  float* d_tmpl = (float*)iq_scratch(ctx, S_TMP2, sizeof(float) * T * ntmpl);
+  uint32_t* d_kl = (uint32_t*)iq_scratch(ctx, S_KLIST, sizeof(uint32_t) * std::max(K, 1));
+  float* d_tv = (float*)iq_scratch(ctx, S_TV, sizeof(float) * std::max<int64_t>(K, 1) * rpad);
+  double* d_b2 = (double*)iq_scratch(ctx, S_B2, sizeof(double) * rpad);
+  uint8_t* d_dis = (uint8_t*)iq_scratch(ctx, S_DIS, (size_t)P);
+  float* d_out = (float*)iq_scratch(ctx, S_D, sizeof(float) * P * ntmpl);
+  if (!d_tmpl || !d_kl || !d_tv || !d_b2 || !d_dis || !d_out) return IQ_ERR_ALLOC;
+  IQ_CUDA_OK(cudaMemcpyAsync(d_tmpl, tmpl, sizeof(float) * T * ntmpl, cudaMemcpyDefault, ctx->stream));
+  if (K) IQ_CUDA_OK(cudaMemcpyAsync(d_kl, kl.data(), sizeof(uint32_t) * K, cudaMemcpyHostToDevice, ctx->stream));
+  if ((rc = iq_launch_disabled(ctx, ctx->d_nanii, ctx->ti, t, d_dis))) return rc;
+  GatherLaunch G;
+  G.grid = d_tmpl; G.grid_dims = t; G.grid_stride = T; G.start0 = 0;
+  G.K = K; G.klist = d_kl; G.ntmpl = ntmpl; G.rpad = rpad; G.tv = d_tv; G.b2 = d_b2;
+  if ((rc = iq_launch_gather(ctx, G))) return rc;
+  CorrLaunch C;
+  C.img = ctx->d_ti; C.img_dims = ctx->ti; C.out_dims = od; C.K = K; C.klist = d_kl;
+  C.tv = d_tv; C.rpad = rpad; C.ntmpl = ntmpl; C.b2 = d_b2;
+  if (full) {
+    C.a2.ii = ctx->d_ti2ii;
+    C.a2.tile[0] = t.x; C.a2.tile[1] = t.y; C.a2.tile[2] = t.z;
+  }
+  C.disabled = d_dis; C.out = d_out; C.out_stride = P;
+  if ((rc = iq_launch_corr(ctx, C))) return rc;
+  IQ_CUDA_OK(cudaMemcpyAsync(out, d_out, sizeof(float) * P * ntmpl, cudaMemcpyDefault, ctx->stream));
+  IQ_CUDA_OK(cudaStreamSynchronize(ctx->stream));
+  return IQ_OK;
+}
+
+extern "C" int iq_finddisabled(iq_ctx* ctx, const int64_t* tilesize, uint8_t* out) {
+  if (!ctx || !tilesize || !out) return iq_set_error(IQ_ERR_ARG, "invalid argument");
+  if (!ctx->has_ti) return iq_set_error(IQ_ERR_STATE, "no training image set");
+  IQ_CUDA_OK(cudaSetDevice(ctx->device));
+  Dim3 t;
+  int rc = read_dims(ctx->ndim, tilesize, t);
+  if (rc) return rc;
+  if (t.x > ctx->ti.x || t.y > ctx->ti.y || t.z > ctx->ti.z)
+    return iq_set_error(IQ_ERR_ARG, "invalid tile size");
+  const int64_t P = (ctx->ti.x - t.x + 1) * (ctx->ti.y - t.y + 1) * (ctx->ti.z - t.z + 1);
+  uint8_t* d = (uint8_t*)iq_scratch(ctx, S_DIS, (size_t)P);
+  if (!d) return IQ_ERR_ALLOC;
+  if ((rc = iq_launch_disabled(ctx, ctx->d_nanii, ctx->ti, t, d))) return rc;
+  IQ_CUDA_OK(cudaMemcpyAsync(out, d, (size_t)P, cudaMemcpyDefault, ctx->stream));
+  IQ_CUDA_OK(cudaStreamSynchronize(ctx->stream));
+  return IQ_OK;
+}
+
+// relaxation sizes of src/relaxation.jl:11-36 for a given npatterns
+void iq_relax_sizes(int64_t npat, double tol, int64_t& dbnorm, int64_t& dbzero, int& nnorm,
+                    int64_t* seqnorm, int& nzero, int64_t* seqzero);
+
+// ---- pick ------------------------------------------------------------------------------
+extern "C" int iq_pick(iq_ctx* ctx, const float* D, int64_t P, int32_t naux,
+                       const float* const* Ds, double tol, uint64_t seed, int64_t tile,
+                       int64_t real, int64_t* out_index, int64_t* out_ncand, int64_t* out_cands,
+                       double* out_weights, int64_t cap) {
+  if (!ctx || !D || P <= 0 || naux < 0 || (naux > 0 && !Ds) || !out_index)
+    return iq_set_error(IQ_ERR_ARG, "invalid argument");
+  if (naux > IQ_MAX_AUX) return iq_set_error(IQ_ERR_LIMIT, "at most %d auxiliary distances", IQ_MAX_AUX);
+  if (P >= ((int64_t)1 << 31)) return iq_set_error(IQ_ERR_LIMIT, "P above 2^31");
+  if (!(tol > 0 && tol <= 1)) return iq_set_error(IQ_ERR_ARG, "tolerance must be in range (0,1]");
+  IQ_CUDA_OK(cudaSetDevice(ctx->device));
+  const int nsrc = 1 + naux;
+  float* d_src = (float*)iq_scratch(ctx, S_D, sizeof(float) * P * nsrc);
+  unsigned* d_mm = (unsigned*)iq_scratch(ctx, S_MINMAX, sizeof(unsigned) * 2);
+  int32_t* cand = (int32_t*)iq_scratch(ctx, S_PICK_CAND, sizeof(int32_t) * P);
+  uint32_t* k0 = (uint32_t*)iq_scratch(ctx, S_PICK_K0, sizeof(uint32_t) * P);
+  uint32_t* v0 = (uint32_t*)iq_scratch(ctx, S_PICK_V0, sizeof(uint32_t) * P);
+  uint32_t* k1 = (uint32_t*)iq_scratch(ctx, S_PICK_K1, sizeof(uint32_t) * P);
+  uint32_t* v1 = (uint32_t*)iq_scratch(ctx, S_PICK_V1, sizeof(uint32_t) * P);
+  double* w = (double*)iq_scratch(ctx, S_PICK_W, sizeof(double) * P);
+  double* prod = (double*)iq_scratch(ctx, S_PICK_PROD, sizeof(double) * P);
+  int64_t* rind = (int64_t*)iq_scratch(ctx, S_RIND, sizeof(int64_t) * 2);
+  if (!d_src || !d_mm || !cand || !k0 || !v0 || !k1 || !v1 || !w || !prod || !rind) return IQ_ERR_ALLOC;
+  IQ_CUDA_OK(cudaMemcpyAsync(d_src, D, sizeof(float) * P, cudaMemcpyDefault, ctx->stream));
+  for (int j = 0; j < naux; ++j)
+    IQ_CUDA_OK(cudaMemcpyAsync(d_src + (j + 1) * P, Ds[j], sizeof(float) * P, cudaMemcpyDefault,
+                               ctx->stream));
+  // min and max-finite of D, and npatterns, on the host copy-free path: small reduction here
+  std::vector<float> hD(P);
+  IQ_CUDA_OK(cudaMemcpyAsync(hD.data(), d_src, sizeof(float) * P, cudaMemcpyDeviceToHost, ctx->stream));
+  IQ_CUDA_OK(cudaStreamSynchronize(ctx->stream));
+  unsigned mn = 0x7F800000u, mx = 0u;
+  int64_t npat = 0;
+  for (int64_t p = 0; p < P; ++p) {
+    unsigned b = fbits(hD[p]);
+    mn = std::min(mn, b);
+    if (b < 0x7F800000u) { mx = std::max(mx, b); ++npat; }
+  }
+  unsigned hmm[2] = {mn, mx};
+  IQ_CUDA_OK(cudaMemcpyAsync(d_mm, hmm, sizeof(hmm), cudaMemcpyHostToDevice, ctx->stream));
+  IQ_CUDA_OK(cudaMemsetAsync(ctx->d_status, 0, sizeof(int), ctx->stream));
+  PickLaunch L;
+  L.P = P; L.npat = npat; L.tol = tol; L.seed = seed; L.tile = tile; L.real0 = real; L.nreal = 1;
+  L.D0 = d_src; L.D0_rstride = 0; L.mm0 = d_mm; L.mm0_rstride = 0;
+  L.naux = naux;
+  for (int j = 0; j < naux; ++j) { L.aux[j] = d_src + (j + 1) * P; L.aux_rstride[j] = 0; }
+  if (naux > 0 && npat > 0)
+    iq_relax_sizes(npat, tol, L.dbsize_norm, L.dbsize_zero, L.nseq_norm, L.seq_norm, L.nseq_zero,
+                   L.seq_zero);
+  L.cand = cand; L.k0 = k0; L.v0 = v0; L.k1 = k1; L.v1 = v1; L.w = w; L.prod = prod;
+  L.rind = rind; L.ncand = rind + 1; L.status = ctx->d_status;
+  int rc = iq_launch_pick(ctx, L);
+  if (rc) return rc;
+  int64_t hr[2];
+  int st = 0;
+  IQ_CUDA_OK(cudaMemcpyAsync(hr, rind, sizeof(hr), cudaMemcpyDeviceToHost, ctx->stream));
+  IQ_CUDA_OK(cudaMemcpyAsync(&st, ctx->d_status, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  IQ_CUDA_OK(cudaStreamSynchronize(ctx->stream));
+  if (st) return iq_set_error(st, "pick failed (status %d): no enabled pattern", st);
+  *out_index = hr[0];
+  const int64_t n = hr[1];
+  if (out_ncand) *out_ncand = n;
+  if (out_cands && cap > 0) {
+    std::vector<int32_t> c(std::min(n, cap));
+    IQ_CUDA_OK(cudaMemcpy(c.data(), cand, sizeof(int32_t) * c.size(), cudaMemcpyDeviceToHost));
+    for (size_t i = 0; i < c.size(); ++i) out_cands[i] = c[i];
+  }
+  if (out_weights && cap > 0)
+    IQ_CUDA_OK(cudaMemcpy(out_weights, w, sizeof(double) * std::min(n, cap), cudaMemcpyDefault));
+  return IQ_OK;
+}
+
+// ---- graph cut ---------------------------------------------------------------------------
+extern "C" int iq_graphcut(iq_ctx* ctx, const float* A, const float* B, int32_t ndim,
+                           const int64_t* size, int32_t dim, uint8_t* mask) {
+  if (!ctx || !A || !B || !mask) return iq_set_error(IQ_ERR_ARG, "null argument");
+  Dim3 d;
+  int rc = read_dims(ndim, size, d);
+  if (rc) return rc;
+  if (dim < 0 || dim >= ndim) return iq_set_error(IQ_ERR_ARG, "invalid cut dimension");
+  IQ_CUDA_OK(cudaSetDevice(ctx->device));
+  const int64_t n = d.vol();
+  if (n >= ((int64_t)1 << 24)) return iq_set_error(IQ_ERR_LIMIT, "slab above 2^24 nodes");
+  float* dA = (float*)iq_scratch(ctx, S_TMP0, sizeof(float) * n * 2);
+  uint8_t* dout = (uint8_t*)iq_scratch(ctx, S_CUTBUF, (size_t)n);
+  void* scr = iq_scratch(ctx, S_CUTSCR, iq_cut_scratch_bytes(n));
+  if (!dA || !dout || !scr) return IQ_ERR_ALLOC;
+  IQ_CUDA_OK(cudaMemcpyAsync(dA, A, sizeof(float) * n, cudaMemcpyDefault, ctx->stream));
+  IQ_CUDA_OK(cudaMemcpyAsync(dA + n, B, sizeof(float) * n, cudaMemcpyDefault, ctx->stream));
+  IQ_CUDA_OK(cudaMemsetAsync(ctx->d_status, 0, sizeof(int), ctx->stream));
+  CutLaunch L;
+  L.nslab = 1;
+  L.slab[0].dim = dim;
+  L.slab[0].next = 0;
+  L.slab[0].off[0] = L.slab[0].off[1] = L.slab[0].off[2] = 0;
+  L.slab[0].ext[0] = d.x; L.slab[0].ext[1] = d.y; L.slab[0].ext[2] = d.z;
+  L.nreal = 1;
+  L.A = dA; L.B = dA + n;
+  L.out = dout; L.slabmax = n;
+  L.scratch = scr; L.scratch_per_cta = (int64_t)iq_cut_scratch_bytes(n);
+  L.status = ctx->d_status;
+  if ((rc = iq_launch_cut(ctx, L))) return rc;
+  int st = 0;
+  IQ_CUDA_OK(cudaMemcpyAsync(mask, dout, (size_t)n, cudaMemcpyDefault, ctx->stream));
+  IQ_CUDA_OK(cudaMemcpyAsync(&st, ctx->d_status, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  IQ_CUDA_OK(cudaStreamSynchronize(ctx->stream));
+  if (st) return iq_set_error(st, "graph cut hit its round limit");
+  return IQ_OK;
+}

@@ -1,0 +1,354 @@
+// Minimum-error boundary cut of the overlap slabs (src/graphcut.jl:5-84).
+//
+// One CTA per (realization, slab). The lattice graph, the capacities
+//   c(u, v) = (|A-B|_u + |A-B|_v) / (|A_v-A_u| + |A_w-A_v| + |B_v-B_u| + |B_w-B_v| + eps())
+// (Float32 differences and sums, Float64 division, as Julia does for Float32 arrays) and the
+// infinite source/sink slices follow the reference. The max-flow is a synchronous
+// push-relabel instead of Boykov-Kolmogorov:
+//   * the first slice along the cut dimension is contracted into s, the last into t;
+//   * residuals are stored per directed arc in Float64; an arc is open when its residual is
+//     above 2^-30 of the larger residual of its edge (the oracle uses the same predicate);
+//   * each round: every active node pushes along its first admissible arc (h(u) = h(v) + 1),
+//     then every node gathers the flow pushed into it in a fixed order and relabels if it
+//     still has excess and no admissible arc -- deterministic, no atomics;
+//   * a global relabel (BFS from t over open arcs) runs at the start, every GR rounds and at
+//     the end; nodes that cannot reach t get height NH and stop being active.
+// At the end the nodes that can reach t are the sink side of the canonical minimum cut (the
+// same set for every maximum flow, which is what BK's sink tree holds at termination), and
+// mask = not sink side (graphcut.jl:75-81). Excess arithmetic uses __dadd/__dsub; every
+// comparison is done on the bit patterns of non-negative doubles (integer compares).
+#include "iq_internal.h"
+
+namespace {
+
+constexpr int CUT_THREADS = 512;
+constexpr int GR_PERIOD = 32;
+
+struct CutArgs {
+  CutSlab slab[6];
+  int nslab;
+  const float* sim; int64_t sx, sy; int64_t sim_rs; int64_t tile_start;
+  const float* ti; int64_t tix, tiy; int64_t dx, dy;
+  const int64_t* rind;
+  const float* A; const float* B;
+  uint8_t* out; int64_t slabmax;
+  char* scratch; int64_t scratch_per_cta;
+  int* status;
+  int round_cap;
+};
+
+__device__ __forceinline__ long long dbits(double x) { return __double_as_longlong(x); }
+
+// saturation threshold of an edge, as bits: max(rf, rb) * 2^-30 (0 below 2^-992)
+__device__ __forceinline__ long long thr_bits(long long a, long long b) {
+  long long m = a > b ? a : b;
+  long long ex = m >> 52;
+  return ex <= 30 ? 0ll : m - (30ll << 52);
+}
+
+struct Graph {
+  int64_t n, ext[3], st[3];
+  int d;          // cut dimension
+  int64_t L;      // extent along d
+  int NH;         // height of s (= number of interior nodes + 2)
+  double* rf[3];
+  double* rb[3];
+  double* ex;
+  double* pamt;
+  int* h[2];
+  signed char* pdir;
+
+  __device__ __forceinline__ int64_t coord(int64_t u, int e) const {
+    return e == 0 ? u % ext[0] : e == 1 ? (u / ext[0]) % ext[1] : u / (ext[0] * ext[1]);
+  }
+  __device__ __forceinline__ int kind(int64_t u) const {  // 0 interior, 1 source, 2 sink
+    int64_t c = coord(u, d);
+    return c == 0 ? 1 : (c == L - 1 ? 2 : 0);
+  }
+  __device__ __forceinline__ bool nbr(int64_t u, int dir, int64_t& v) const {
+    const int e = dir >> 1;
+    const int64_t c = coord(u, e);
+    if (dir & 1) {
+      if (c + 1 >= ext[e]) return false;
+      v = u + st[e];
+    } else {
+      if (c == 0) return false;
+      v = u - st[e];
+    }
+    return true;
+  }
+  __device__ __forceinline__ int height(const int* hc, int64_t v) const {
+    int k = kind(v);
+    return k == 1 ? NH : (k == 2 ? 0 : hc[v]);
+  }
+  // residual u->v (and pointers to both arc residuals) for direction dir
+  __device__ __forceinline__ void arc(int64_t u, int64_t v, int dir, double*& ruv,
+                                      double*& rvu) const {
+    const int e = dir >> 1;
+    if (dir & 1) { ruv = &rf[e][u]; rvu = &rb[e][u]; }
+    else { ruv = &rb[e][v]; rvu = &rf[e][v]; }
+  }
+  __device__ __forceinline__ bool open(const double* ruv, const double* rvu) const {
+    long long a = dbits(*ruv), b = dbits(*rvu);
+    return a > thr_bits(a, b);
+  }
+};
+
+__device__ void global_relabel(const Graph& g, int* hc) {
+  for (int64_t u = threadIdx.x; u < g.n; u += blockDim.x)
+    if (g.kind(u) == 0) hc[u] = g.NH;
+  __syncthreads();
+  for (int level = 0; level < g.NH; ++level) {
+    int any = 0;
+    for (int64_t u = threadIdx.x; u < g.n; u += blockDim.x) {
+      if (g.kind(u) != 0 || hc[u] != g.NH) continue;
+      for (int dir = 0; dir < 6; ++dir) {
+        int64_t v;
+        if (!g.nbr(u, dir, v)) continue;
+        if (g.height(hc, v) != level) continue;
+        double *ruv, *rvu;
+        g.arc(u, v, dir, ruv, rvu);
+        if (g.open(ruv, rvu)) { hc[u] = level + 1; any = 1; break; }
+      }
+    }
+    if (!__syncthreads_or(any)) break;
+  }
+}
+
+__global__ void __launch_bounds__(CUT_THREADS) cut_kernel(const CutArgs a) {
+  extern __shared__ __align__(16) char smem[];
+  const int s_id = blockIdx.x;
+  const int r = blockIdx.y;
+  const CutSlab sl = a.slab[s_id];
+  Graph g;
+  g.ext[0] = sl.ext[0]; g.ext[1] = sl.ext[1]; g.ext[2] = sl.ext[2];
+  g.st[0] = 1; g.st[1] = g.ext[0]; g.st[2] = g.ext[0] * g.ext[1];
+  g.n = g.ext[0] * g.ext[1] * g.ext[2];
+  g.d = sl.dim;
+  g.L = g.ext[g.d];
+  g.NH = (int)(g.n / g.L * (g.L > 2 ? g.L - 2 : 0)) + 2;
+  const int64_t n = g.n;
+
+  char* base = a.scratch ? a.scratch + (int64_t)(blockIdx.y * gridDim.x + blockIdx.x) *
+                                           a.scratch_per_cta
+                         : smem;
+  double* dp = reinterpret_cast<double*>(base);
+  for (int e = 0; e < 3; ++e) { g.rf[e] = dp + (2 * e) * n; g.rb[e] = dp + (2 * e + 1) * n; }
+  g.ex = dp + 6 * n;
+  g.pamt = dp + 7 * n;
+  int* ip = reinterpret_cast<int*>(dp + 8 * n);
+  g.h[0] = ip;
+  g.h[1] = ip + n;
+  g.pdir = reinterpret_cast<signed char*>(ip + 2 * n);
+  float* Av = reinterpret_cast<float*>(g.pamt);  // A and B alias pamt during set-up
+  float* Bv = Av + n;                            // (8n bytes = pamt)
+  // ex holds nothing yet either; B needs n floats after A: pamt is n doubles = 2n floats
+
+  // ---- load A (simulation grid) and B (training image at the drawn pattern) ----
+  int64_t bstart = 0;
+  if (!a.A) {
+    const int64_t ri = a.rind[r];
+    if (ri < 0) {  // pick failed: no cut (status already set)
+      for (int64_t u = threadIdx.x; u < n; u += blockDim.x)
+        a.out[((int64_t)r * a.nslab + s_id) * a.slabmax + u] = 0;
+      return;
+    }
+    const int64_t rx = ri % a.dx, rr = ri / a.dx, ry = rr % a.dy, rz = rr / a.dy;
+    bstart = rx + a.tix * (ry + a.tiy * rz);
+  }
+  for (int64_t u = threadIdx.x; u < n; u += blockDim.x) {
+    const int64_t x = u % g.ext[0], y = (u / g.ext[0]) % g.ext[1], z = u / g.st[2];
+    if (a.A) {
+      Av[u] = a.A[u];
+      Bv[u] = a.B[u];
+    } else {
+      const int64_t lx = sl.off[0] + x, ly = sl.off[1] + y, lz = sl.off[2] + z;
+      Av[u] = a.sim[(int64_t)r * a.sim_rs + a.tile_start + lx + a.sx * (ly + a.sy * lz)];
+      Bv[u] = a.ti[bstart + lx + a.tix * (ly + a.tiy * lz)];
+    }
+  }
+  __syncthreads();
+
+  // ---- capacities (graphcut.jl:22-50) ----
+  const double EPS = 2.220446049250313e-16;  // eps(Float64) = 2^-52
+  for (int64_t u = threadIdx.x; u < n; u += blockDim.x) {
+    for (int e = 0; e < 3; ++e) {
+      const int64_t c = g.coord(u, e);
+      if (c + 1 >= g.ext[e]) continue;
+      const int64_t v = u + g.st[e];
+      const bool ok = c + 2 < g.ext[e];
+      const int64_t w = ok ? v + g.st[e] : v;
+      const float Du = fabsf(__fsub_rn(Av[u], Bv[u]));
+      const float Dv = fabsf(__fsub_rn(Av[v], Bv[v]));
+      const float gAu = fabsf(__fsub_rn(Av[v], Av[u]));
+      const float gBu = fabsf(__fsub_rn(Bv[v], Bv[u]));
+      const float gAv = ok ? fabsf(__fsub_rn(Av[w], Av[v])) : gAu;
+      const float gBv = ok ? fabsf(__fsub_rn(Bv[w], Bv[v])) : gBu;
+      const float num = __fadd_rn(Du, Dv);
+      float den = __fadd_rn(gAu, gAv);
+      den = __fadd_rn(den, gBu);
+      den = __fadd_rn(den, gBv);
+      const double cap = __ddiv_rn((double)num, __dadd_rn((double)den, EPS));
+      g.rf[e][u] = cap;
+      g.rb[e][u] = cap;
+    }
+  }
+  __syncthreads();
+
+  // ---- saturate the source slice: push c(s, v) into every interior node of slice 1 ----
+  for (int64_t u = threadIdx.x; u < n; u += blockDim.x) {
+    double e0 = 0.0;
+    if (g.kind(u) == 0 && g.coord(u, g.d) == 1) {
+      const int64_t sN = u - g.st[g.d];
+      const double c = g.rf[g.d][sN];
+      g.rf[g.d][sN] = 0.0;
+      g.rb[g.d][sN] = __dadd_rn(c, c);
+      e0 = c;
+    }
+    g.ex[u] = e0;
+    g.pdir[u] = -1;
+  }
+  __syncthreads();
+
+  int cur = 0;
+  if (g.L > 2) {
+    global_relabel(g, g.h[cur]);
+    int round = 0;
+    bool capped = false;
+    for (;;) {
+      int* hc = g.h[cur];
+      int* hn = g.h[cur ^ 1];
+      // push phase
+      for (int64_t u = threadIdx.x; u < n; u += blockDim.x) {
+        signed char pd = -1;
+        if (g.kind(u) == 0 && dbits(g.ex[u]) > 0 && hc[u] < g.NH) {
+          const int hu = hc[u];
+          for (int dir = 0; dir < 6; ++dir) {
+            int64_t v;
+            if (!g.nbr(u, dir, v)) continue;
+            if (hu != g.height(hc, v) + 1) continue;
+            double *ruv, *rvu;
+            g.arc(u, v, dir, ruv, rvu);
+            if (!g.open(ruv, rvu)) continue;
+            const double e = g.ex[u], rr = *ruv;
+            const double delta = dbits(e) < dbits(rr) ? e : rr;
+            *ruv = __dsub_rn(rr, delta);
+            *rvu = __dadd_rn(*rvu, delta);
+            g.ex[u] = __dsub_rn(e, delta);
+            g.pamt[u] = delta;
+            pd = (signed char)dir;
+            break;
+          }
+        }
+        g.pdir[u] = pd;
+      }
+      __syncthreads();
+      // gather + relabel phase
+      int active = 0;
+      for (int64_t u = threadIdx.x; u < n; u += blockDim.x) {
+        if (g.kind(u) != 0) continue;
+        double e = g.ex[u];
+        for (int dir = 0; dir < 6; ++dir) {
+          int64_t v;
+          if (!g.nbr(u, dir, v)) continue;
+          if (g.pdir[v] == (dir ^ 1) && g.kind(v) == 0) e = __dadd_rn(e, g.pamt[v]);
+        }
+        g.ex[u] = e;
+        int hu = hc[u];
+        int hnew = hu;
+        if (dbits(e) > 0 && hu < g.NH) {
+          bool adm = false;
+          int mh = 0x7fffffff;
+          for (int dir = 0; dir < 6; ++dir) {
+            int64_t v;
+            if (!g.nbr(u, dir, v)) continue;
+            double *ruv, *rvu;
+            g.arc(u, v, dir, ruv, rvu);
+            if (!g.open(ruv, rvu)) continue;
+            const int hv = g.height(hc, v);
+            if (hu == hv + 1) { adm = true; break; }
+            mh = min(mh, hv);
+          }
+          if (!adm) hnew = mh >= g.NH - 1 ? g.NH : mh + 1;
+        }
+        hn[u] = hnew;
+        if (dbits(e) > 0 && hnew < g.NH) active = 1;
+      }
+      active = __syncthreads_or(active);
+      cur ^= 1;
+      ++round;
+      if (!active) break;
+      if (round >= a.round_cap) { capped = true; break; }
+      if (round % GR_PERIOD == 0) {
+        global_relabel(g, g.h[cur]);
+        __syncthreads();
+      }
+    }
+    global_relabel(g, g.h[cur]);
+    __syncthreads();
+    if (capped && threadIdx.x == 0) iq_dev_fail(a.status, IQ_ERR_CUTCAP);
+  }
+
+  // ---- mask: not sink side ----
+  const int* hc = g.h[cur];
+  uint8_t* out = a.out + ((int64_t)r * a.nslab + s_id) * a.slabmax;
+  for (int64_t u = threadIdx.x; u < n; u += blockDim.x) {
+    const int k = g.kind(u);
+    int M = k == 1 ? 1 : (k == 2 ? 0 : (hc[u] >= g.NH ? 1 : 0));
+    out[u] = (uint8_t)(sl.next ? !M : M);
+  }
+}
+
+}  // namespace
+
+size_t iq_cut_scratch_bytes(int64_t nodes) {
+  // rf, rb (6n doubles), ex, pamt (2n doubles), two heights (2n ints), push dir (n bytes)
+  size_t b = (size_t)nodes * (8 * 8 + 2 * 4 + 1);
+  return (b + 255) & ~(size_t)255;
+}
+
+int iq_launch_cut(iq_ctx* ctx, const CutLaunch& L) {
+  if (L.nslab <= 0 || L.nreal <= 0) return IQ_OK;
+  CutArgs a;
+  for (int i = 0; i < 6; ++i) a.slab[i] = L.slab[i];
+  a.nslab = L.nslab;
+  a.sim = L.sim; a.sx = L.sim_dims.x; a.sy = L.sim_dims.y; a.sim_rs = L.sim_rstride;
+  a.tile_start = L.tile_start;
+  a.ti = L.ti; a.tix = L.ti_dims.x; a.tiy = L.ti_dims.y;
+  a.dx = L.dist_dims.x; a.dy = L.dist_dims.y;
+  a.rind = L.rind;
+  a.A = L.A; a.B = L.B;
+  a.out = L.out; a.slabmax = L.slabmax;
+  a.status = L.status;
+  a.round_cap = L.round_cap;
+  int64_t nmax = 0;
+  for (int i = 0; i < L.nslab; ++i)
+    nmax = std::max<int64_t>(nmax, L.slab[i].ext[0] * L.slab[i].ext[1] * L.slab[i].ext[2]);
+  const size_t need = iq_cut_scratch_bytes(nmax);
+  static int smem_limit = -1;
+  if (smem_limit < 0) {
+    int dev = 0, v = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    smem_limit = v;
+    cudaFuncSetAttribute(cut_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, v);
+  }
+  size_t dyn = 0;
+  if ((int64_t)need <= smem_limit) {
+    a.scratch = nullptr;
+    a.scratch_per_cta = 0;
+    dyn = need;
+  } else {
+    if (!L.scratch || L.scratch_per_cta < (int64_t)need)
+      return iq_set_error(IQ_ERR_LIMIT, "graph cut slab of %lld nodes needs global scratch",
+                          (long long)nmax);
+    a.scratch = (char*)L.scratch;
+    a.scratch_per_cta = L.scratch_per_cta;
+  }
+  dim3 grid((unsigned)L.nslab, (unsigned)L.nreal);
+  iq_timer_start(ctx, "graphcut");
+  cut_kernel<<<grid, CUT_THREADS, dyn, ctx->stream>>>(a);
+  iq_timer_stop(ctx, "graphcut");
+  IQ_CUDA_OK(cudaGetLastError());
+  return IQ_OK;
+}

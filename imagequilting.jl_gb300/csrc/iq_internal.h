@@ -1,0 +1,210 @@
+// Internal declarations shared by the translation units of libiqgpu.so.
+#pragma once
+
+#include <map>
+#include <string>
+#include <vector>
+
+#include "iq_common.cuh"
+
+// ---------------------------------------------------------------------------------------
+// Context
+// ---------------------------------------------------------------------------------------
+struct IqTimer {
+  std::vector<cudaEvent_t> ev;  // start/stop pairs
+  size_t used = 0;              // pairs recorded
+};
+
+struct iq_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  // resident training image
+  bool has_ti = false;
+  int ndim = 0;
+  Dim3 ti{1, 1, 1};
+  float* d_ti = nullptr;       // prepared TI, NaN -> 0 (float32)
+  double* d_ti2ii = nullptr;   // integral image of TI^2, (x+1)(y+1)(z+1) doubles
+  int32_t* d_nanii = nullptr;  // integral image of the NaN indicator
+  int64_t ti_nan = 0;          // number of NaN voxels
+  int* d_status = nullptr;     // device status word (first kernel error)
+  // grow-only scratch buffers, by slot
+  std::vector<void*> buf;
+  std::vector<size_t> buf_bytes;
+  // profiling
+  bool prof = false;
+  std::map<std::string, IqTimer> timers;
+};
+
+// scratch slot ids
+enum IqSlot {
+  S_SIM = 0, S_CUT, S_D, S_DHARD, S_SOFT, S_TV, S_B2, S_KLIST, S_MINMAX, S_PICK_CAND,
+  S_PICK_K0, S_PICK_V0, S_PICK_K1, S_PICK_V1, S_PICK_W, S_PICK_PROD, S_RIND, S_NCAND,
+  S_CUTBUF, S_CUTSCR, S_DIS, S_AUX, S_AUXTI, S_AUXII, S_HARDLIST, S_HARDPTS, S_OUT,
+  S_TMP0, S_TMP1, S_TMP2, S_STARTS, S_SOFTTV, S_SOFTB2, S_VOX, S_COUNT
+};
+
+// device scratch of at least `bytes` in slot `slot` (contents undefined); nullptr on failure
+void* iq_scratch(iq_ctx* ctx, int slot, size_t bytes);
+
+// ---------------------------------------------------------------------------------------
+// Timing helpers (no-ops unless ctx->prof)
+// ---------------------------------------------------------------------------------------
+void iq_timer_start(iq_ctx* ctx, const char* name);
+void iq_timer_stop(iq_ctx* ctx, const char* name);
+
+// ---------------------------------------------------------------------------------------
+// Distance (iq_distance.cu)
+// ---------------------------------------------------------------------------------------
+// Packed template offset: kx | ky << 10 | kz << 20 (each < 1024).
+IQ_HD uint32_t kpack(int64_t kx, int64_t ky, int64_t kz) {
+  return (uint32_t)kx | ((uint32_t)ky << 10) | ((uint32_t)kz << 20);
+}
+IQ_HD int kx_of(uint32_t k) { return (int)(k & 1023u); }
+IQ_HD int ky_of(uint32_t k) { return (int)((k >> 10) & 1023u); }
+IQ_HD int kz_of(uint32_t k) { return (int)(k >> 20); }
+
+// A^2 term of the distance: either the integral-image box difference (full tile minus an
+// inner box [lo, hi)), or summed directly over the offset list.
+struct A2Spec {
+  const double* ii = nullptr;  // integral image of img^2; nullptr => direct accumulation
+  int64_t tile[3] = {0, 0, 0};
+  int64_t lo[3] = {0, 0, 0};   // inner (excluded) box; empty when lo >= hi in some dim
+  int64_t hi[3] = {0, 0, 0};
+};
+
+struct CorrLaunch {
+  const float* img = nullptr;  // image, extents `img_dims`
+  Dim3 img_dims{1, 1, 1};
+  Dim3 out_dims{1, 1, 1};      // valid extent
+  int K = 0;                   // offsets in the mask
+  const uint32_t* klist = nullptr;  // K packed offsets
+  const float* tv = nullptr;   // K x rpad template values (weights applied)
+  int rpad = 0;                // row length of tv (multiple of the register tile)
+  int ntmpl = 0;               // templates actually computed (<= rpad)
+  const double* b2 = nullptr;  // per template: sum of squared template values
+  A2Spec a2;
+  const uint8_t* disabled = nullptr;  // 1 -> +Inf (nullable)
+  float* out = nullptr;        // ntmpl x P
+  int64_t out_stride = 0;      // floats between templates in `out`
+  unsigned* minmax = nullptr;  // per template: [min bits, max finite bits] (nullable)
+};
+
+int iq_launch_corr(iq_ctx* ctx, const CorrLaunch& L);
+
+// gather of template values tv[k][t] = grid_t[start_t + k] for the packed offsets
+struct GatherLaunch {
+  const float* grid = nullptr;  // base grid
+  Dim3 grid_dims{1, 1, 1};
+  int64_t grid_stride = 0;      // floats between consecutive templates' grids
+  const int64_t* starts = nullptr;  // per template start (linear), device; nullable
+  int64_t start0 = 0;           // start when `starts` is null
+  int K = 0;
+  const uint32_t* klist = nullptr;
+  const float* kval = nullptr;  // per-offset values instead of a grid (hard data); nullable
+  int ntmpl = 0;
+  int rpad = 0;
+  float* tv = nullptr;          // K x rpad
+  double* b2 = nullptr;         // rpad
+  unsigned* minmax = nullptr;   // reset to [+Inf bits, 0] per template (nullable)
+};
+int iq_launch_gather(iq_ctx* ctx, const GatherLaunch& G);
+
+int iq_register_tile(int ntmpl);  // register tile width used for `ntmpl` templates
+
+// integral images and disabled windows
+int iq_build_integrals(iq_ctx* ctx, const float* d_img, Dim3 dims, double* d_sqii,
+                       int32_t* d_nanii, const uint8_t* d_nan);
+int iq_launch_disabled(iq_ctx* ctx, const int32_t* d_nanii, Dim3 dims, Dim3 tile, uint8_t* out);
+
+// ---------------------------------------------------------------------------------------
+// Pick (iq_pick.cu)
+// ---------------------------------------------------------------------------------------
+struct PickLaunch {
+  int64_t P = 0;           // positions
+  int64_t npat = 0;        // enabled positions (finite D)
+  double tol = 0.1;
+  uint64_t seed = 0;
+  int64_t tile = 0;        // tile linear index (Philox counter)
+  int64_t real0 = 0;       // realization index of CTA 0
+  int nreal = 0;           // CTAs
+  const float* D0 = nullptr;  int64_t D0_rstride = 0;  // primary source of CTA r
+  const unsigned* mm0 = nullptr; int64_t mm0_rstride = 0;  // its [min, max finite] bits
+  int naux = 0;
+  const float* aux[IQ_MAX_AUX] = {};
+  int64_t aux_rstride[IQ_MAX_AUX] = {};
+  // relaxation sizes (src/relaxation.jl:11-36): normal and all-zero cases
+  int64_t dbsize_norm = 0, dbsize_zero = 0;
+  int nseq_norm = 0, nseq_zero = 0;
+  int64_t seq_norm[IQ_MAX_SEQ] = {}, seq_zero[IQ_MAX_SEQ] = {};
+  // scratch, each nreal x P
+  int32_t* cand = nullptr;
+  uint32_t *k0 = nullptr, *v0 = nullptr, *k1 = nullptr, *v1 = nullptr;
+  double* w = nullptr;
+  double* prod = nullptr;
+  // outputs
+  int64_t* rind = nullptr;   // per CTA
+  int64_t* ncand = nullptr;  // per CTA (nullable)
+  int* status = nullptr;
+};
+int iq_launch_pick(iq_ctx* ctx, const PickLaunch& L);
+
+// ---------------------------------------------------------------------------------------
+// Graph cut (iq_graphcut.cu)
+// ---------------------------------------------------------------------------------------
+struct CutSlab {
+  int dim;          // cut dimension
+  int next;         // 0: overlap with the previous tile (keep M), 1: with the next (keep !M)
+  int64_t off[3];   // slab origin inside the tile
+  int64_t ext[3];   // slab extents
+};
+
+struct CutLaunch {
+  int nslab = 0;
+  CutSlab slab[6];
+  int nreal = 0;
+  // A: simulation grid of realization r at tile origin; B: TI at rind[r]
+  const float* sim = nullptr; Dim3 sim_dims{1, 1, 1}; int64_t sim_rstride = 0;
+  int64_t tile_start = 0;     // linear index of the tile origin in sim
+  const float* ti = nullptr;  Dim3 ti_dims{1, 1, 1};
+  Dim3 dist_dims{1, 1, 1};
+  const int64_t* rind = nullptr;
+  // direct mode (iq_graphcut): A/B arrays of the slab itself
+  const float* A = nullptr; const float* B = nullptr;
+  uint8_t* out = nullptr;      // nreal x nslab x slabmax bytes: keep-old flags
+  int64_t slabmax = 0;
+  void* scratch = nullptr;     // global scratch for slabs too large for shared memory
+  int64_t scratch_per_cta = 0;
+  int* status = nullptr;
+  int round_cap = 1 << 18;
+};
+int iq_launch_cut(iq_ctx* ctx, const CutLaunch& L);
+size_t iq_cut_scratch_bytes(int64_t nodes);
+
+// ---------------------------------------------------------------------------------------
+// Paste and finishing (iq_paste.cu)
+// ---------------------------------------------------------------------------------------
+struct PasteLaunch {
+  int nreal = 0;
+  float* sim = nullptr; Dim3 sim_dims{1, 1, 1}; int64_t sim_rstride = 0;
+  float* cut = nullptr;       // debug cut grid (nullable)
+  int64_t tile_start = 0;
+  Dim3 tile{1, 1, 1};
+  const float* ti = nullptr; Dim3 ti_dims{1, 1, 1}; Dim3 dist_dims{1, 1, 1};
+  const int64_t* rind = nullptr;
+  int nslab = 0;
+  CutSlab slab[6];
+  const uint8_t* cutbuf = nullptr; int64_t slabmax = 0;
+};
+int iq_launch_paste(iq_ctx* ctx, const PasteLaunch& L);
+
+int iq_launch_hard_overwrite(iq_ctx* ctx, int nreal, float* sim, float* cut, Dim3 sim_dims,
+                             int64_t sim_rstride, int64_t n, const int64_t* lin,
+                             const float* val);
+int iq_launch_crop(iq_ctx* ctx, int nreal, const float* src, Dim3 src_dims, int64_t src_rstride,
+                   Dim3 out_dims, float* dst);
+int iq_launch_voxsum(iq_ctx* ctx, int nreal, const float* cut, int64_t n, int64_t rstride,
+                     double* out);
+int iq_launch_pad_symmetric(iq_ctx* ctx, const float* src, Dim3 src_dims, float* dst,
+                            Dim3 dst_dims);
+int iq_launch_prepare(iq_ctx* ctx, float* data, int64_t n, uint8_t* nanmask);
+int iq_launch_to_f32(iq_ctx* ctx, const double* src, float* dst, int64_t n);

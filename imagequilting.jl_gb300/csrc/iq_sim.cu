@@ -1,0 +1,665 @@
+// iq_simulate: the iqsim driver (src/iqsim.jl:50-315) on the GPU.
+//
+// All realizations of a call share the tile path (genpath runs once per call,
+// src/iqsim.jl:139), so every step processes one tile for the whole batch of realizations:
+//   gather templates -> batched overlap distance -> [hard distance] -> pick (one CTA per
+//   realization) -> graph cuts (one CTA per realization and slab) -> paste.
+// The hard and soft distance terms do not depend on the realization; the soft maps of all
+// tiles are computed up front in batches of 16 tiles and kept resident in HBM, the hard map
+// of a data tile is computed once per step. Nothing is copied back to the host until the
+// crop at the end.
+#include <math.h>
+#include <string.h>
+
+#include <algorithm>
+#include <cmath>
+#include <unordered_map>
+#include <vector>
+
+#include "iq_internal.h"
+
+// ---------------------------------------------------------------------------------------
+// host helpers
+// ---------------------------------------------------------------------------------------
+namespace {
+
+struct PathStream {
+  uint64_t seed;
+  uint32_t i = 0;
+  explicit PathStream(uint64_t s) : seed(s) {}
+  uint64_t below(uint64_t m) {
+    uint64_t v = iq_rand64(seed, i++, 0u, 2u);
+    return (uint64_t)(((unsigned __int128)v * m) >> 64);
+  }
+  void shuffle(std::vector<int64_t>& a) {
+    for (int64_t i2 = (int64_t)a.size() - 1; i2 > 0; --i2) {
+      int64_t j = (int64_t)below((uint64_t)i2 + 1);
+      std::swap(a[i2], a[j]);
+    }
+  }
+};
+
+struct Grid3 {
+  int64_t e[3];
+  int64_t vol() const { return e[0] * e[1] * e[2]; }
+};
+
+// 3^N box dilation of a boolean grid (outside = false)
+std::vector<uint8_t> dilate(const std::vector<uint8_t>& g, const Grid3& d) {
+  std::vector<uint8_t> o(g.size(), 0);
+  for (int64_t z = 0; z < d.e[2]; ++z)
+    for (int64_t y = 0; y < d.e[1]; ++y)
+      for (int64_t x = 0; x < d.e[0]; ++x) {
+        uint8_t v = 0;
+        for (int64_t dz = -1; dz <= 1 && !v; ++dz)
+          for (int64_t dy = -1; dy <= 1 && !v; ++dy)
+            for (int64_t dx = -1; dx <= 1 && !v; ++dx) {
+              int64_t X = x + dx, Y = y + dy, Z = z + dz;
+              if (X < 0 || Y < 0 || Z < 0 || X >= d.e[0] || Y >= d.e[1] || Z >= d.e[2]) continue;
+              v = g[X + d.e[0] * (Y + d.e[1] * Z)];
+            }
+        o[x + d.e[0] * (y + d.e[1] * z)] = v;
+      }
+  return o;
+}
+
+void dilation_rings(std::vector<uint8_t>& grid, const Grid3& d, std::vector<int64_t>& path) {
+  for (;;) {
+    bool all = true;
+    for (uint8_t v : grid) all = all && v;
+    if (all) break;
+    std::vector<uint8_t> dl = dilate(grid, d);
+    for (int64_t i = 0; i < (int64_t)dl.size(); ++i)
+      if (dl[i] && !grid[i]) path.push_back(i);
+    grid.swap(dl);
+  }
+}
+
+}  // namespace
+
+// genpath (src/utils.jl:158-204) with the Philox path stream
+static std::vector<int64_t> genpath_host(uint64_t seed, const Grid3& ext, int kind,
+                                         std::vector<int64_t> datainds) {
+  PathStream rs(seed);
+  const int64_t n = ext.vol();
+  std::vector<int64_t> path;
+  path.reserve(n);
+  if (datainds.empty()) {
+    if (kind == IQ_PATH_RASTER) {
+      for (int64_t i = 0; i < n; ++i) path.push_back(i);
+    } else if (kind == IQ_PATH_RANDOM) {
+      path.resize(n);
+      for (int64_t i = 0; i < n; ++i) path[i] = i;
+      rs.shuffle(path);
+    } else {
+      int64_t pivot = (int64_t)rs.below((uint64_t)n);
+      std::vector<uint8_t> grid(n, 0);
+      grid[pivot] = 1;
+      path.push_back(pivot);
+      dilation_rings(grid, ext, path);
+    }
+  } else {
+    rs.shuffle(datainds);
+    std::vector<uint8_t> grid(n, 0);
+    for (int64_t p : datainds) {
+      grid[p] = 1;
+      path.push_back(p);
+    }
+    dilation_rings(grid, ext, path);
+  }
+  return path;
+}
+
+extern "C" int iq_genpath(uint64_t seed, int32_t ndim, const int64_t* extent, int32_t kind,
+                          int64_t ndata, const int64_t* datainds, int64_t* path_out) {
+  if (ndim < 1 || ndim > 3 || !extent || !path_out || ndata < 0 || (ndata > 0 && !datainds))
+    return iq_set_error(IQ_ERR_ARG, "invalid argument");
+  if (kind < 0 || kind > 2) return iq_set_error(IQ_ERR_ARG, "invalid simulation path");
+  Grid3 g{{1, 1, 1}};
+  for (int d = 0; d < ndim; ++d) {
+    if (extent[d] <= 0) return iq_set_error(IQ_ERR_ARG, "extents must be positive");
+    g.e[d] = extent[d];
+  }
+  std::vector<int64_t> di(datainds, datainds + ndata);
+  for (int64_t v : di)
+    if (v < 0 || v >= g.vol()) return iq_set_error(IQ_ERR_ARG, "data tile index out of range");
+  std::vector<int64_t> p = genpath_host(seed, g, kind, di);
+  std::copy(p.begin(), p.end(), path_out);
+  return IQ_OK;
+}
+
+void iq_relax_sizes(int64_t npat, double tol, int64_t& dbnorm, int64_t& dbzero, int& nnorm,
+                    int64_t* seqnorm, int& nzero, int64_t* seqzero) {
+  auto seq = [&](int64_t dbsize, int64_t* out) {
+    int n = 0;
+    double frac = 0.1 * ((double)dbsize / (double)npat);
+    for (;;) {
+      out[n++] = (int64_t)std::ceil(frac * (double)npat);
+      if (frac >= 1.0 || n >= IQ_MAX_SEQ) break;
+      frac = std::min(frac + 0.1, 1.0);
+    }
+    return n;
+  };
+  dbnorm = (int64_t)std::ceil(tol * (double)npat);
+  dbzero = npat;
+  nnorm = seq(dbnorm, seqnorm);
+  nzero = seq(dbzero, seqzero);
+}
+
+// ---------------------------------------------------------------------------------------
+// iq_simulate
+// ---------------------------------------------------------------------------------------
+namespace {
+
+struct Geo {
+  int ndim;
+  int64_t tile[3], ovl[3], spacing[3], ntiles[3], pad[3], sim[3], dist[3];
+  int64_t ovlvol;
+  int64_t ntot;
+};
+
+struct MaskCfg {
+  int prev[3], next[3];
+  int64_t lo[3], hi[3];
+  int K;
+  int id;
+};
+
+#define RET_IF(rc_expr)              \
+  do {                               \
+    int rc_ = (rc_expr);             \
+    if (rc_) return rc_;             \
+  } while (0)
+
+}  // namespace
+
+extern "C" int iq_simulate(iq_ctx* ctx, const iq_sim_params* p, const iq_hard_data* hard,
+                           int32_t nsoft, const iq_soft_data* soft, float* reals, float* cuts,
+                           double* voxs) {
+  if (!ctx || !p || !reals) return iq_set_error(IQ_ERR_ARG, "null argument");
+  if (!ctx->has_ti) return iq_set_error(IQ_ERR_STATE, "no training image set");
+  IQ_CUDA_OK(cudaSetDevice(ctx->device));
+  const int N = p->ndim;
+  if (N != ctx->ndim) return iq_set_error(IQ_ERR_ARG, "ndim differs from the training image");
+  const int64_t TIe[3] = {ctx->ti.x, ctx->ti.y, ctx->ti.z};
+
+  // ---- sanity checks (src/iqsim.jl:68-89) ----
+  for (int d = 0; d < N; ++d)
+    if (!(p->tilesize[d] > 0 && p->tilesize[d] <= TIe[d]))
+      return iq_set_error(IQ_ERR_ARG, "invalid tile size");
+  for (int d = 0; d < N; ++d)
+    if (!(p->simsize[d] >= p->tilesize[d])) return iq_set_error(IQ_ERR_ARG, "invalid grid size");
+  for (int d = 0; d < N; ++d)
+    if (!(p->overlap[d] > 0 && p->overlap[d] < 1))
+      return iq_set_error(IQ_ERR_ARG, "overlaps must be in range (0,1)");
+  if (!(p->tol > 0 && p->tol <= 1)) return iq_set_error(IQ_ERR_ARG, "tolerance must be in range (0,1]");
+  if (p->path < 0 || p->path > 2) return iq_set_error(IQ_ERR_ARG, "invalid simulation path");
+  if (p->nreal <= 0) return iq_set_error(IQ_ERR_ARG, "invalid number of realizations");
+  if (nsoft < 0 || (nsoft > 0 && !soft)) return iq_set_error(IQ_ERR_ARG, "invalid soft data");
+  if (nsoft + 1 > IQ_MAX_AUX) return iq_set_error(IQ_ERR_LIMIT, "at most %d soft variables", IQ_MAX_AUX - 1);
+  for (int s = 0; s < nsoft; ++s) {
+    if (!soft[s].aux || !soft[s].auxti) return iq_set_error(IQ_ERR_ARG, "null soft data");
+    for (int d = 0; d < N; ++d)
+      if (!(soft[s].auxsize[d] >= p->simsize[d]))
+        return iq_set_error(IQ_ERR_ARG, "soft data size < grid size");
+  }
+  for (int d = 0; d < N; ++d)
+    if (p->tilesize[d] >= 1024) return iq_set_error(IQ_ERR_LIMIT, "tile extent >= 1024");
+
+  // ---- geometry (src/iqsim.jl:91-115) ----
+  Geo g;
+  g.ndim = N;
+  for (int d = 0; d < 3; ++d) {
+    if (d < N) {
+      g.tile[d] = p->tilesize[d];
+      g.ovl[d] = (int64_t)std::ceil(p->overlap[d] * (double)p->tilesize[d]);
+      g.spacing[d] = g.tile[d] - g.ovl[d];
+      g.sim[d] = p->simsize[d];
+      g.ntiles[d] = (int64_t)std::ceil((double)g.sim[d] / (double)std::max<int64_t>(g.spacing[d], 1));
+      g.pad[d] = g.ntiles[d] * (g.tile[d] - g.ovl[d]) + g.ovl[d];
+      if (g.pad[d] < g.sim[d])
+        return iq_set_error(IQ_ERR_ARG, "tiles with zero spacing cannot cover the grid");
+    } else {
+      g.tile[d] = 1; g.ovl[d] = 0; g.spacing[d] = 1; g.sim[d] = 1; g.ntiles[d] = 1; g.pad[d] = 1;
+    }
+    g.dist[d] = TIe[d] - g.tile[d] + 1;
+  }
+  {
+    int64_t a = 1, b = 1;
+    for (int d = 0; d < 3; ++d) { a *= g.pad[d]; b *= g.pad[d] - (g.ntiles[d] - 1) * g.ovl[d]; }
+    g.ovlvol = a - b;
+  }
+  g.ntot = g.ntiles[0] * g.ntiles[1] * g.ntiles[2];
+  const Dim3 padD{g.pad[0], g.pad[1], g.pad[2]};
+  const Dim3 tileD{g.tile[0], g.tile[1], g.tile[2]};
+  const Dim3 distD{g.dist[0], g.dist[1], g.dist[2]};
+  const Dim3 simD{g.sim[0], g.sim[1], g.sim[2]};
+  const int64_t padvol = padD.vol(), T = tileD.vol(), P = distD.vol(), simvol = simD.vol();
+  if (P >= ((int64_t)1 << 31)) return iq_set_error(IQ_ERR_LIMIT, "distance map above 2^31");
+  const int R = p->nreal;
+  cudaStream_t st = ctx->stream;
+
+  // ---- hard data (src/utils.jl:18-55,131-156) ----
+  int64_t nh = hard ? hard->n : 0;
+  std::vector<int64_t> hcoord(nh * N);
+  std::vector<double> hval(nh);
+  if (nh > 0) {
+    if (!hard->coords || !hard->values) return iq_set_error(IQ_ERR_ARG, "null hard data");
+    IQ_CUDA_OK(cudaMemcpy(hcoord.data(), hard->coords, sizeof(int64_t) * nh * N, cudaMemcpyDefault));
+    IQ_CUDA_OK(cudaMemcpy(hval.data(), hard->values, sizeof(double) * nh, cudaMemcpyDefault));
+    for (int64_t i = 0; i < nh; ++i)
+      for (int d = 0; d < N; ++d) {
+        if (hcoord[i * N + d] >= g.sim[d]) return iq_set_error(IQ_ERR_ARG, "hard data coordinates outside of grid");
+        if (hcoord[i * N + d] < 0) return iq_set_error(IQ_ERR_ARG, "hard data coordinates must be positive indices");
+      }
+  }
+  // unique coordinates (the reference's Dict): last one wins
+  std::unordered_map<int64_t, int64_t> hidx;
+  std::vector<int64_t> hlin;
+  std::vector<double> hv;
+  for (int64_t i = 0; i < nh; ++i) {
+    int64_t c[3] = {0, 0, 0};
+    for (int d = 0; d < N; ++d) c[d] = hcoord[i * N + d];
+    int64_t lin = c[0] + g.pad[0] * (c[1] + g.pad[1] * c[2]);
+    auto it = hidx.find(lin);
+    if (it == hidx.end()) {
+      hidx[lin] = (int64_t)hlin.size();
+      hlin.push_back(lin);
+      hv.push_back(hval[i]);
+    } else {
+      hv[it->second] = hval[i];
+    }
+  }
+  nh = (int64_t)hlin.size();
+  std::vector<int64_t> nan_cnt(g.ntot, 0);
+  std::vector<uint8_t> has_data(g.ntot, 0);
+  std::vector<std::vector<std::pair<uint32_t, float>>> tile_hard(g.ntot);
+  for (int64_t i = 0; i < nh; ++i) {
+    int64_t c[3] = {hlin[i] % g.pad[0], (hlin[i] / g.pad[0]) % g.pad[1], hlin[i] / (g.pad[0] * g.pad[1])};
+    int64_t lo[3], hi[3];
+    for (int d = 0; d < 3; ++d) {
+      // tiles t with t*spacing <= c < t*spacing + tile
+      const int64_t sp = std::max<int64_t>(g.spacing[d], 1);
+      const int64_t num = c[d] - g.tile[d] + 1;
+      lo[d] = num <= 0 ? 0 : (num + sp - 1) / sp;
+      hi[d] = std::min<int64_t>(c[d] / sp, g.ntiles[d] - 1);
+    }
+    const bool isn = std::isnan(hv[i]);
+    for (int64_t tz = lo[2]; tz <= hi[2]; ++tz)
+      for (int64_t ty = lo[1]; ty <= hi[1]; ++ty)
+        for (int64_t tx = lo[0]; tx <= hi[0]; ++tx) {
+          const int64_t sx = tx * g.spacing[0], sy = ty * g.spacing[1], sz = tz * g.spacing[2];
+          if (c[0] < sx || c[0] >= sx + g.tile[0] || c[1] < sy || c[1] >= sy + g.tile[1] ||
+              c[2] < sz || c[2] >= sz + g.tile[2])
+            continue;
+          const int64_t t = tx + g.ntiles[0] * (ty + g.ntiles[1] * tz);
+          if (isn) {
+            nan_cnt[t]++;
+          } else {
+            has_data[t] = 1;
+            tile_hard[t].push_back({kpack(c[0] - sx, c[1] - sy, c[2] - sz), (float)hv[i]});
+          }
+        }
+  }
+  std::vector<uint8_t> skipped(g.ntot, 0);
+  std::vector<int64_t> datainds;
+  for (int64_t t = 0; t < g.ntot; ++t) {
+    int64_t ti3[3] = {t % g.ntiles[0], (t / g.ntiles[0]) % g.ntiles[1], t / (g.ntiles[0] * g.ntiles[1])};
+    bool beyond = false;
+    for (int d = 0; d < 3; ++d) beyond = beyond || ti3[d] * g.spacing[d] >= g.sim[d];
+    if (beyond || nan_cnt[t] == T) skipped[t] = 1;
+    else if (has_data[t]) datainds.push_back(t);
+  }
+  // hard offsets of a tile in column-major order
+  for (auto& v : tile_hard)
+    std::sort(v.begin(), v.end(), [](const std::pair<uint32_t, float>& a,
+                                     const std::pair<uint32_t, float>& b) {
+      const uint32_t ra = (uint32_t)kz_of(a.first) << 20 | (uint32_t)ky_of(a.first) << 10 | (uint32_t)kx_of(a.first);
+      const uint32_t rb = (uint32_t)kz_of(b.first) << 20 | (uint32_t)ky_of(b.first) << 10 | (uint32_t)kx_of(b.first);
+      return ra < rb;
+    });
+
+  // ---- path (src/utils.jl:158-204) ----
+  Grid3 text{{g.ntiles[0], g.ntiles[1], g.ntiles[2]}};
+  std::vector<int64_t> path = genpath_host(p->seed, text, p->path, datainds);
+
+  // ---- disabled windows (src/utils.jl:115-129) ----
+  uint8_t* d_dis = (uint8_t*)iq_scratch(ctx, S_DIS, (size_t)P);
+  if (!d_dis) return IQ_ERR_ALLOC;
+  RET_IF(iq_launch_disabled(ctx, ctx->d_nanii, ctx->ti, tileD, d_dis));
+  int64_t npat = P;
+  if (ctx->ti_nan > 0) {
+    std::vector<uint8_t> hd(P);
+    IQ_CUDA_OK(cudaMemcpyAsync(hd.data(), d_dis, (size_t)P, cudaMemcpyDeviceToHost, st));
+    IQ_CUDA_OK(cudaStreamSynchronize(st));
+    for (uint8_t v : hd) npat -= v;
+  }
+
+  // ---- step plan: neighbour flags per step, distinct masks ----
+  struct Step { int64_t tile; int64_t start[3]; int cfg; bool hardtile; int nslab; CutSlab slab[6]; };
+  std::vector<Step> steps;
+  std::vector<MaskCfg> cfgs;
+  std::vector<uint8_t> pasted(g.ntot, 0);
+  for (int64_t ind : path) {
+    if (skipped[ind]) continue;
+    Step s;
+    s.tile = ind;
+    int64_t ti3[3] = {ind % g.ntiles[0], (ind / g.ntiles[0]) % g.ntiles[1], ind / (g.ntiles[0] * g.ntiles[1])};
+    MaskCfg m;
+    s.nslab = 0;
+    for (int d = 0; d < 3; ++d) {
+      s.start[d] = ti3[d] * g.spacing[d];
+      m.prev[d] = m.next[d] = 0;
+      if (d < N && g.ovl[d] > 1) {
+        int64_t pv[3] = {ti3[0], ti3[1], ti3[2]}, nx[3] = {ti3[0], ti3[1], ti3[2]};
+        pv[d] -= 1;
+        nx[d] += 1;
+        if (pv[d] >= 0 && pasted[pv[0] + g.ntiles[0] * (pv[1] + g.ntiles[1] * pv[2])]) m.prev[d] = 1;
+        if (nx[d] < g.ntiles[d] && pasted[nx[0] + g.ntiles[0] * (nx[1] + g.ntiles[1] * nx[2])]) m.next[d] = 1;
+      }
+      m.lo[d] = m.prev[d] ? g.ovl[d] : 0;
+      m.hi[d] = m.next[d] ? g.spacing[d] : g.tile[d];
+    }
+    for (int d = 0; d < 3; ++d) {
+      for (int side = 0; side < 2; ++side) {
+        if (!(side ? m.next[d] : m.prev[d])) continue;
+        CutSlab& c = s.slab[s.nslab++];
+        c.dim = d;
+        c.next = side;
+        for (int e = 0; e < 3; ++e) { c.off[e] = 0; c.ext[e] = g.tile[e]; }
+        c.off[d] = side ? g.spacing[d] : 0;
+        c.ext[d] = side ? g.tile[d] - g.spacing[d] : g.ovl[d];
+      }
+    }
+    // inner box volume (excluded from the mask)
+    int64_t inner = 1;
+    for (int d = 0; d < 3; ++d) inner *= std::max<int64_t>(m.hi[d] - m.lo[d], 0);
+    m.K = (int)(T - inner);
+    int id = -1;
+    for (auto& c : cfgs)
+      if (!memcmp(c.prev, m.prev, sizeof(m.prev)) && !memcmp(c.next, m.next, sizeof(m.next))) id = c.id;
+    if (id < 0) {
+      m.id = (int)cfgs.size();
+      cfgs.push_back(m);
+      id = m.id;
+    }
+    s.cfg = id;
+    s.hardtile = has_data[ind] != 0;
+    steps.push_back(s);
+    pasted[ind] = 1;
+  }
+  // offset lists: one block of T entries per mask configuration, plus the full tile
+  const int ncfg = (int)cfgs.size();
+  std::vector<uint32_t> klist((size_t)(ncfg + 1) * T);
+  for (int c = 0; c <= ncfg; ++c) {
+    int k = 0;
+    for (int64_t z = 0; z < g.tile[2]; ++z)
+      for (int64_t y = 0; y < g.tile[1]; ++y)
+        for (int64_t x = 0; x < g.tile[0]; ++x) {
+          bool in = true;
+          if (c < ncfg) {
+            const MaskCfg& m = cfgs[c];
+            const bool inner = x >= m.lo[0] && x < m.hi[0] && y >= m.lo[1] && y < m.hi[1] &&
+                               z >= m.lo[2] && z < m.hi[2];
+            in = !inner;
+          }
+          if (in) klist[(size_t)c * T + k++] = kpack(x, y, z);
+        }
+  }
+  // hard lists of data tiles
+  std::vector<int64_t> hoff(g.ntot + 1, 0);
+  for (int64_t t = 0; t < g.ntot; ++t) hoff[t + 1] = hoff[t] + (int64_t)tile_hard[t].size();
+  std::vector<uint32_t> hk(std::max<int64_t>(hoff[g.ntot], 1));
+  std::vector<float> hkv(std::max<int64_t>(hoff[g.ntot], 1));
+  for (int64_t t = 0; t < g.ntot; ++t)
+    for (size_t i = 0; i < tile_hard[t].size(); ++i) {
+      hk[hoff[t] + i] = tile_hard[t][i].first;
+      hkv[hoff[t] + i] = tile_hard[t][i].second;
+    }
+
+  // ---- device buffers ----
+  const int rt = iq_register_tile(R);
+  const int rpad = ((R + rt - 1) / rt) * rt;
+  const bool debug = p->debug != 0 && (cuts || voxs);
+  float* d_sim = (float*)iq_scratch(ctx, S_SIM, sizeof(float) * padvol * R);
+  float* d_cut = debug ? (float*)iq_scratch(ctx, S_CUT, sizeof(float) * padvol * R) : nullptr;
+  float* d_D = (float*)iq_scratch(ctx, S_D, sizeof(float) * P * R);
+  float* d_Dh = (float*)iq_scratch(ctx, S_DHARD, sizeof(float) * P);
+  // template values: the overlap batch (T x rpad), then the hard template (T x 1)
+  float* d_tv = (float*)iq_scratch(ctx, S_TV, sizeof(float) * T * (std::max(rpad, 16) + 1));
+  double* d_b2 = (double*)iq_scratch(ctx, S_B2, sizeof(double) * (std::max(rpad, 16) + 1));
+  uint32_t* d_kl = (uint32_t*)iq_scratch(ctx, S_KLIST, sizeof(uint32_t) * klist.size());
+  unsigned* d_mm = (unsigned*)iq_scratch(ctx, S_MINMAX, sizeof(unsigned) * 2 * (R + 1));
+  uint32_t* d_hk = (uint32_t*)iq_scratch(ctx, S_HARDLIST, sizeof(uint32_t) * hk.size());
+  float* d_hkv = (float*)iq_scratch(ctx, S_HARDPTS, sizeof(float) * hkv.size());
+  int32_t* d_cand = (int32_t*)iq_scratch(ctx, S_PICK_CAND, sizeof(int32_t) * P * R);
+  uint32_t* d_k0 = (uint32_t*)iq_scratch(ctx, S_PICK_K0, sizeof(uint32_t) * P * R);
+  uint32_t* d_v0 = (uint32_t*)iq_scratch(ctx, S_PICK_V0, sizeof(uint32_t) * P * R);
+  uint32_t* d_k1 = (uint32_t*)iq_scratch(ctx, S_PICK_K1, sizeof(uint32_t) * P * R);
+  uint32_t* d_v1 = (uint32_t*)iq_scratch(ctx, S_PICK_V1, sizeof(uint32_t) * P * R);
+  double* d_w = (double*)iq_scratch(ctx, S_PICK_W, sizeof(double) * P * R);
+  double* d_prod = (double*)iq_scratch(ctx, S_PICK_PROD, sizeof(double) * P * R);
+  int64_t* d_rind = (int64_t*)iq_scratch(ctx, S_RIND, sizeof(int64_t) * R);
+  int64_t* d_ncand = (int64_t*)iq_scratch(ctx, S_NCAND, sizeof(int64_t) * R);
+  int64_t slabmax = 1;
+  for (int d = 0; d < N; ++d) slabmax = std::max<int64_t>(slabmax, T / g.tile[d] * g.ovl[d]);
+  uint8_t* d_cutbuf = (uint8_t*)iq_scratch(ctx, S_CUTBUF, (size_t)R * 6 * slabmax);
+  if (!d_sim || (debug && !d_cut) || !d_D || !d_Dh || !d_tv || !d_b2 || !d_kl || !d_mm || !d_hk ||
+      !d_hkv || !d_cand || !d_k0 || !d_v0 || !d_k1 || !d_v1 || !d_w || !d_prod || !d_rind ||
+      !d_ncand || !d_cutbuf)
+    return IQ_ERR_ALLOC;
+  // global scratch for cut slabs that do not fit in shared memory
+  void* d_cutscr = nullptr;
+  int64_t cutscr_per = 0;
+  {
+    int dev = 0, lim = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&lim, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    if ((int64_t)iq_cut_scratch_bytes(slabmax) > lim) {
+      cutscr_per = (int64_t)iq_cut_scratch_bytes(slabmax);
+      d_cutscr = iq_scratch(ctx, S_CUTSCR, (size_t)cutscr_per * 6 * R);
+      if (!d_cutscr) return IQ_ERR_ALLOC;
+    }
+  }
+  IQ_CUDA_OK(cudaMemsetAsync(d_sim, 0, sizeof(float) * padvol * R, st));
+  if (debug) IQ_CUDA_OK(cudaMemsetAsync(d_cut, 0, sizeof(float) * padvol * R, st));
+  IQ_CUDA_OK(cudaMemcpyAsync(d_kl, klist.data(), sizeof(uint32_t) * klist.size(), cudaMemcpyHostToDevice, st));
+  IQ_CUDA_OK(cudaMemcpyAsync(d_hk, hk.data(), sizeof(uint32_t) * hk.size(), cudaMemcpyHostToDevice, st));
+  IQ_CUDA_OK(cudaMemcpyAsync(d_hkv, hkv.data(), sizeof(float) * hkv.size(), cudaMemcpyHostToDevice, st));
+  IQ_CUDA_OK(cudaMemsetAsync(ctx->d_status, 0, sizeof(int), st));
+
+  // ---- soft data: padded aux grids, auxTI integral images, per-tile distance maps ----
+  std::vector<float*> d_aux(nsoft), d_auxti(nsoft);
+  std::vector<double*> d_auxii(nsoft);
+  float* d_soft = nullptr;
+  std::vector<int64_t> slot_of(g.ntot, -1);
+  int64_t nslot = 0;
+  if (nsoft > 0) {
+    for (int64_t t = 0; t < g.ntot; ++t)
+      if (!skipped[t]) slot_of[t] = nslot++;
+    const int64_t tivol = ctx->ti.vol();
+    // one arena for all soft arrays
+    int64_t amax[3] = {1, 1, 1};
+    for (int s = 0; s < nsoft; ++s)
+      for (int d = 0; d < N; ++d) amax[d] = std::max(amax[d], std::max(soft[s].auxsize[d], g.pad[d]));
+    const int64_t auxvol = amax[0] * amax[1] * amax[2];
+    const int64_t iivol = (ctx->ti.x + 1) * (ctx->ti.y + 1) * (ctx->ti.z + 1);
+    float* a_aux = (float*)iq_scratch(ctx, S_AUX, sizeof(float) * auxvol * nsoft);
+    float* a_ti = (float*)iq_scratch(ctx, S_AUXTI, sizeof(float) * tivol * nsoft);
+    double* a_ii = (double*)iq_scratch(ctx, S_AUXII, sizeof(double) * iivol * nsoft);
+    float* a_raw = (float*)iq_scratch(ctx, S_TMP1, sizeof(float) * auxvol);
+    d_soft = (float*)iq_scratch(ctx, S_SOFT, sizeof(float) * P * nslot * nsoft);
+    int64_t* d_starts = (int64_t*)iq_scratch(ctx, S_STARTS, sizeof(int64_t) * (nslot + 16));
+    if (!a_aux || !a_ti || !a_ii || !a_raw || !d_soft || !d_starts) return IQ_ERR_ALLOC;
+    for (int s = 0; s < nsoft; ++s) {
+      Dim3 asz{1, 1, 1};
+      int64_t ae[3] = {1, 1, 1};
+      for (int d = 0; d < N; ++d) ae[d] = soft[s].auxsize[d];
+      asz = Dim3{ae[0], ae[1], ae[2]};
+      Dim3 psz{std::max(ae[0], g.pad[0]), std::max(ae[1], g.pad[1]), std::max(ae[2], g.pad[2])};
+      d_aux[s] = a_aux + auxvol * s;
+      d_auxti[s] = a_ti + tivol * s;
+      d_auxii[s] = a_ii + iivol * s;
+      IQ_CUDA_OK(cudaMemcpyAsync(a_raw, soft[s].aux, sizeof(float) * asz.vol(), cudaMemcpyDefault, st));
+      RET_IF(iq_launch_pad_symmetric(ctx, a_raw, asz, d_aux[s], psz));
+      IQ_CUDA_OK(cudaMemcpyAsync(d_auxti[s], soft[s].auxti, sizeof(float) * tivol, cudaMemcpyDefault, st));
+      RET_IF(iq_launch_prepare(ctx, d_auxti[s], tivol, nullptr));
+      RET_IF(iq_build_integrals(ctx, d_auxti[s], ctx->ti, d_auxii[s], nullptr, nullptr));
+      // per-tile soft distance maps, 16 tiles per launch
+      std::vector<int64_t> tl;
+      for (int64_t t = 0; t < g.ntot; ++t)
+        if (!skipped[t]) tl.push_back(t);
+      std::vector<int64_t> starts(tl.size());
+      for (size_t i = 0; i < tl.size(); ++i) {
+        const int64_t t = tl[i];
+        const int64_t sx = (t % g.ntiles[0]) * g.spacing[0];
+        const int64_t sy = ((t / g.ntiles[0]) % g.ntiles[1]) * g.spacing[1];
+        const int64_t sz = (t / (g.ntiles[0] * g.ntiles[1])) * g.spacing[2];
+        starts[i] = sx + psz.x * (sy + psz.y * sz);
+      }
+      IQ_CUDA_OK(cudaMemcpyAsync(d_starts, starts.data(), sizeof(int64_t) * starts.size(),
+                                 cudaMemcpyHostToDevice, st));
+      for (size_t b0 = 0; b0 < tl.size(); b0 += 16) {
+        const int nb = (int)std::min<size_t>(16, tl.size() - b0);
+        GatherLaunch G;
+        G.grid = d_aux[s]; G.grid_dims = psz; G.grid_stride = 0; G.starts = d_starts + b0;
+        G.K = (int)T; G.klist = d_kl + (size_t)ncfg * T; G.ntmpl = nb; G.rpad = 16;
+        G.tv = d_tv; G.b2 = d_b2;
+        RET_IF(iq_launch_gather(ctx, G));
+        CorrLaunch C;
+        C.img = d_auxti[s]; C.img_dims = ctx->ti; C.out_dims = distD; C.K = (int)T;
+        C.klist = d_kl + (size_t)ncfg * T; C.tv = d_tv; C.rpad = 16; C.ntmpl = nb; C.b2 = d_b2;
+        C.a2.ii = d_auxii[s];
+        C.a2.tile[0] = g.tile[0]; C.a2.tile[1] = g.tile[1]; C.a2.tile[2] = g.tile[2];
+        C.disabled = d_dis;
+        C.out = d_soft + ((int64_t)s * nslot + slot_of[tl[b0]]) * P;
+        C.out_stride = P;
+        RET_IF(iq_launch_corr(ctx, C));
+      }
+      IQ_CUDA_OK(cudaStreamSynchronize(st));  // `starts` is a host vector
+    }
+  }
+
+  // ---- the tile loop (src/iqsim.jl:172-285) ----
+  int64_t dbn = 0, dbz = 0;
+  int nsn = 0, nsz = 0;
+  int64_t seqn[IQ_MAX_SEQ], seqz[IQ_MAX_SEQ];
+  if (npat > 0) iq_relax_sizes(npat, p->tol, dbn, dbz, nsn, seqn, nsz, seqz);
+  unsigned* d_mmh = d_mm + 2 * R;
+  for (const Step& s : steps) {
+    const MaskCfg& m = cfgs[s.cfg];
+    const int64_t tstart = s.start[0] + padD.x * (s.start[1] + padD.y * s.start[2]);
+    // overlap distance of every realization
+    GatherLaunch G;
+    G.grid = d_sim; G.grid_dims = padD; G.grid_stride = padvol; G.start0 = tstart;
+    G.K = m.K; G.klist = d_kl + (size_t)s.cfg * T; G.ntmpl = R; G.rpad = rpad;
+    G.tv = d_tv; G.b2 = d_b2; G.minmax = d_mm;
+    RET_IF(iq_launch_gather(ctx, G));
+    CorrLaunch C;
+    C.img = ctx->d_ti; C.img_dims = ctx->ti; C.out_dims = distD; C.K = m.K;
+    C.klist = d_kl + (size_t)s.cfg * T; C.tv = d_tv; C.rpad = rpad; C.ntmpl = R; C.b2 = d_b2;
+    C.a2.ii = ctx->d_ti2ii;
+    for (int d = 0; d < 3; ++d) { C.a2.tile[d] = g.tile[d]; C.a2.lo[d] = m.lo[d]; C.a2.hi[d] = m.hi[d]; }
+    C.disabled = d_dis; C.out = d_D; C.out_stride = P; C.minmax = d_mm;
+    RET_IF(iq_launch_corr(ctx, C));
+    // hard distance of a data tile
+    if (s.hardtile) {
+      const int64_t h0 = hoff[s.tile], hn = hoff[s.tile + 1] - hoff[s.tile];
+      GatherLaunch H;
+      H.K = (int)hn; H.klist = d_hk + h0; H.kval = d_hkv + h0; H.ntmpl = 1; H.rpad = 1;
+      H.tv = d_tv + (size_t)T * rpad; H.b2 = d_b2 + rpad; H.minmax = d_mmh;
+      // tv/b2 regions past the overlap batch
+      RET_IF(iq_launch_gather(ctx, H));
+      CorrLaunch Ch;
+      Ch.img = ctx->d_ti; Ch.img_dims = ctx->ti; Ch.out_dims = distD; Ch.K = (int)hn;
+      Ch.klist = d_hk + h0; Ch.tv = H.tv; Ch.rpad = 1; Ch.ntmpl = 1; Ch.b2 = H.b2;
+      Ch.disabled = d_dis; Ch.out = d_Dh; Ch.out_stride = P; Ch.minmax = d_mmh;
+      RET_IF(iq_launch_corr(ctx, Ch));
+    }
+    // pick
+    PickLaunch L;
+    L.P = P; L.npat = npat; L.tol = p->tol; L.seed = p->seed; L.tile = s.tile; L.real0 = 0;
+    L.nreal = R;
+    int na = 0;
+    if (s.hardtile) {
+      L.D0 = d_Dh; L.D0_rstride = 0; L.mm0 = d_mmh; L.mm0_rstride = 0;
+      L.aux[na] = d_D; L.aux_rstride[na] = P; ++na;
+    } else {
+      L.D0 = d_D; L.D0_rstride = P; L.mm0 = d_mm; L.mm0_rstride = 2;
+    }
+    for (int q = 0; q < nsoft; ++q) {
+      L.aux[na] = d_soft + ((int64_t)q * nslot + slot_of[s.tile]) * P;
+      L.aux_rstride[na] = 0;
+      ++na;
+    }
+    L.naux = na;
+    L.dbsize_norm = dbn; L.dbsize_zero = dbz; L.nseq_norm = nsn; L.nseq_zero = nsz;
+    for (int q = 0; q < IQ_MAX_SEQ; ++q) { L.seq_norm[q] = q < nsn ? seqn[q] : 0; L.seq_zero[q] = q < nsz ? seqz[q] : 0; }
+    L.cand = d_cand; L.k0 = d_k0; L.v0 = d_v0; L.k1 = d_k1; L.v1 = d_v1; L.w = d_w; L.prod = d_prod;
+    L.rind = d_rind; L.ncand = d_ncand; L.status = ctx->d_status;
+    RET_IF(iq_launch_pick(ctx, L));
+    // boundary cuts
+    if (s.nslab > 0) {
+      CutLaunch K;
+      K.nslab = s.nslab;
+      for (int i = 0; i < s.nslab; ++i) K.slab[i] = s.slab[i];
+      K.nreal = R;
+      K.sim = d_sim; K.sim_dims = padD; K.sim_rstride = padvol; K.tile_start = tstart;
+      K.ti = ctx->d_ti; K.ti_dims = ctx->ti; K.dist_dims = distD; K.rind = d_rind;
+      K.out = d_cutbuf; K.slabmax = slabmax;
+      K.scratch = d_cutscr; K.scratch_per_cta = cutscr_per;
+      K.status = ctx->d_status;
+      RET_IF(iq_launch_cut(ctx, K));
+    }
+    // paste
+    PasteLaunch Pl;
+    Pl.nreal = R; Pl.sim = d_sim; Pl.sim_dims = padD; Pl.sim_rstride = padvol; Pl.cut = d_cut;
+    Pl.tile_start = tstart; Pl.tile = tileD; Pl.ti = ctx->d_ti; Pl.ti_dims = ctx->ti;
+    Pl.dist_dims = distD; Pl.rind = d_rind; Pl.nslab = s.nslab;
+    for (int i = 0; i < s.nslab; ++i) Pl.slab[i] = s.slab[i];
+    Pl.cutbuf = d_cutbuf; Pl.slabmax = slabmax;
+    RET_IF(iq_launch_paste(ctx, Pl));
+  }
+
+  // ---- voxel reuse, hard overwrite, crop (src/iqsim.jl:287-307) ----
+  double* d_vox = nullptr;
+  if (debug && voxs) {
+    d_vox = (double*)iq_scratch(ctx, S_VOX, sizeof(double) * R);
+    if (!d_vox) return IQ_ERR_ALLOC;
+    RET_IF(iq_launch_voxsum(ctx, R, d_cut, padvol, padvol, d_vox));
+  }
+  if (nh > 0) {
+    std::vector<float> hvf(nh);
+    for (int64_t i = 0; i < nh; ++i) hvf[i] = (float)hv[i];
+    int64_t* d_hl = (int64_t*)iq_scratch(ctx, S_TMP0, sizeof(int64_t) * nh);
+    float* d_hv = (float*)iq_scratch(ctx, S_TMP2, sizeof(float) * nh);
+    if (!d_hl || !d_hv) return IQ_ERR_ALLOC;
+    IQ_CUDA_OK(cudaMemcpyAsync(d_hl, hlin.data(), sizeof(int64_t) * nh, cudaMemcpyHostToDevice, st));
+    IQ_CUDA_OK(cudaMemcpyAsync(d_hv, hvf.data(), sizeof(float) * nh, cudaMemcpyHostToDevice, st));
+    RET_IF(iq_launch_hard_overwrite(ctx, R, d_sim, d_cut, padD, padvol, nh, d_hl, d_hv));
+    IQ_CUDA_OK(cudaStreamSynchronize(st));  // host vectors above go out of scope
+  }
+  float* d_out = (float*)iq_scratch(ctx, S_OUT, sizeof(float) * simvol * R);
+  if (!d_out) return IQ_ERR_ALLOC;
+  RET_IF(iq_launch_crop(ctx, R, d_sim, padD, padvol, simD, d_out));
+  IQ_CUDA_OK(cudaMemcpyAsync(reals, d_out, sizeof(float) * simvol * R, cudaMemcpyDefault, st));
+  if (debug && cuts) {
+    IQ_CUDA_OK(cudaStreamSynchronize(st));
+    RET_IF(iq_launch_crop(ctx, R, d_cut, padD, padvol, simD, d_out));
+    IQ_CUDA_OK(cudaMemcpyAsync(cuts, d_out, sizeof(float) * simvol * R, cudaMemcpyDefault, st));
+  }
+  std::vector<double> hvox(R, 0.0);
+  if (d_vox) IQ_CUDA_OK(cudaMemcpyAsync(hvox.data(), d_vox, sizeof(double) * R, cudaMemcpyDeviceToHost, st));
+  int status = 0;
+  IQ_CUDA_OK(cudaMemcpyAsync(&status, ctx->d_status, sizeof(int), cudaMemcpyDeviceToHost, st));
+  IQ_CUDA_OK(cudaStreamSynchronize(st));
+  if (d_vox)
+    for (int r = 0; r < R; ++r) {
+      double v = hvox[r] / (double)g.ovlvol;
+      IQ_CUDA_OK(cudaMemcpy(voxs + r, &v, sizeof(double), cudaMemcpyDefault));
+    }
+  if (status == IQ_ERR_NOPATTERN) return iq_set_error(status, "every training-image pattern is disabled");
+  if (status == IQ_ERR_CUTCAP) return iq_set_error(status, "graph cut hit its round limit");
+  if (status) return iq_set_error(status, "kernel status %d", status);
+  return IQ_OK;
+}

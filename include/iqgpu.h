@@ -1,0 +1,150 @@
+/*
+ * iqgpu.h -- C ABI of libiqgpu.so, the GB300 (sm_103a) image-quilting hot path.
+ *
+ * Drop-in boundary for ImageQuilting.jl v1.3.1. The reference has no FFI: its hot path is a
+ * set of Julia functions. Each entry point below replaces one of them; a Julia host binds
+ * them with `ccall` (imagequilting.jl_gb300/julia/IQGPU.jl), Python with ctypes.
+ *
+ * Conventions
+ *   - Arrays are column-major (Julia order, dim 1 fastest); extents are given per dim.
+ *   - Indices and coordinates are 0-based (Julia index minus one).
+ *   - Buffers may be host memory (pageable or pinned) or device memory of the context's
+ *     device: the library copies with cudaMemcpyDefault (unified addressing).
+ *   - Every call returns IQ_OK (0) or an IQ_ERR_* code; iq_last_error() gives the message
+ *     of the last failure on the calling thread. Calls on one context run in order on its
+ *     stream and return after their results are written (synchronous for the caller).
+ *   - One context per host thread; a context owns its device buffers.
+ */
+#ifndef IQGPU_H
+#define IQGPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define IQ_OK 0
+#define IQ_ERR_ARG 1       /* invalid argument (the reference's @assert failures) */
+#define IQ_ERR_CUDA 2      /* CUDA runtime error */
+#define IQ_ERR_ALLOC 3     /* device allocation failed */
+#define IQ_ERR_NOPATTERN 4 /* every training-image pattern is disabled */
+#define IQ_ERR_CUTCAP 5    /* graph cut hit its round limit */
+#define IQ_ERR_STATE 6     /* no training image set on the context */
+#define IQ_ERR_LIMIT 7     /* size beyond a stated maximum */
+
+#define IQ_F32 0
+#define IQ_F64 1
+
+#define IQ_PATH_RASTER 0
+#define IQ_PATH_DILATION 1
+#define IQ_PATH_RANDOM 2
+
+typedef struct iq_ctx iq_ctx;
+
+/* Keyword arguments of iqsim (src/iqsim.jl:50-63). */
+typedef struct iq_sim_params {
+  int32_t ndim;        /* 1, 2 or 3: dimension of the training image */
+  int64_t tilesize[3]; /* tile size */
+  int64_t simsize[3];  /* simulation grid size */
+  double overlap[3];   /* overlap fraction per dim, in (0,1) */
+  double tol;          /* relaxation tolerance in (0,1] */
+  int32_t path;        /* IQ_PATH_RASTER / _DILATION / _RANDOM */
+  int32_t nreal;       /* number of realizations */
+  int32_t debug;       /* nonzero: also write boundary cuts and voxel reuse */
+  uint64_t seed;       /* key of the Philox4x32-10 streams (path and draws) */
+} iq_sim_params;
+
+/* Hard data: the reference's Dict{CartesianIndex,Real} as a list of unique coordinates. */
+typedef struct iq_hard_data {
+  int64_t n;             /* number of data */
+  const int64_t* coords; /* n x ndim, 0-based, one row per datum */
+  const double* values;  /* n values; NaN marks an inactive voxel of the grid */
+} iq_hard_data;
+
+/* Soft data: one (aux, auxTI) pair of the reference's `soft` vector (src/iqsim.jl:77-82). */
+typedef struct iq_soft_data {
+  const float* aux;    /* auxiliary variable on the grid, extents auxsize (>= simsize) */
+  int64_t auxsize[3];
+  const float* auxti;  /* auxiliary variable on the training image, extents of the TI */
+} iq_soft_data;
+
+/* Version of this ABI (major * 10000 + minor * 100 + patch). */
+int iq_version(void);
+
+/* Message of the last failed call on this thread ("" if none). */
+const char* iq_last_error(void);
+
+/* Create a context on `device` with its own stream. */
+int iq_ctx_create(int device, iq_ctx** out);
+int iq_ctx_destroy(iq_ctx* ctx);
+
+/* Stream (cudaStream_t) the context launches on, for callers that time it. */
+void* iq_ctx_stream(iq_ctx* ctx);
+
+/*
+ * Upload the training image and keep it resident: prepare (src/utils.jl:96-102, NaN -> 0,
+ * Float32 on the device like the reference's GPU path src/utils.jl:59), its NaN mask and the
+ * Float64 integral image of its squares. dtype IQ_F32 or IQ_F64; NaN marks inactive voxels.
+ */
+int iq_set_ti(iq_ctx* ctx, const void* ti, int32_t dtype, int32_t ndim, const int64_t* size);
+
+/*
+ * The whole iqsim (src/iqsim.jl:50-315) on the resident training image.
+ *   reals : nreal x prod(simsize) floats (realization r at offset r*prod(simsize))
+ *   cuts  : nreal x prod(simsize) floats, or NULL (boundary cuts, needs p->debug)
+ *   voxs  : nreal doubles, or NULL (voxel reuse, needs p->debug)
+ * hard may be NULL; soft may be NULL when nsoft == 0.
+ */
+int iq_simulate(iq_ctx* ctx, const iq_sim_params* p, const iq_hard_data* hard, int32_t nsoft,
+                const iq_soft_data* soft, float* reals, float* cuts, double* voxs);
+
+/*
+ * fastdistance (src/utils.jl:5-13) of `ntmpl` templates against the resident TI:
+ *   out[t][p] = |sum_k w_k TI[p+k]^2 - 2 sum_k w_k tmpl_t[k] TI[p+k] + sum_k w_k tmpl_t[k]^2|
+ * tmpl: ntmpl x prod(tilesize) floats; weights: prod(tilesize) bytes (0/1) or NULL for all
+ * ones; out: ntmpl x prod(TIsize - tilesize + 1) floats. Windows that cover an inactive
+ * TI voxel get +Inf (src/iqsim.jl:207).
+ */
+int iq_fastdistance(iq_ctx* ctx, const int64_t* tilesize, int32_t ntmpl, const float* tmpl,
+                    const uint8_t* weights, float* out);
+
+/*
+ * Pattern pick of one tile (src/iqsim.jl:236-246): the threshold pick
+ * findall(D .<= (1+tol)*minimum(D)) when naux == 0, else relaxation(D, Ds, tol)
+ * (src/relaxation.jl:5-39); tau-model weights (src/taumodel.jl:5-45); the weighted draw with
+ * u from Philox(seed; tile, real). D and Ds[i] hold P floats each.
+ * out_index: drawn linear index; out_ncand: candidate count; out_cands (nullable, capacity
+ * cap): candidate indices ascending; out_weights (nullable, capacity cap): their weights.
+ */
+int iq_pick(iq_ctx* ctx, const float* D, int64_t P, int32_t naux, const float* const* Ds,
+            double tol, uint64_t seed, int64_t tile, int64_t real, int64_t* out_index,
+            int64_t* out_ncand, int64_t* out_cands, double* out_weights, int64_t cap);
+
+/*
+ * Minimum-error boundary cut (src/graphcut.jl:5-84) of two arrays of extents `size` along
+ * `dim` (0-based). mask[v] = 1 when voxel v stays on the source side (keeps A).
+ */
+int iq_graphcut(iq_ctx* ctx, const float* A, const float* B, int32_t ndim, const int64_t* size,
+                int32_t dim, uint8_t* mask);
+
+/* Windows of the resident TI that cover an inactive voxel (src/utils.jl:115-129). */
+int iq_finddisabled(iq_ctx* ctx, const int64_t* tilesize, uint8_t* out);
+
+/*
+ * Tile visiting order (src/utils.jl:158-204) over a grid of `extent` tiles: raster, random,
+ * dilation or, when ndata > 0, data-first dilation from the shuffled `datainds`.
+ * path_out receives prod(extent) 0-based linear tile indices.
+ */
+int iq_genpath(uint64_t seed, int32_t ndim, const int64_t* extent, int32_t kind, int64_t ndata,
+               const int64_t* datainds, int64_t* path_out);
+
+/* Per-kernel timing with CUDA events on the context stream (enable = 1 clears the totals). */
+int iq_profile(iq_ctx* ctx, int32_t enable);
+int iq_profile_get(iq_ctx* ctx, const char* kernel, double* ms_total, int64_t* launches);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* IQGPU_H */
