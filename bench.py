@@ -1,0 +1,431 @@
+"""Benchmark of the GB300 image-quilting path: simulated voxels/s.
+
+Default workload (N=1): the 3-D continuous configuration -- TI 100x100x50 Float32 lognormal
+(a seeded Gaussian field smoothed with sigma=(6,6,2) voxels, standardized, exponentiated),
+tile 24x24x12, overlap 1/4, tol 0.1, output 200x200x100, nreal 16, 500 hard data drawn from a
+second seeded realization of the same field, one soft variable (aux = that second
+realization smoothed with sigma=4, auxTI = the TI smoothed with sigma=4). A step is one
+complete iqsim call (16 realizations, 64M voxels).
+
+  value : voxels/s with inputs resident in HBM (TI uploaded before timing; hard and soft
+          data and the outputs in device memory), CUDA events on the library's stream
+  e2e   : the same through the C ABI with host buffers: TI upload, hard/soft upload and the
+          copy of the realizations back to the host inside the timed region
+  cpu_baseline / --impl reference : the CPU oracle (Float64, FFT correlation with scipy.fft
+          on all host cores, C Boykov-Kolmogorov cut) on a bounded sample of the same
+          workload: realization 0, the first tiles of the path, scaled to voxels/s
+N>1 (torchrun): every rank runs its own replica (weak scaling, no data-path collective).
+"""
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = ("simulated voxels/s on 1 GB300: plain vs BF16+learned-proposal form at "
+          "≥0.99 recall")
+
+
+# ---------------------------------------------------------------------------------------
+# synthetic workloads (seeded)
+# ---------------------------------------------------------------------------------------
+def gaussian_field(shape, sigma, seed):
+    import scipy.ndimage as ndi
+    rng = np.random.default_rng(seed)
+    f = ndi.gaussian_filter(rng.standard_normal(shape), sigma, mode="wrap")
+    return (f - f.mean()) / f.std()
+
+
+def workload(name):
+    import scipy.ndimage as ndi
+    if name == "cfg2":
+        ti = np.exp(gaussian_field((100, 100, 50), (6, 6, 2), 1)).astype(np.float32)
+        simsize = (200, 200, 100)
+        f2 = np.exp(gaussian_field(simsize, (6, 6, 2), 2)).astype(np.float32)
+        rng = np.random.default_rng(3)
+        pts = np.stack([rng.integers(0, s, 500) for s in simsize], axis=1)
+        hard = {}
+        for c in pts:
+            hard[tuple(int(v) for v in c)] = float(f2[tuple(c)])
+        aux = ndi.gaussian_filter(f2, 4).astype(np.float32)
+        auxti = ndi.gaussian_filter(ti, 4).astype(np.float32)
+        return dict(name="cfg2", ti=ti, tilesize=(24, 24, 12), simsize=simsize,
+                    overlap=(0.25, 0.25, 0.25), tol=0.1, nreal=16, hard=hard,
+                    soft=[(aux, auxti)], path="raster",
+                    desc="3-D continuous: TI 100x100x50 f32 lognormal, tile 24x24x12, "
+                         "overlap 1/4, tol 0.1, out 200x200x100, nreal 16, 500 hard, 1 soft")
+    if name == "cfg1":
+        f = gaussian_field((128, 128), 8, 1)
+        ti = (f > np.quantile(f, 0.6)).astype(np.float64)
+        return dict(name="cfg1", ti=ti, tilesize=(32, 32), simsize=(256, 256),
+                    overlap=(1 / 6, 1 / 6), tol=0.1, nreal=1, hard={}, soft=[],
+                    path="raster",
+                    desc="2-D binary: TI 128x128 f64, tile 32x32, overlap 1/6, tol 0.1, "
+                         "out 256x256, nreal 1")
+    raise ValueError(name)
+
+
+# ---------------------------------------------------------------------------------------
+# helpers
+# ---------------------------------------------------------------------------------------
+class Clocks:
+    """nvidia-smi clock/throttle samples taken during the timed region."""
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL,
+                                         text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return d, "measured"
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0}, "fallback"
+
+
+def profile_traffic(kernel, workload_name):
+    """dram bytes per launch of `kernel` from a committed ncu summary, if one exists."""
+    fn = os.path.join(ROOT, "profiles", "%s_%s.txt" % (kernel, workload_name))
+    if not os.path.exists(fn):
+        return None
+    for ln in open(fn):
+        if ln.startswith("dram_bytes_per_launch:"):
+            try:
+                return float(ln.split(":", 1)[1].split()[0])
+            except ValueError:
+                return None
+    return None
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        backend = "nccl" if torch.cuda.is_available() else "gloo"
+        dist.init_process_group(backend)
+        return dist, rank, world
+    return None, 0, 1
+
+
+def reduce_max(dist, value):
+    if dist is None:
+        return value
+    import torch
+    dev = "cuda" if torch.cuda.is_available() and dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([value], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+# ---------------------------------------------------------------------------------------
+# CPU oracle baseline (bounded sample)
+# ---------------------------------------------------------------------------------------
+def cpu_sample(W, budget_s=15.0, max_steps=None):
+    """Run the oracle on realization 0 for a bounded number of tiles; returns voxels/s
+    scaled from the fraction of tiles done, plus a description."""
+    from oracle import iqsim_oracle as O
+    workers = os.cpu_count()
+    simvol = int(np.prod(W["simsize"]))
+    geo = O.geometry(W["ti"].shape, W["tilesize"], W["simsize"], W["overlap"])
+    hg = O.hard_grid(W["hard"], geo.padsize)
+    skipped, _ = O.findskipped(hg, geo)
+    ntiles = int(np.prod(geo.ntiles)) - len(skipped)
+    # calibrate: time a few tiles, then size the sample to the budget
+    steps = max_steps
+    if steps is None:
+        t0 = time.perf_counter()
+        O.iqsim(W["ti"], W["tilesize"], W["simsize"], overlap=W["overlap"], soft=W["soft"],
+                hard=W["hard"], tol=W["tol"], path=W["path"], nreal=1, seed=0, method="fft",
+                workers=workers, max_steps=4)
+        per = (time.perf_counter() - t0) / 4
+        steps = int(max(4, min(ntiles, budget_s / max(per, 1e-6))))
+    t0 = time.perf_counter()
+    O.iqsim(W["ti"], W["tilesize"], W["simsize"], overlap=W["overlap"], soft=W["soft"],
+            hard=W["hard"], tol=W["tol"], path=W["path"], nreal=1, seed=0, method="fft",
+            workers=workers, max_steps=steps)
+    dt = time.perf_counter() - t0
+    vps = simvol * (steps / ntiles) / dt
+    return vps, steps, ntiles, dt, workers
+
+
+# ---------------------------------------------------------------------------------------
+# arms
+# ---------------------------------------------------------------------------------------
+def run_reference(args, W, dist, rank, world):
+    if rank != 0:
+        return
+    vals = []
+    for i in range(args.warmup + args.steps):
+        vps, steps, ntiles, dt, cores = cpu_sample(W, budget_s=args.cpu_budget)
+        if i >= args.warmup:
+            vals.append((vps, dt))
+    v = float(np.mean([x[0] for x in vals]))
+    ms = float(np.mean([x[1] for x in vals])) * 1e3
+    line = {"metric": METRIC, "value": v, "unit": "voxels/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "impl": "reference",
+            "data": "synthetic (seeded Gaussian fields)",
+            "config": {"workload": W["desc"], "global_batch": W["nreal"],
+                       "sample": "realization 0, first %d of %d tiles per step" % (steps, ntiles)},
+            "cpu_baseline": {"value": v, "unit": "voxels/s", "cores": cores, "kind": "port",
+                             "sample": "realization 0, first %d of %d tiles, scaled by the "
+                                       "tile fraction" % (steps, ntiles)},
+            "e2e": {"value": v, "unit": "voxels/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args, W, dist, rank, world):
+    import ctypes
+
+    import torch
+    from __graft_entry__ import _package
+    iq = _package()
+    from iqgpu import _lib
+    lib = _lib.load()
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(dev)
+    ctx = iq.Context(dev)
+    stream = torch.cuda.ExternalStream(ctx.stream, device=dev)
+    N = W["ti"].ndim
+    nreal = W["nreal"]
+    simvol = int(np.prod(W["simsize"]))
+    voxels = simvol * nreal
+
+    # host inputs (column-major)
+    ti_h = np.asfortranarray(W["ti"])
+    ti_dt = _lib.IQ_F32 if ti_h.dtype == np.float32 else _lib.IQ_F64
+    coords_h = np.array(list(W["hard"].keys()), dtype=np.int64).reshape(len(W["hard"]), N)
+    vals_h = np.array(list(W["hard"].values()), dtype=np.float64)
+    soft_h = [(np.asfortranarray(a, np.float32), np.asfortranarray(b, np.float32))
+              for a, b in W["soft"]]
+    out_h = np.empty(voxels, np.float32)
+    # device copies for the resident arm
+    coords_d = torch.from_numpy(coords_h).cuda(dev) if len(vals_h) else None
+    vals_d = torch.from_numpy(vals_h).cuda(dev) if len(vals_h) else None
+    soft_d = [(torch.from_numpy(np.ascontiguousarray(a.ravel(order="F"))).cuda(dev),
+               torch.from_numpy(np.ascontiguousarray(b.ravel(order="F"))).cuda(dev))
+              for a, b in soft_h]
+    out_d = torch.empty(voxels, dtype=torch.float32, device=dev)
+    torch.cuda.synchronize()
+
+    p = _lib.SimParams()
+    p.ndim = N
+    for d in range(N):
+        p.tilesize[d] = W["tilesize"][d]
+        p.simsize[d] = W["simsize"][d]
+        p.overlap[d] = W["overlap"][d]
+    p.tol = W["tol"]
+    p.path = _lib.PATHS[W["path"]]
+    p.nreal = nreal
+    p.debug = 0
+
+    def make_io(device):
+        if device:
+            hd = _lib.HardData(len(vals_h), coords_d.data_ptr() if coords_d is not None else None,
+                               vals_d.data_ptr() if vals_d is not None else None)
+            srcs = [(a.data_ptr(), b.data_ptr()) for a, b in soft_d]
+        else:
+            hd = _lib.HardData(len(vals_h), coords_h.ctypes.data if len(vals_h) else None,
+                               vals_h.ctypes.data if len(vals_h) else None)
+            srcs = [(a.ctypes.data, b.ctypes.data) for a, b in soft_h]
+        sd = (_lib.SoftData * max(len(srcs), 1))()
+        for i, (a, b) in enumerate(srcs):
+            sd[i].aux = a
+            sd[i].auxti = b
+            for d in range(3):
+                sd[i].auxsize[d] = soft_h[i][0].shape[d] if d < N else 1
+        return hd, sd
+
+    hd_dev, sd_dev = make_io(True)
+    hd_host, sd_host = make_io(False)
+    size = _lib.i64arr(ti_h.shape)
+
+    def step_resident(i):
+        p.seed = 1000 + 7919 * i + 104729 * rank
+        _lib.check(lib.iq_simulate(ctx.h, ctypes.byref(p), ctypes.byref(hd_dev), len(soft_d),
+                                   sd_dev if soft_d else None, out_d.data_ptr(), None, None))
+
+    def step_e2e(i):
+        p.seed = 1000 + 7919 * i + 104729 * rank
+        _lib.check(lib.iq_set_ti(ctx.h, ti_h.ctypes.data, ti_dt, N, size))
+        _lib.check(lib.iq_simulate(ctx.h, ctypes.byref(p), ctypes.byref(hd_host), len(soft_h),
+                                   sd_host if soft_h else None, out_h.ctypes.data, None, None))
+
+    # ---- resident arm ----
+    _lib.check(lib.iq_set_ti(ctx.h, ti_h.ctypes.data, ti_dt, N, size))
+    for i in range(args.warmup):
+        step_resident(i)
+    torch.cuda.synchronize()
+    barrier(dist)
+    clocks = Clocks(dev)
+    clocks.start()
+    time.sleep(0.3)
+    ctx.profile(True)
+    l0 = ctx.launches
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for i in range(args.steps):
+        step_resident(args.warmup + i)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    launches = ctx.launches - l0
+    ms = e0.elapsed_time(e1)
+    clk = clocks.stop()
+    prof = {k: ctx.profile_get(k) for k in ("corr", "pick", "graphcut", "paste")}
+    ctx.profile(False)
+    ms_max = reduce_max(dist, ms)
+    barrier(dist)
+
+    # ---- end-to-end arm (host buffers through the C ABI) ----
+    for i in range(max(1, args.warmup // 2)):
+        step_e2e(i)
+    torch.cuda.synchronize()
+    barrier(dist)
+    t0 = time.perf_counter()
+    e2 = torch.cuda.Event(enable_timing=True)
+    e3 = torch.cuda.Event(enable_timing=True)
+    e2.record(stream)
+    for i in range(args.steps):
+        step_e2e(args.warmup + i)
+    e3.record(stream)
+    torch.cuda.synchronize()
+    wall = (time.perf_counter() - t0) * 1e3
+    ms_e2e = max(e2.elapsed_time(e3), wall)
+    ms_e2e_max = reduce_max(dist, ms_e2e)
+    h2d = ti_h.nbytes + coords_h.nbytes + vals_h.nbytes + sum(a.nbytes + b.nbytes for a, b in soft_h)
+    d2h = out_h.nbytes
+
+    if rank != 0:
+        ctx.close()
+        return
+    value = voxels * args.steps * world / (ms_max / 1e3)
+    e2e_value = voxels * args.steps * world / (ms_e2e_max / 1e3)
+    peaks, peak_kind = measured_peaks()
+    shares = {k: v[0] for k, v in prof.items()}
+    dom = max(shares, key=lambda k: shares[k])
+    corr_ms, corr_n, corr_flops = prof["corr"]
+    roof = {"bound": "tensor", "kernel": "corr",
+            "achieved": (corr_flops / corr_n) / (corr_ms / corr_n / 1e3) / 1e12 if corr_n else None,
+            "peak": peaks.get("bf16_tflops"), "unit": "TFLOP/s",
+            "peak_kind": "%s (bf16 dense, burst)" % peak_kind,
+            "flops_per_launch": corr_flops / corr_n if corr_n else None,
+            "traffic": profile_traffic("corr", W["name"]),
+            "fp32_simt_peak_tflops_nominal": 2 * 152 * 128 * 2.07e9 / 1e12,
+            "note": "the correlation runs on the FP32 SIMT pipes in this version; frac is "
+                    "against the dense bf16 tensor peak"}
+    if roof["achieved"] is not None and roof["peak"]:
+        roof["frac"] = roof["achieved"] / roof["peak"]
+        roof["frac_of_fp32_simt_nominal"] = roof["achieved"] / roof["fp32_simt_peak_tflops_nominal"]
+    kernel_share = {k: {"ms": round(v[0], 3), "launches": v[1],
+                        "share_of_step": round(v[0] / ms, 4) if ms else None}
+                    for k, v in prof.items()}
+    cpu = None
+    if not args.no_cpu_baseline:
+        vps, steps, ntiles, dt, cores = cpu_sample(W, budget_s=args.cpu_budget)
+        cpu = {"value": vps, "unit": "voxels/s", "cores": cores, "kind": "port",
+               "sample": "realization 0, first %d of %d tiles (%.1f s), scaled by the tile "
+                         "fraction" % (steps, ntiles, dt)}
+    line = {"metric": METRIC, "value": value, "unit": "voxels/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_max / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded Gaussian fields)",
+            "config": {"workload": W["desc"], "global_batch": nreal * world,
+                       "voxels_per_step": voxels * world, "parallelism": "replicas x%d" % world,
+                       "l2": "working set > L2 (simulation grids 350 MB, soft maps 1.6 GB)",
+                       "form": "plain (FP32 direct correlation)"},
+            "roofline": roof, "dominant_kernel": dom, "kernels": kernel_share,
+            "cpu_baseline": cpu,
+            "e2e": {"value": e2e_value, "unit": "voxels/s", "h2d_bytes_per_step": int(h2d),
+                    "d2h_bytes_per_step": int(d2h), "ms_per_step": ms_e2e_max / args.steps},
+            "clocks": clk, "gpu_launches": int(launches)}
+    print(json.dumps(line), flush=True)
+    ctx.close()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="cfg2", choices=["cfg2", "cfg1"])
+    ap.add_argument("--cpu-budget", type=float, default=15.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    dist, rank, world = dist_setup()
+    W = workload(args.workload)
+    if args.impl == "reference":
+        run_reference(args, W, dist, rank, world)
+    else:
+        run_ours(args, W, dist, rank, world)
+    if dist is not None:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -72,7 +72,9 @@ SIGNATURES = {
                                   ctypes.c_int64, c_i64p, c_i64p]),
     "iq_profile": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32]),
     "iq_profile_get": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p,
-                                      ctypes.POINTER(ctypes.c_double), c_i64p]),
+                                      ctypes.POINTER(ctypes.c_double), c_i64p,
+                                      ctypes.POINTER(ctypes.c_double)]),
+    "iq_ctx_launches": (ctypes.c_int64, [ctypes.c_void_p]),
 }
 
 _lib = None

@@ -89,10 +89,17 @@ class Context:
         check(load().iq_profile(self.h, 1 if enable else 0))
 
     def profile_get(self, kernel):
+        """(milliseconds, launches, algorithmic work) of a kernel since profile(True)."""
         ms = ctypes.c_double()
         n = ctypes.c_int64()
-        check(load().iq_profile_get(self.h, kernel.encode(), ctypes.byref(ms), ctypes.byref(n)))
-        return ms.value, n.value
+        w = ctypes.c_double()
+        check(load().iq_profile_get(self.h, kernel.encode(), ctypes.byref(ms), ctypes.byref(n),
+                                    ctypes.byref(w)))
+        return ms.value, n.value, w.value
+
+    @property
+    def launches(self):
+        return int(load().iq_ctx_launches(self.h))
 
 
 def default_context():

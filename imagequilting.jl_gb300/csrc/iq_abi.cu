@@ -63,29 +63,33 @@ void iq_timer_start(iq_ctx* ctx, const char* name) {
   cudaEventRecord(t.ev[2 * t.used], ctx->stream);
 }
 
-void iq_timer_stop(iq_ctx* ctx, const char* name) {
+void iq_timer_stop(iq_ctx* ctx, const char* name, double work) {
   if (!ctx->prof) return;
   IqTimer& t = ctx->timers[name];
   cudaEventRecord(t.ev[2 * t.used + 1], ctx->stream);
   t.used++;
+  t.work += work;
 }
 
 extern "C" int iq_profile(iq_ctx* ctx, int32_t enable) {
   if (!ctx) return iq_set_error(IQ_ERR_ARG, "null context");
   cudaStreamSynchronize(ctx->stream);
-  for (auto& kv : ctx->timers) kv.second.used = 0;
+  for (auto& kv : ctx->timers) { kv.second.used = 0; kv.second.work = 0; }
   ctx->prof = enable != 0;
   return IQ_OK;
 }
 
+extern "C" int64_t iq_ctx_launches(iq_ctx* ctx) { return ctx ? ctx->launches : 0; }
+
 extern "C" int iq_profile_get(iq_ctx* ctx, const char* kernel, double* ms_total,
-                              int64_t* launches) {
+                              int64_t* launches, double* work) {
   if (!ctx || !kernel) return iq_set_error(IQ_ERR_ARG, "null argument");
   IQ_CUDA_OK(cudaStreamSynchronize(ctx->stream));
-  double ms = 0;
+  double ms = 0, wk = 0;
   int64_t n = 0;
   auto it = ctx->timers.find(kernel);
   if (it != ctx->timers.end()) {
+    wk = it->second.work;
     for (size_t i = 0; i < it->second.used; ++i) {
       float f = 0;
       cudaEventElapsedTime(&f, it->second.ev[2 * i], it->second.ev[2 * i + 1]);
@@ -95,6 +99,7 @@ extern "C" int iq_profile_get(iq_ctx* ctx, const char* kernel, double* ms_total,
   }
   if (ms_total) *ms_total = ms;
   if (launches) *launches = n;
+  if (work) *work = wk;
   return IQ_OK;
 }
 

@@ -345,7 +345,8 @@ int iq_launch_corr(iq_ctx* ctx, const CorrLaunch& L) {
     case 2: launch_corr_t<2, 8>(a, ctx->stream); break;
     default: launch_corr_t<1, 8>(a, ctx->stream); break;
   }
-  iq_timer_stop(ctx, "corr");
+  iq_timer_stop(ctx, "corr", 2.0 * (double)a.P * (double)a.K * (double)L.ntmpl);
+  iq_count(ctx);
   IQ_CUDA_OK(cudaGetLastError());
   return IQ_OK;
 }
@@ -367,6 +368,7 @@ int iq_launch_gather(iq_ctx* ctx, const GatherLaunch& G) {
   g.b2 = G.b2;
   g.minmax = G.minmax;
   gather_kernel<<<G.rpad, 256, 0, ctx->stream>>>(g);
+  iq_count(ctx);
   IQ_CUDA_OK(cudaGetLastError());
   return IQ_OK;
 }
@@ -381,6 +383,7 @@ int iq_build_integrals(iq_ctx* ctx, const float* d_img, Dim3 dims, double* d_sqi
     IQ_CUDA_OK(cudaMemsetAsync(d_sqii, 0, sizeof(double) * sx * sy * sz, ctx->stream));
     ii_fill_kernel<double><<<blocks, threads, 0, ctx->stream>>>(d_img, nullptr, dims.x, dims.y,
                                                                 dims.z, d_sqii, 0);
+    iq_count(ctx, 4);
     for (int ax = 0; ax < 3; ++ax) {
       int64_t nl = ax == 0 ? sy * sz : ax == 1 ? sx * sz : sx * sy;
       ii_scan_kernel<double><<<(int)((nl + 127) / 128), 128, 0, ctx->stream>>>(d_sqii, sx, sy,
@@ -391,6 +394,7 @@ int iq_build_integrals(iq_ctx* ctx, const float* d_img, Dim3 dims, double* d_sqi
     IQ_CUDA_OK(cudaMemsetAsync(d_nanii, 0, sizeof(int32_t) * sx * sy * sz, ctx->stream));
     ii_fill_kernel<int32_t><<<blocks, threads, 0, ctx->stream>>>(nullptr, d_nan, dims.x, dims.y,
                                                                  dims.z, d_nanii, 1);
+    iq_count(ctx, 4);
     for (int ax = 0; ax < 3; ++ax) {
       int64_t nl = ax == 0 ? sy * sz : ax == 1 ? sx * sz : sx * sy;
       ii_scan_kernel<int32_t><<<(int)((nl + 127) / 128), 128, 0, ctx->stream>>>(d_nanii, sx, sy,
@@ -408,6 +412,7 @@ int iq_launch_disabled(iq_ctx* ctx, const int32_t* d_nanii, Dim3 dims, Dim3 tile
   const int blocks = (int)std::min<int64_t>((P + 255) / 256, 4096);
   disabled_kernel<<<blocks, 256, 0, ctx->stream>>>(d_nanii, dims.x, dims.y, od.x, od.y, P, tile.x,
                                                    tile.y, tile.z, out);
+  iq_count(ctx);
   IQ_CUDA_OK(cudaGetLastError());
   return IQ_OK;
 }

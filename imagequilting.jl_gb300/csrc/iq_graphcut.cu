@@ -348,7 +348,13 @@ int iq_launch_cut(iq_ctx* ctx, const CutLaunch& L) {
   dim3 grid((unsigned)L.nslab, (unsigned)L.nreal);
   iq_timer_start(ctx, "graphcut");
   cut_kernel<<<grid, CUT_THREADS, dyn, ctx->stream>>>(a);
-  iq_timer_stop(ctx, "graphcut");
+  double edges = 0;
+  for (int i = 0; i < L.nslab; ++i) {
+    const int64_t* e = L.slab[i].ext;
+    edges += (double)((e[0] - 1) * e[1] * e[2] + e[0] * (e[1] - 1) * e[2] + e[0] * e[1] * (e[2] - 1));
+  }
+  iq_timer_stop(ctx, "graphcut", edges * L.nreal);
+  iq_count(ctx);
   IQ_CUDA_OK(cudaGetLastError());
   return IQ_OK;
 }

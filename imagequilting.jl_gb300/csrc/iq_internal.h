@@ -13,6 +13,7 @@
 struct IqTimer {
   std::vector<cudaEvent_t> ev;  // start/stop pairs
   size_t used = 0;              // pairs recorded
+  double work = 0;              // algorithmic work of the recorded launches
 };
 
 struct iq_ctx {
@@ -33,6 +34,7 @@ struct iq_ctx {
   // profiling
   bool prof = false;
   std::map<std::string, IqTimer> timers;
+  int64_t launches = 0;         // kernels launched by this context
 };
 
 // scratch slot ids
@@ -50,7 +52,9 @@ void* iq_scratch(iq_ctx* ctx, int slot, size_t bytes);
 // Timing helpers (no-ops unless ctx->prof)
 // ---------------------------------------------------------------------------------------
 void iq_timer_start(iq_ctx* ctx, const char* name);
-void iq_timer_stop(iq_ctx* ctx, const char* name);
+void iq_timer_stop(iq_ctx* ctx, const char* name, double work = 0);
+// count a kernel launch of this context
+inline void iq_count(iq_ctx* ctx, int n = 1) { ctx->launches += n; }
 
 // ---------------------------------------------------------------------------------------
 // Distance (iq_distance.cu)

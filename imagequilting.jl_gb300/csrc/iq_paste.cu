@@ -141,7 +141,8 @@ int iq_launch_paste(iq_ctx* ctx, const PasteLaunch& L) {
   dim3 grid(blocks_for(L.tile.vol(), 256, 64), (unsigned)L.nreal);
   iq_timer_start(ctx, "paste");
   paste_kernel<<<grid, 256, 0, ctx->stream>>>(a);
-  iq_timer_stop(ctx, "paste");
+  iq_timer_stop(ctx, "paste", 4.0 * (double)L.tile.vol() * L.nreal);
+  iq_count(ctx);
   IQ_CUDA_OK(cudaGetLastError());
   return IQ_OK;
 }
@@ -152,6 +153,7 @@ int iq_launch_hard_overwrite(iq_ctx* ctx, int nreal, float* sim, float* cut, Dim
   if (n <= 0) return IQ_OK;
   dim3 grid(blocks_for(n, 256, 1024), (unsigned)nreal);
   hard_kernel<<<grid, 256, 0, ctx->stream>>>(nreal, sim, cut, sim_rstride, n, lin, val);
+  iq_count(ctx);
   IQ_CUDA_OK(cudaGetLastError());
   return IQ_OK;
 }
@@ -161,6 +163,7 @@ int iq_launch_crop(iq_ctx* ctx, int nreal, const float* src, Dim3 src_dims, int6
   dim3 grid(blocks_for(out_dims.vol(), 256, 4096), (unsigned)nreal);
   crop_kernel<<<grid, 256, 0, ctx->stream>>>(src, src_dims.x, src_dims.y, src_rstride,
                                              out_dims.x, out_dims.y, out_dims.z, dst);
+  iq_count(ctx);
   IQ_CUDA_OK(cudaGetLastError());
   return IQ_OK;
 }
@@ -168,6 +171,7 @@ int iq_launch_crop(iq_ctx* ctx, int nreal, const float* src, Dim3 src_dims, int6
 int iq_launch_voxsum(iq_ctx* ctx, int nreal, const float* cut, int64_t n, int64_t rstride,
                      double* out) {
   voxsum_kernel<<<nreal, 1024, 0, ctx->stream>>>(cut, n, rstride, out);
+  iq_count(ctx);
   IQ_CUDA_OK(cudaGetLastError());
   return IQ_OK;
 }
@@ -176,18 +180,21 @@ int iq_launch_pad_symmetric(iq_ctx* ctx, const float* src, Dim3 src_dims, float*
                             Dim3 dst_dims) {
   pad_kernel<<<blocks_for(dst_dims.vol()), 256, 0, ctx->stream>>>(
       src, src_dims.x, src_dims.y, src_dims.z, dst, dst_dims.x, dst_dims.y, dst_dims.z);
+  iq_count(ctx);
   IQ_CUDA_OK(cudaGetLastError());
   return IQ_OK;
 }
 
 int iq_launch_prepare(iq_ctx* ctx, float* data, int64_t n, uint8_t* nanmask) {
   prepare_kernel<<<blocks_for(n), 256, 0, ctx->stream>>>(data, n, nanmask);
+  iq_count(ctx);
   IQ_CUDA_OK(cudaGetLastError());
   return IQ_OK;
 }
 
 int iq_launch_to_f32(iq_ctx* ctx, const double* src, float* dst, int64_t n) {
   to_f32_kernel<<<blocks_for(n), 256, 0, ctx->stream>>>(src, dst, n);
+  iq_count(ctx);
   IQ_CUDA_OK(cudaGetLastError());
   return IQ_OK;
 }

@@ -499,7 +499,8 @@ int iq_launch_pick(iq_ctx* ctx, const PickLaunch& L) {
   a.w = L.w; a.prod = L.prod; a.rind = L.rind; a.ncand = L.ncand; a.status = L.status;
   iq_timer_start(ctx, "pick");
   pick_kernel<<<L.nreal, PT, 0, ctx->stream>>>(a);
-  iq_timer_stop(ctx, "pick");
+  iq_timer_stop(ctx, "pick", 4.0 * (double)L.P * (double)(1 + L.naux) * (double)L.nreal);
+  iq_count(ctx);
   IQ_CUDA_OK(cudaGetLastError());
   return IQ_OK;
 }

@@ -139,9 +139,19 @@ int iq_finddisabled(iq_ctx* ctx, const int64_t* tilesize, uint8_t* out);
 int iq_genpath(uint64_t seed, int32_t ndim, const int64_t* extent, int32_t kind, int64_t ndata,
                const int64_t* datainds, int64_t* path_out);
 
-/* Per-kernel timing with CUDA events on the context stream (enable = 1 clears the totals). */
+/*
+ * Per-kernel timing with CUDA events on the context stream (enable = 1 clears the totals).
+ * iq_profile_get reports, for kernel "corr", "pick", "graphcut" or "paste": the summed
+ * event time, the launches, and the algorithmic work of those launches (corr: FLOPs of the
+ * masked correlation, 2 * positions * offsets * templates; pick: bytes of the distance maps it
+ * reads once; graphcut: lattice edges; paste: bytes written).
+ */
 int iq_profile(iq_ctx* ctx, int32_t enable);
-int iq_profile_get(iq_ctx* ctx, const char* kernel, double* ms_total, int64_t* launches);
+int iq_profile_get(iq_ctx* ctx, const char* kernel, double* ms_total, int64_t* launches,
+                   double* work);
+
+/* Kernels this context has launched since it was created. */
+int64_t iq_ctx_launches(iq_ctx* ctx);
 
 #ifdef __cplusplus
 }
