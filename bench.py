@@ -336,11 +336,17 @@ def run_ours(args, W, dist, rank, world):
     ms = e0.elapsed_time(e1)
     clk = clocks.stop()
     prof = {k: ctx.profile_get(k) for k in ("corr", "pick", "graphcut", "paste")}
+    counters = {k: ctx.profile_get(k) for k in ("graphcut.rounds", "graphcut.levels",
+                                                 "pick.iterations", "pick.candidates")}
+    counters = {k: {"mean": (v[2] / v[1]) if v[1] else None, "ctas": v[1]}
+                for k, v in counters.items()}
     ctx.profile(False)
     ms_max = reduce_max(dist, ms)
     barrier(dist)
 
     # ---- end-to-end arm (host buffers through the C ABI) ----
+    if args.no_e2e:
+        step_e2e = lambda i: None  # noqa: E731  (profiling runs: resident arm only)
     for i in range(max(1, args.warmup // 2)):
         step_e2e(i)
     torch.cuda.synchronize()
@@ -398,6 +404,7 @@ def run_ours(args, W, dist, rank, world):
                        "l2": "working set > L2 (simulation grids 350 MB, soft maps 1.6 GB)",
                        "form": "plain (FP32 direct correlation)"},
             "roofline": roof, "dominant_kernel": dom, "kernels": kernel_share,
+            "counters": counters,
             "cpu_baseline": cpu,
             "e2e": {"value": e2e_value, "unit": "voxels/s", "h2d_bytes_per_step": int(h2d),
                     "d2h_bytes_per_step": int(d2h), "ms_per_step": ms_e2e_max / args.steps},
@@ -415,6 +422,7 @@ def main():
     ap.add_argument("--workload", default="cfg2", choices=["cfg2", "cfg1"])
     ap.add_argument("--cpu-budget", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer arm")
     args = ap.parse_args()
     dist, rank, world = dist_setup()
     W = workload(args.workload)

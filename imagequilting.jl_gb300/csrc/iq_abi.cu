@@ -75,6 +75,7 @@ extern "C" int iq_profile(iq_ctx* ctx, int32_t enable) {
   if (!ctx) return iq_set_error(IQ_ERR_ARG, "null context");
   cudaStreamSynchronize(ctx->stream);
   for (auto& kv : ctx->timers) { kv.second.used = 0; kv.second.work = 0; }
+  cudaMemset(ctx->d_stats, 0, sizeof(unsigned long long) * ST_COUNT);
   ctx->prof = enable != 0;
   return IQ_OK;
 }
@@ -87,6 +88,20 @@ extern "C" int iq_profile_get(iq_ctx* ctx, const char* kernel, double* ms_total,
   IQ_CUDA_OK(cudaStreamSynchronize(ctx->stream));
   double ms = 0, wk = 0;
   int64_t n = 0;
+  // counters: "graphcut.rounds", "graphcut.levels" (work = total, launches = CTAs),
+  // "pick.iterations", "pick.candidates" (work = total, launches = CTAs)
+  const char* names[4] = {"graphcut.rounds", "graphcut.levels", "pick.iterations", "pick.candidates"};
+  const int idx[4][2] = {{ST_CUT_ROUNDS, ST_CUT_CTAS}, {ST_CUT_LEVELS, ST_CUT_CTAS},
+                         {ST_PICK_ITERS, ST_PICK_CTAS}, {ST_PICK_CAND, ST_PICK_CTAS}};
+  for (int i = 0; i < 4; ++i)
+    if (!strcmp(kernel, names[i])) {
+      unsigned long long h[ST_COUNT];
+      IQ_CUDA_OK(cudaMemcpy(h, ctx->d_stats, sizeof(h), cudaMemcpyDeviceToHost));
+      if (ms_total) *ms_total = 0;
+      if (launches) *launches = (int64_t)h[idx[i][1]];
+      if (work) *work = (double)h[idx[i][0]];
+      return IQ_OK;
+    }
   auto it = ctx->timers.find(kernel);
   if (it != ctx->timers.end()) {
     wk = it->second.work;
@@ -120,6 +135,13 @@ extern "C" int iq_ctx_create(int device, iq_ctx** out) {
     return iq_set_error(IQ_ERR_ALLOC, "status word allocation failed");
   }
   cudaMemset(c->d_status, 0, sizeof(int));
+  if (cudaMalloc(&c->d_stats, sizeof(unsigned long long) * ST_COUNT) != cudaSuccess) {
+    cudaFree(c->d_status);
+    cudaStreamDestroy(c->stream);
+    delete c;
+    return iq_set_error(IQ_ERR_ALLOC, "counter allocation failed");
+  }
+  cudaMemset(c->d_stats, 0, sizeof(unsigned long long) * ST_COUNT);
   *out = c;
   return IQ_OK;
 }
@@ -143,6 +165,7 @@ extern "C" int iq_ctx_destroy(iq_ctx* ctx) {
   for (auto& kv : ctx->timers)
     for (auto e : kv.second.ev) cudaEventDestroy(e);
   cudaFree(ctx->d_status);
+  cudaFree(ctx->d_stats);
   cudaStreamDestroy(ctx->stream);
   delete ctx;
   return IQ_OK;

@@ -35,6 +35,7 @@ struct CutArgs {
   char* scratch; int64_t scratch_per_cta;
   int* status;
   int round_cap;
+  unsigned long long* stats;
 };
 
 __device__ __forceinline__ long long dbits(double x) { return __double_as_longlong(x); }
@@ -47,9 +48,9 @@ __device__ __forceinline__ long long thr_bits(long long a, long long b) {
 }
 
 struct Graph {
-  int64_t n, ext[3], st[3];
+  int n, ext[3], st[3];
   int d;          // cut dimension
-  int64_t L;      // extent along d
+  int L;          // extent along d
   int NH;         // height of s (= number of interior nodes + 2)
   double* rf[3];
   double* rb[3];
@@ -57,33 +58,20 @@ struct Graph {
   double* pamt;
   int* h[2];
   signed char* pdir;
+  uint8_t* info;  // bits 0-5: neighbour exists in direction 0..5; bits 6-7: kind
 
-  __device__ __forceinline__ int64_t coord(int64_t u, int e) const {
-    return e == 0 ? u % ext[0] : e == 1 ? (u / ext[0]) % ext[1] : u / (ext[0] * ext[1]);
-  }
-  __device__ __forceinline__ int kind(int64_t u) const {  // 0 interior, 1 source, 2 sink
-    int64_t c = coord(u, d);
-    return c == 0 ? 1 : (c == L - 1 ? 2 : 0);
-  }
-  __device__ __forceinline__ bool nbr(int64_t u, int dir, int64_t& v) const {
-    const int e = dir >> 1;
-    const int64_t c = coord(u, e);
-    if (dir & 1) {
-      if (c + 1 >= ext[e]) return false;
-      v = u + st[e];
-    } else {
-      if (c == 0) return false;
-      v = u - st[e];
-    }
+  __device__ __forceinline__ int kind(int u) const { return info[u] >> 6; }  // 0 interior, 1 s, 2 t
+  __device__ __forceinline__ bool nbr(int u, int dir, int& v) const {
+    if (!(info[u] >> dir & 1)) return false;
+    v = (dir & 1) ? u + st[dir >> 1] : u - st[dir >> 1];
     return true;
   }
-  __device__ __forceinline__ int height(const int* hc, int64_t v) const {
+  __device__ __forceinline__ int height(const int* hc, int v) const {
     int k = kind(v);
     return k == 1 ? NH : (k == 2 ? 0 : hc[v]);
   }
   // residual u->v (and pointers to both arc residuals) for direction dir
-  __device__ __forceinline__ void arc(int64_t u, int64_t v, int dir, double*& ruv,
-                                      double*& rvu) const {
+  __device__ __forceinline__ void arc(int u, int v, int dir, double*& ruv, double*& rvu) const {
     const int e = dir >> 1;
     if (dir & 1) { ruv = &rf[e][u]; rvu = &rb[e][u]; }
     else { ruv = &rb[e][v]; rvu = &rf[e][v]; }
@@ -94,16 +82,16 @@ struct Graph {
   }
 };
 
-__device__ void global_relabel(const Graph& g, int* hc) {
-  for (int64_t u = threadIdx.x; u < g.n; u += blockDim.x)
+__device__ int global_relabel(const Graph& g, int* hc) {
+  for (int u = threadIdx.x; u < g.n; u += blockDim.x)
     if (g.kind(u) == 0) hc[u] = g.NH;
   __syncthreads();
   for (int level = 0; level < g.NH; ++level) {
     int any = 0;
-    for (int64_t u = threadIdx.x; u < g.n; u += blockDim.x) {
+    for (int u = threadIdx.x; u < g.n; u += blockDim.x) {
       if (g.kind(u) != 0 || hc[u] != g.NH) continue;
       for (int dir = 0; dir < 6; ++dir) {
-        int64_t v;
+        int v;
         if (!g.nbr(u, dir, v)) continue;
         if (g.height(hc, v) != level) continue;
         double *ruv, *rvu;
@@ -111,8 +99,9 @@ __device__ void global_relabel(const Graph& g, int* hc) {
         if (g.open(ruv, rvu)) { hc[u] = level + 1; any = 1; break; }
       }
     }
-    if (!__syncthreads_or(any)) break;
+    if (!__syncthreads_or(any)) return level + 1;
   }
+  return g.NH;
 }
 
 __global__ void __launch_bounds__(CUT_THREADS) cut_kernel(const CutArgs a) {
@@ -121,13 +110,13 @@ __global__ void __launch_bounds__(CUT_THREADS) cut_kernel(const CutArgs a) {
   const int r = blockIdx.y;
   const CutSlab sl = a.slab[s_id];
   Graph g;
-  g.ext[0] = sl.ext[0]; g.ext[1] = sl.ext[1]; g.ext[2] = sl.ext[2];
+  g.ext[0] = (int)sl.ext[0]; g.ext[1] = (int)sl.ext[1]; g.ext[2] = (int)sl.ext[2];
   g.st[0] = 1; g.st[1] = g.ext[0]; g.st[2] = g.ext[0] * g.ext[1];
   g.n = g.ext[0] * g.ext[1] * g.ext[2];
   g.d = sl.dim;
   g.L = g.ext[g.d];
-  g.NH = (int)(g.n / g.L * (g.L > 2 ? g.L - 2 : 0)) + 2;
-  const int64_t n = g.n;
+  g.NH = g.n / g.L * (g.L > 2 ? g.L - 2 : 0) + 2;
+  const int n = g.n;
 
   char* base = a.scratch ? a.scratch + (int64_t)(blockIdx.y * gridDim.x + blockIdx.x) *
                                            a.scratch_per_cta
@@ -140,6 +129,7 @@ __global__ void __launch_bounds__(CUT_THREADS) cut_kernel(const CutArgs a) {
   g.h[0] = ip;
   g.h[1] = ip + n;
   g.pdir = reinterpret_cast<signed char*>(ip + 2 * n);
+  g.info = reinterpret_cast<uint8_t*>(g.pdir + n);
   float* Av = reinterpret_cast<float*>(g.pamt);  // A and B alias pamt during set-up
   float* Bv = Av + n;                            // (8n bytes = pamt)
   // ex holds nothing yet either; B needs n floats after A: pamt is n doubles = 2n floats
@@ -156,8 +146,17 @@ __global__ void __launch_bounds__(CUT_THREADS) cut_kernel(const CutArgs a) {
     const int64_t rx = ri % a.dx, rr = ri / a.dx, ry = rr % a.dy, rz = rr / a.dy;
     bstart = rx + a.tix * (ry + a.tiy * rz);
   }
-  for (int64_t u = threadIdx.x; u < n; u += blockDim.x) {
-    const int64_t x = u % g.ext[0], y = (u / g.ext[0]) % g.ext[1], z = u / g.st[2];
+  for (int u = threadIdx.x; u < n; u += blockDim.x) {
+    const int x = u % g.ext[0], y = (u / g.ext[0]) % g.ext[1], z = u / g.st[2];
+    const int c[3] = {x, y, z};
+    uint8_t inf = 0;
+    for (int e = 0; e < 3; ++e) {
+      if (c[e] > 0) inf |= (uint8_t)(1u << (2 * e));
+      if (c[e] + 1 < g.ext[e]) inf |= (uint8_t)(1u << (2 * e + 1));
+    }
+    const int cd = c[g.d];
+    inf |= (uint8_t)((cd == 0 ? 1 : (cd == g.L - 1 ? 2 : 0)) << 6);
+    g.info[u] = inf;
     if (a.A) {
       Av[u] = a.A[u];
       Bv[u] = a.B[u];
@@ -171,13 +170,12 @@ __global__ void __launch_bounds__(CUT_THREADS) cut_kernel(const CutArgs a) {
 
   // ---- capacities (graphcut.jl:22-50) ----
   const double EPS = 2.220446049250313e-16;  // eps(Float64) = 2^-52
-  for (int64_t u = threadIdx.x; u < n; u += blockDim.x) {
+  for (int u = threadIdx.x; u < n; u += blockDim.x) {
     for (int e = 0; e < 3; ++e) {
-      const int64_t c = g.coord(u, e);
-      if (c + 1 >= g.ext[e]) continue;
-      const int64_t v = u + g.st[e];
-      const bool ok = c + 2 < g.ext[e];
-      const int64_t w = ok ? v + g.st[e] : v;
+      int v;
+      if (!g.nbr(u, 2 * e + 1, v)) continue;
+      const bool ok = (g.info[v] >> (2 * e + 1)) & 1;
+      const int w = ok ? v + g.st[e] : v;
       const float Du = fabsf(__fsub_rn(Av[u], Bv[u]));
       const float Dv = fabsf(__fsub_rn(Av[v], Bv[v]));
       const float gAu = fabsf(__fsub_rn(Av[v], Av[u]));
@@ -196,10 +194,10 @@ __global__ void __launch_bounds__(CUT_THREADS) cut_kernel(const CutArgs a) {
   __syncthreads();
 
   // ---- saturate the source slice: push c(s, v) into every interior node of slice 1 ----
-  for (int64_t u = threadIdx.x; u < n; u += blockDim.x) {
+  for (int u = threadIdx.x; u < n; u += blockDim.x) {
     double e0 = 0.0;
-    if (g.kind(u) == 0 && g.coord(u, g.d) == 1) {
-      const int64_t sN = u - g.st[g.d];
+    if (g.kind(u) == 0 && g.kind(u - g.st[g.d]) == 1) {
+      const int sN = u - g.st[g.d];
       const double c = g.rf[g.d][sN];
       g.rf[g.d][sN] = 0.0;
       g.rb[g.d][sN] = __dadd_rn(c, c);
@@ -211,20 +209,20 @@ __global__ void __launch_bounds__(CUT_THREADS) cut_kernel(const CutArgs a) {
   __syncthreads();
 
   int cur = 0;
+  int round = 0, levels = 0;
   if (g.L > 2) {
-    global_relabel(g, g.h[cur]);
-    int round = 0;
+    levels += global_relabel(g, g.h[cur]);
     bool capped = false;
     for (;;) {
       int* hc = g.h[cur];
       int* hn = g.h[cur ^ 1];
       // push phase
-      for (int64_t u = threadIdx.x; u < n; u += blockDim.x) {
+      for (int u = threadIdx.x; u < n; u += blockDim.x) {
         signed char pd = -1;
         if (g.kind(u) == 0 && dbits(g.ex[u]) > 0 && hc[u] < g.NH) {
           const int hu = hc[u];
           for (int dir = 0; dir < 6; ++dir) {
-            int64_t v;
+            int v;
             if (!g.nbr(u, dir, v)) continue;
             if (hu != g.height(hc, v) + 1) continue;
             double *ruv, *rvu;
@@ -245,11 +243,11 @@ __global__ void __launch_bounds__(CUT_THREADS) cut_kernel(const CutArgs a) {
       __syncthreads();
       // gather + relabel phase
       int active = 0;
-      for (int64_t u = threadIdx.x; u < n; u += blockDim.x) {
+      for (int u = threadIdx.x; u < n; u += blockDim.x) {
         if (g.kind(u) != 0) continue;
         double e = g.ex[u];
         for (int dir = 0; dir < 6; ++dir) {
-          int64_t v;
+          int v;
           if (!g.nbr(u, dir, v)) continue;
           if (g.pdir[v] == (dir ^ 1) && g.kind(v) == 0) e = __dadd_rn(e, g.pamt[v]);
         }
@@ -260,7 +258,7 @@ __global__ void __launch_bounds__(CUT_THREADS) cut_kernel(const CutArgs a) {
           bool adm = false;
           int mh = 0x7fffffff;
           for (int dir = 0; dir < 6; ++dir) {
-            int64_t v;
+            int v;
             if (!g.nbr(u, dir, v)) continue;
             double *ruv, *rvu;
             g.arc(u, v, dir, ruv, rvu);
@@ -280,19 +278,24 @@ __global__ void __launch_bounds__(CUT_THREADS) cut_kernel(const CutArgs a) {
       if (!active) break;
       if (round >= a.round_cap) { capped = true; break; }
       if (round % GR_PERIOD == 0) {
-        global_relabel(g, g.h[cur]);
+        levels += global_relabel(g, g.h[cur]);
         __syncthreads();
       }
     }
-    global_relabel(g, g.h[cur]);
+    levels += global_relabel(g, g.h[cur]);
     __syncthreads();
     if (capped && threadIdx.x == 0) iq_dev_fail(a.status, IQ_ERR_CUTCAP);
   }
 
+  if (a.stats && threadIdx.x == 0) {
+    atomicAdd(a.stats + ST_CUT_ROUNDS, (unsigned long long)round);
+    atomicAdd(a.stats + ST_CUT_LEVELS, (unsigned long long)levels);
+    atomicAdd(a.stats + ST_CUT_CTAS, 1ull);
+  }
   // ---- mask: not sink side ----
   const int* hc = g.h[cur];
   uint8_t* out = a.out + ((int64_t)r * a.nslab + s_id) * a.slabmax;
-  for (int64_t u = threadIdx.x; u < n; u += blockDim.x) {
+  for (int u = threadIdx.x; u < n; u += blockDim.x) {
     const int k = g.kind(u);
     int M = k == 1 ? 1 : (k == 2 ? 0 : (hc[u] >= g.NH ? 1 : 0));
     out[u] = (uint8_t)(sl.next ? !M : M);
@@ -302,8 +305,9 @@ __global__ void __launch_bounds__(CUT_THREADS) cut_kernel(const CutArgs a) {
 }  // namespace
 
 size_t iq_cut_scratch_bytes(int64_t nodes) {
-  // rf, rb (6n doubles), ex, pamt (2n doubles), two heights (2n ints), push dir (n bytes)
-  size_t b = (size_t)nodes * (8 * 8 + 2 * 4 + 1);
+  // rf, rb (6n doubles), ex, pamt (2n doubles), two heights (2n ints), push dir and node
+  // info (2n bytes)
+  size_t b = (size_t)nodes * (8 * 8 + 2 * 4 + 2);
   return (b + 255) & ~(size_t)255;
 }
 
@@ -321,6 +325,7 @@ int iq_launch_cut(iq_ctx* ctx, const CutLaunch& L) {
   a.out = L.out; a.slabmax = L.slabmax;
   a.status = L.status;
   a.round_cap = L.round_cap;
+  a.stats = L.stats;
   int64_t nmax = 0;
   for (int i = 0; i < L.nslab; ++i)
     nmax = std::max<int64_t>(nmax, L.slab[i].ext[0] * L.slab[i].ext[1] * L.slab[i].ext[2]);

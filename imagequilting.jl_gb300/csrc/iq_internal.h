@@ -35,7 +35,12 @@ struct iq_ctx {
   bool prof = false;
   std::map<std::string, IqTimer> timers;
   int64_t launches = 0;         // kernels launched by this context
+  // device counters filled while profiling: [0] cut rounds, [1] cut BFS levels, [2] cut CTAs,
+  // [3] pick relaxation iterations, [4] pick candidates, [5] pick CTAs
+  unsigned long long* d_stats = nullptr;
 };
+enum IqStat { ST_CUT_ROUNDS = 0, ST_CUT_LEVELS, ST_CUT_CTAS, ST_PICK_ITERS, ST_PICK_CAND,
+              ST_PICK_CTAS, ST_COUNT };
 
 // scratch slot ids
 enum IqSlot {
@@ -149,6 +154,7 @@ struct PickLaunch {
   int64_t* rind = nullptr;   // per CTA
   int64_t* ncand = nullptr;  // per CTA (nullable)
   int* status = nullptr;
+  unsigned long long* stats = nullptr;  // profiling counters (nullable)
 };
 int iq_launch_pick(iq_ctx* ctx, const PickLaunch& L);
 
@@ -180,6 +186,7 @@ struct CutLaunch {
   int64_t scratch_per_cta = 0;
   int* status = nullptr;
   int round_cap = 1 << 18;
+  unsigned long long* stats = nullptr;  // profiling counters (nullable)
 };
 int iq_launch_cut(iq_ctx* ctx, const CutLaunch& L);
 size_t iq_cut_scratch_bytes(int64_t nodes);

@@ -40,6 +40,7 @@ struct PickArgs {
   int64_t* rind;
   int64_t* ncand;
   int* status;
+  unsigned long long* stats;
 };
 
 struct Smem {
@@ -107,12 +108,31 @@ __device__ unsigned long long block_sum_u64(Smem& s, unsigned long long v) {
   return r;
 }
 
-// Warp-aggregated increment of s.hist[d] (valid lanes only).
-__device__ __forceinline__ void hist_add(Smem& s, bool valid, uint32_t d) {
+// Histograms are counted per warp (s.wcnt[warp][digit], one leader per distinct digit of a
+// warp after __match_any_sync) and summed into s.hist: no two warps touch the same counter,
+// which matters because float bit patterns pile into a few high-order digits.
+__device__ __forceinline__ void whist_zero(Smem& s) {
+  for (int i = threadIdx.x; i < NW * 256; i += PT) (&s.wcnt[0][0])[i] = 0;
+  __syncthreads();
+}
+
+__device__ __forceinline__ void whist_add(Smem& s, bool valid, uint32_t d) {
   const int lane = threadIdx.x & 31;
   uint32_t key = valid ? d : (0x10000u + lane);
   uint32_t peers = __match_any_sync(0xffffffffu, key);
-  if (valid && lane == __ffs(peers) - 1) atomicAdd(&s.hist[d], (uint32_t)__popc(peers));
+  if (valid && lane == __ffs(peers) - 1)
+    atomicAdd(&s.wcnt[threadIdx.x >> 5][d], (uint32_t)__popc(peers));
+}
+
+__device__ __forceinline__ void whist_reduce(Smem& s) {
+  __syncthreads();
+  for (int d = threadIdx.x; d < 256; d += PT) {
+    uint32_t t = 0;
+#pragma unroll 8
+    for (int w = 0; w < NW; ++w) t += s.wcnt[w][d];
+    s.hist[d] = t;
+  }
+  __syncthreads();
 }
 
 // Bucket holding the kk-th (1-based) element of s.hist; sets s.sel, s.cnt, s.kk (rank
@@ -162,15 +182,15 @@ __device__ Key select_kth(Smem& s, const float* __restrict__ src, int64_t P, int
   const int64_t iters = (P + PT - 1) / PT;
   uint32_t cnt_eq = 0;
   for (int shift = 24; shift >= 0; shift -= 8) {
-    for (int i = threadIdx.x; i < 256; i += PT) s.hist[i] = 0;
-    __syncthreads();
+    whist_zero(s);
     for (int64_t it = 0; it < iters; ++it) {
       int64_t p = it * PT + threadIdx.x;
       bool valid = p < P;
       uint32_t b = valid ? fbits(src[p]) : 0u;
       valid = valid && (b & mask) == prefix;
-      hist_add(s, valid, (b >> shift) & 255u);
+      whist_add(s, valid, (b >> shift) & 255u);
     }
+    whist_reduce(s);
     find_bucket(s, kk);
     prefix |= s.sel << shift;
     mask |= 255u << shift;
@@ -184,15 +204,15 @@ __device__ Key select_kth(Smem& s, const float* __restrict__ src, int64_t P, int
   while (topbit < 31 && ((int64_t)1 << (topbit + 1)) <= P - 1) ++topbit;
   uint32_t ip = 0, im = 0;
   for (int shift = (topbit / 8) * 8; shift >= 0; shift -= 8) {
-    for (int i = threadIdx.x; i < 256; i += PT) s.hist[i] = 0;
-    __syncthreads();
+    whist_zero(s);
     for (int64_t it = 0; it < iters; ++it) {
       int64_t p = it * PT + threadIdx.x;
       bool valid = p < P;
       uint32_t b = valid ? fbits(src[p]) : 0u;
       valid = valid && b == prefix && ((uint32_t)p & im) == ip;
-      hist_add(s, valid, ((uint32_t)p >> shift) & 255u);
+      whist_add(s, valid, ((uint32_t)p >> shift) & 255u);
     }
+    whist_reduce(s);
     find_bucket(s, kk);
     ip |= s.sel << shift;
     im |= 255u << shift;
@@ -246,15 +266,6 @@ __device__ int64_t compact(Smem& s, const Pred& pred, int64_t P, int32_t* out) {
   return base;
 }
 
-// Any position satisfying pred?
-template <typename Pred>
-__device__ bool any_of(const Pred& pred, int64_t P) {
-  int hit = 0;
-  for (int64_t p = threadIdx.x; p < P; p += PT)
-    if (!hit && pred(p)) hit = 1;
-  return __syncthreads_or(hit) != 0;
-}
-
 // Stable LSD radix sort of (keys, vals)[0..n) between the buffer pairs; returns 0 if the
 // result is in (ka, va), 1 if in (kb, vb).
 __device__ int radix_sort(Smem& s, uint32_t* ka, uint32_t* va, uint32_t* kb, uint32_t* vb,
@@ -265,15 +276,14 @@ __device__ int radix_sort(Smem& s, uint32_t* ka, uint32_t* va, uint32_t* kb, uin
   for (int shift = 0; shift < 32; shift += 8) {
     uint32_t* ks = cur ? kb : ka; uint32_t* vs = cur ? vb : va;
     uint32_t* kd = cur ? ka : kb; uint32_t* vd = cur ? va : vb;
-    for (int i = threadIdx.x; i < 256; i += PT) s.hist[i] = 0;
-    __syncthreads();
+    whist_zero(s);
     for (int64_t t = 0; t < ntiles; ++t) {
       int64_t i = t * PT + threadIdx.x;
       bool valid = i < n;
       uint32_t d = valid ? (ks[i] >> shift) & 255u : 0u;
-      hist_add(s, valid, d);
+      whist_add(s, valid, d);
     }
-    __syncthreads();
+    whist_reduce(s);
     // single-bucket pass: order unchanged, skip it
     int single = 0;
     if (threadIdx.x < 256 && (int64_t)s.hist[threadIdx.x] == n) single = 1;
@@ -409,22 +419,29 @@ __global__ void __launch_bounds__(PT) pick_kernel(const PickArgs a) {
     pr.naux = a.naux;
     for (int j = 0; j < a.naux; ++j) pr.aux[j] = aux[j];
     pr.kD = select_kth(s, D, P, dbsize);
-    for (int q = 0; q < nseq; ++q) {
+    n = 0;
+    int q = 0;
+    for (; q < nseq && n == 0; ++q) {
       const int64_t sz = allzero ? a.seq_zero[q] : a.seq_norm[q];
       for (int j = 0; j < a.naux; ++j) {
         if (sz >= P) pr.ka[j] = Key{0xFFFFFFFFu, 0xFFFFFFFFu};
         else if (sz <= 0) pr.ka[j] = Key{0u, 0u};  // nothing selected (never at valid sizes)
         else pr.ka[j] = select_kth(s, aux[j], P, sz);
       }
-      if (any_of(pr, P) || q == nseq - 1) break;
+      // the compaction counts: an empty intersection moves on to the next softdbsize
+      n = compact(s, pr, P, cand);
     }
-    n = compact(s, pr, P, cand);
+    if (a.stats && threadIdx.x == 0) atomicAdd(a.stats + ST_PICK_ITERS, (unsigned long long)q);
   }
   if (n <= 0) {
     if (threadIdx.x == 0) { iq_dev_fail(a.status, IQ_ERR_NOPATTERN); a.rind[r] = -1; }
     return;
   }
   if (a.ncand && threadIdx.x == 0) a.ncand[r] = n;
+  if (a.stats && threadIdx.x == 0) {
+    atomicAdd(a.stats + ST_PICK_CAND, (unsigned long long)n);
+    atomicAdd(a.stats + ST_PICK_CTAS, 1ull);
+  }
 
   // ---- tau model weights ----
   if (n == 1) {
@@ -497,6 +514,7 @@ int iq_launch_pick(iq_ctx* ctx, const PickLaunch& L) {
   for (int q = 0; q < IQ_MAX_SEQ; ++q) { a.seq_norm[q] = L.seq_norm[q]; a.seq_zero[q] = L.seq_zero[q]; }
   a.cand = L.cand; a.k0 = L.k0; a.v0 = L.v0; a.k1 = L.k1; a.v1 = L.v1;
   a.w = L.w; a.prod = L.prod; a.rind = L.rind; a.ncand = L.ncand; a.status = L.status;
+  a.stats = L.stats;
   iq_timer_start(ctx, "pick");
   pick_kernel<<<L.nreal, PT, 0, ctx->stream>>>(a);
   iq_timer_stop(ctx, "pick", 4.0 * (double)L.P * (double)(1 + L.naux) * (double)L.nreal);

@@ -597,6 +597,7 @@ extern "C" int iq_simulate(iq_ctx* ctx, const iq_sim_params* p, const iq_hard_da
     for (int q = 0; q < IQ_MAX_SEQ; ++q) { L.seq_norm[q] = q < nsn ? seqn[q] : 0; L.seq_zero[q] = q < nsz ? seqz[q] : 0; }
     L.cand = d_cand; L.k0 = d_k0; L.v0 = d_v0; L.k1 = d_k1; L.v1 = d_v1; L.w = d_w; L.prod = d_prod;
     L.rind = d_rind; L.ncand = d_ncand; L.status = ctx->d_status;
+    L.stats = ctx->prof ? ctx->d_stats : nullptr;
     RET_IF(iq_launch_pick(ctx, L));
     // boundary cuts
     if (s.nslab > 0) {
@@ -609,6 +610,7 @@ extern "C" int iq_simulate(iq_ctx* ctx, const iq_sim_params* p, const iq_hard_da
       K.out = d_cutbuf; K.slabmax = slabmax;
       K.scratch = d_cutscr; K.scratch_per_cta = cutscr_per;
       K.status = ctx->d_status;
+      K.stats = ctx->prof ? ctx->d_stats : nullptr;
       RET_IF(iq_launch_cut(ctx, K));
     }
     // paste
