@@ -75,7 +75,7 @@ extern "C" int iq_profile(iq_ctx* ctx, int32_t enable) {
   if (!ctx) return iq_set_error(IQ_ERR_ARG, "null context");
   cudaStreamSynchronize(ctx->stream);
   for (auto& kv : ctx->timers) { kv.second.used = 0; kv.second.work = 0; }
-  cudaMemset(ctx->d_stats, 0, sizeof(unsigned long long) * ST_COUNT);
+  cudaMemsetAsync(ctx->d_stats, 0, sizeof(unsigned long long) * ST_COUNT, ctx->stream);
   ctx->prof = enable != 0;
   return IQ_OK;
 }
@@ -337,25 +337,34 @@ extern "C" int iq_pick(iq_ctx* ctx, const float* D, int64_t P, int32_t naux,
   for (int j = 0; j < naux; ++j)
     IQ_CUDA_OK(cudaMemcpyAsync(d_src + (j + 1) * P, Ds[j], sizeof(float) * P, cudaMemcpyDefault,
                                ctx->stream));
-  // min and max-finite of D, and npatterns, on the host copy-free path: small reduction here
+  // min and max-finite bits of every source, and npatterns (finite entries of D)
   std::vector<float> hD(P);
-  IQ_CUDA_OK(cudaMemcpyAsync(hD.data(), d_src, sizeof(float) * P, cudaMemcpyDeviceToHost, ctx->stream));
-  IQ_CUDA_OK(cudaStreamSynchronize(ctx->stream));
-  unsigned mn = 0x7F800000u, mx = 0u;
+  std::vector<unsigned> hmm(2 * nsrc);
   int64_t npat = 0;
-  for (int64_t p = 0; p < P; ++p) {
-    unsigned b = fbits(hD[p]);
-    mn = std::min(mn, b);
-    if (b < 0x7F800000u) { mx = std::max(mx, b); ++npat; }
+  IQ_CUDA_OK(cudaStreamSynchronize(ctx->stream));  // the uploads above are on the ctx stream
+  for (int j = 0; j < nsrc; ++j) {
+    IQ_CUDA_OK(cudaMemcpy(hD.data(), d_src + j * P, sizeof(float) * P, cudaMemcpyDeviceToHost));
+    unsigned mn = 0x7F800000u, mx = 0u;
+    for (int64_t q = 0; q < P; ++q) {
+      unsigned b = fbits(hD[q]);
+      mn = std::min(mn, b);
+      if (b < 0x7F800000u) { mx = std::max(mx, b); if (j == 0) ++npat; }
+    }
+    hmm[2 * j] = mn;
+    hmm[2 * j + 1] = mx;
   }
-  unsigned hmm[2] = {mn, mx};
-  IQ_CUDA_OK(cudaMemcpyAsync(d_mm, hmm, sizeof(hmm), cudaMemcpyHostToDevice, ctx->stream));
+  d_mm = (unsigned*)iq_scratch(ctx, S_MINMAX, sizeof(unsigned) * 2 * nsrc);
+  if (!d_mm) return IQ_ERR_ALLOC;
+  IQ_CUDA_OK(cudaMemcpyAsync(d_mm, hmm.data(), sizeof(unsigned) * 2 * nsrc, cudaMemcpyHostToDevice, ctx->stream));
   IQ_CUDA_OK(cudaMemsetAsync(ctx->d_status, 0, sizeof(int), ctx->stream));
   PickLaunch L;
   L.P = P; L.npat = npat; L.tol = tol; L.seed = seed; L.tile = tile; L.real0 = real; L.nreal = 1;
   L.D0 = d_src; L.D0_rstride = 0; L.mm0 = d_mm; L.mm0_rstride = 0;
   L.naux = naux;
-  for (int j = 0; j < naux; ++j) { L.aux[j] = d_src + (j + 1) * P; L.aux_rstride[j] = 0; }
+  for (int j = 0; j < naux; ++j) {
+    L.aux[j] = d_src + (j + 1) * P; L.aux_rstride[j] = 0;
+    L.aux_mm[j] = d_mm + 2 * (j + 1); L.aux_mm_rstride[j] = 0;
+  }
   if (naux > 0 && npat > 0)
     iq_relax_sizes(npat, tol, L.dbsize_norm, L.dbsize_zero, L.nseq_norm, L.seq_norm, L.nseq_zero,
                    L.seq_zero);

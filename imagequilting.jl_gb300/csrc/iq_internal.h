@@ -141,6 +141,8 @@ struct PickLaunch {
   int naux = 0;
   const float* aux[IQ_MAX_AUX] = {};
   int64_t aux_rstride[IQ_MAX_AUX] = {};
+  const unsigned* aux_mm[IQ_MAX_AUX] = {};  // [min, max finite] bits of each source
+  int64_t aux_mm_rstride[IQ_MAX_AUX] = {};
   // relaxation sizes (src/relaxation.jl:11-36): normal and all-zero cases
   int64_t dbsize_norm = 0, dbsize_zero = 0;
   int nseq_norm = 0, nseq_zero = 0;

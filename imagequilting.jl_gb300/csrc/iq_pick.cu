@@ -7,18 +7,27 @@
 //                   x = x0 * prod((1 - P)/P / x0), p = 1/(1 + x)
 //   draw            t = u * sum(p), first i with cumsum(p)[i] >= t   src/iqsim.jl:243
 //
-// "Top-k" follows partialsortperm: order by (value, index). The k-th key is found by an MSD
-// radix select on the value bits (non-negative floats order like their bits) and, among equal
-// values, on the index. Candidate lists are compacted in ascending index order. Dense ranks
-// come from a stable LSD radix sort of the candidates' values. All Float64 arithmetic uses
-// explicit round-to-nearest intrinsics so that the weights equal the oracle's bit for bit;
-// the draw sums in the fixed order of oracle/iqsim_oracle.sample_index.
+// "Top-k" follows partialsortperm: order by (value, index). The k-th (value, index) key is
+// found by a histogram select: non-negative floats order like their bit patterns, so 4096
+// bins over [bits(min), bits(max finite)] (the distance kernel supplies both) locate the bin
+// that holds the k-th element in one pass over the map; a second pass collects that bin's
+// (value, index) keys into shared memory and a bitonic sort gives the exact key. Bins too
+// large to collect are narrowed by another histogram; a bin of one repeated value falls back
+// to a radix select over the indices. The primary and one auxiliary source share passes.
+// Candidate lists are compacted in ascending index order; dense ranks come from a
+// shared-memory bitonic sort (a stable LSD radix sort in global memory above 8192
+// candidates). All Float64 arithmetic uses explicit round-to-nearest intrinsics so that the
+// weights equal the oracle's bit for bit; the draw sums in the fixed order of
+// oracle/iqsim_oracle.sample_index.
 #include "iq_internal.h"
 
 namespace {
 
 constexpr int PT = 1024;
 constexpr int NW = PT / 32;
+constexpr int NBIN = 4096;       // histogram bins per source
+constexpr int SORT_CAP = 8192;   // 64-bit keys sorted in shared memory
+constexpr int CITEMS = 8;        // positions per thread per compaction tile
 
 struct PickArgs {
   int64_t P, npat;
@@ -30,6 +39,8 @@ struct PickArgs {
   int naux;
   const float* aux[IQ_MAX_AUX];
   int64_t aux_rs[IQ_MAX_AUX];
+  const unsigned* aux_mm[IQ_MAX_AUX];
+  int64_t aux_mm_rs[IQ_MAX_AUX];
   int64_t dbsize_norm, dbsize_zero;
   int nseq_norm, nseq_zero;
   int64_t seq_norm[IQ_MAX_SEQ], seq_zero[IQ_MAX_SEQ];
@@ -43,17 +54,22 @@ struct PickArgs {
   unsigned long long* stats;
 };
 
+// small shared state (static); the large regions are dynamic shared memory:
+//   hist : 2 x NBIN uint32 (32 KB)          histograms of up to two sources
+//   sbuf : SORT_CAP uint64 (64 KB)          sort buffer; also the radix sort's per-warp
+//                                           digit counters (NW x 256 uint32)
+constexpr size_t DYN_BYTES = 2 * NBIN * 4 + SORT_CAP * 8;
+
 struct Smem {
   uint32_t hist[256];
   uint32_t base[256];
-  uint32_t wcnt[NW][256];
   uint32_t warp[NW];
   unsigned long long wred[NW];
   uint32_t sel, cnt;
   int64_t kk;
   int flag;
-  double dval;
-  int64_t ival;
+  uint32_t ncol;
+  int64_t bin[2], below[2], bcnt[2];
 };
 
 __device__ __forceinline__ uint32_t lanemask_lt() {
@@ -81,7 +97,7 @@ __device__ uint32_t block_excl_sum(Smem& s, uint32_t v, uint32_t& total) {
       uint32_t y = __shfl_up_sync(0xffffffffu, u, o);
       if (lane >= o) u += y;
     }
-    s.warp[lane] = u - t;  // exclusive warp offsets
+    s.warp[lane] = u - t;
     if (lane == 31) s.cnt = u;
   }
   __syncthreads();
@@ -108,35 +124,32 @@ __device__ unsigned long long block_sum_u64(Smem& s, unsigned long long v) {
   return r;
 }
 
-// Histograms are counted per warp (s.wcnt[warp][digit], one leader per distinct digit of a
-// warp after __match_any_sync) and summed into s.hist: no two warps touch the same counter,
-// which matters because float bit patterns pile into a few high-order digits.
-__device__ __forceinline__ void whist_zero(Smem& s) {
-  for (int i = threadIdx.x; i < NW * 256; i += PT) (&s.wcnt[0][0])[i] = 0;
+// ---- per-warp 256-bin histograms (radix select over indices, radix sort) -----------------
+__device__ __forceinline__ void whist_zero(uint32_t* wcnt) {
+  for (int i = threadIdx.x; i < NW * 256; i += PT) wcnt[i] = 0;
   __syncthreads();
 }
 
-__device__ __forceinline__ void whist_add(Smem& s, bool valid, uint32_t d) {
+__device__ __forceinline__ void whist_add(uint32_t* wcnt, bool valid, uint32_t d) {
   const int lane = threadIdx.x & 31;
   uint32_t key = valid ? d : (0x10000u + lane);
   uint32_t peers = __match_any_sync(0xffffffffu, key);
   if (valid && lane == __ffs(peers) - 1)
-    atomicAdd(&s.wcnt[threadIdx.x >> 5][d], (uint32_t)__popc(peers));
+    atomicAdd(&wcnt[(threadIdx.x >> 5) * 256 + d], (uint32_t)__popc(peers));
 }
 
-__device__ __forceinline__ void whist_reduce(Smem& s) {
+__device__ __forceinline__ void whist_reduce(Smem& s, const uint32_t* wcnt) {
   __syncthreads();
   for (int d = threadIdx.x; d < 256; d += PT) {
     uint32_t t = 0;
 #pragma unroll 8
-    for (int w = 0; w < NW; ++w) t += s.wcnt[w][d];
+    for (int w = 0; w < NW; ++w) t += wcnt[w * 256 + d];
     s.hist[d] = t;
   }
   __syncthreads();
 }
 
-// Bucket holding the kk-th (1-based) element of s.hist; sets s.sel, s.cnt, s.kk (rank
-// within the bucket). Called by all threads.
+// Bucket of s.hist holding the kk-th (1-based) element; sets s.sel, s.cnt, s.kk.
 __device__ void find_bucket(Smem& s, int64_t kk) {
   __syncthreads();
   if (threadIdx.x < 32) {
@@ -176,69 +189,205 @@ __device__ __forceinline__ bool key_le(uint32_t b, uint32_t p, Key k) {
   return b < k.v || (b == k.v && p <= k.i);
 }
 
-// The kk-th smallest (value, index) key of src[0..P) (1 <= kk <= P).
-__device__ Key select_kth(Smem& s, const float* __restrict__ src, int64_t P, int64_t kk) {
+// Radix select (MSD, 8-bit digits) of the kk-th smallest (value, index) key: the general
+// fallback. With `fixed_value` set it only selects among the indices holding that value.
+__device__ Key radix_select(Smem& s, uint32_t* wcnt, const float* __restrict__ src, int64_t P,
+                            int64_t kk, bool fixed_value, uint32_t value) {
   uint32_t prefix = 0, mask = 0;
   const int64_t iters = (P + PT - 1) / PT;
   uint32_t cnt_eq = 0;
-  for (int shift = 24; shift >= 0; shift -= 8) {
-    whist_zero(s);
-    for (int64_t it = 0; it < iters; ++it) {
-      int64_t p = it * PT + threadIdx.x;
-      bool valid = p < P;
-      uint32_t b = valid ? fbits(src[p]) : 0u;
-      valid = valid && (b & mask) == prefix;
-      whist_add(s, valid, (b >> shift) & 255u);
+  if (!fixed_value) {
+    for (int shift = 24; shift >= 0; shift -= 8) {
+      whist_zero(wcnt);
+      for (int64_t it = 0; it < iters; ++it) {
+        int64_t p = it * PT + threadIdx.x;
+        bool valid = p < P;
+        uint32_t b = valid ? fbits(src[p]) : 0u;
+        valid = valid && (b & mask) == prefix;
+        whist_add(wcnt, valid, (b >> shift) & 255u);
+      }
+      whist_reduce(s, wcnt);
+      find_bucket(s, kk);
+      prefix |= s.sel << shift;
+      mask |= 255u << shift;
+      kk = s.kk;
+      cnt_eq = s.cnt;
     }
-    whist_reduce(s);
-    find_bucket(s, kk);
-    prefix |= s.sel << shift;
-    mask |= 255u << shift;
-    kk = s.kk;
-    cnt_eq = s.cnt;
+    if (kk >= (int64_t)cnt_eq) return Key{prefix, 0xFFFFFFFFu};
+  } else {
+    prefix = value;
   }
-  Key k{prefix, 0xFFFFFFFFu};
-  if (kk >= (int64_t)cnt_eq) return k;  // every index with this value is inside
-  // select among equal values by index
   int topbit = 0;
   while (topbit < 31 && ((int64_t)1 << (topbit + 1)) <= P - 1) ++topbit;
   uint32_t ip = 0, im = 0;
   for (int shift = (topbit / 8) * 8; shift >= 0; shift -= 8) {
-    whist_zero(s);
+    whist_zero(wcnt);
     for (int64_t it = 0; it < iters; ++it) {
       int64_t p = it * PT + threadIdx.x;
       bool valid = p < P;
       uint32_t b = valid ? fbits(src[p]) : 0u;
       valid = valid && b == prefix && ((uint32_t)p & im) == ip;
-      whist_add(s, valid, ((uint32_t)p >> shift) & 255u);
+      whist_add(wcnt, valid, ((uint32_t)p >> shift) & 255u);
     }
-    whist_reduce(s);
+    whist_reduce(s, wcnt);
     find_bucket(s, kk);
     ip |= s.sel << shift;
     im |= 255u << shift;
     kk = s.kk;
   }
-  k.i = ip;
-  return k;
+  return Key{prefix, ip};
 }
 
-// Predicates over a position p.
-struct ThrPred {
-  const float* D; double thr;
-  __device__ bool operator()(int64_t p) const { return (double)D[p] <= thr; }
-};
-struct RelaxPred {
-  const float* D; Key kD;
-  int naux; const float* aux[IQ_MAX_AUX]; Key ka[IQ_MAX_AUX];
-  __device__ bool operator()(int64_t p) const {
-    if (!key_le(fbits(D[p]), (uint32_t)p, kD)) return false;
-    for (int a = 0; a < naux; ++a)
-      if (!key_le(fbits(aux[a][p]), (uint32_t)p, ka[a])) return false;
-    return true;
+// Bitonic sort of buf[0..n) ascending (n rounded up to a power of two, padded with ~0).
+__device__ void bitonic_sort(unsigned long long* buf, int n) {
+  int n2 = 2;
+  while (n2 < n) n2 <<= 1;
+  for (int i = n + threadIdx.x; i < n2; i += PT) buf[i] = ~0ull;
+  __syncthreads();
+  for (int k = 2; k <= n2; k <<= 1) {
+    for (int j = k >> 1; j > 0; j >>= 1) {
+      for (int i = threadIdx.x; i < n2; i += PT) {
+        const int l = i ^ j;
+        if (l > i) {
+          const unsigned long long a = buf[i], b = buf[l];
+          const bool asc = (i & k) == 0;
+          if ((a > b) == asc) { buf[i] = b; buf[l] = a; }
+        }
+      }
+      __syncthreads();
+    }
   }
+}
+
+// Histogram select of the k-th smallest (value, index) key of up to two sources at once.
+// mn/mx: bits of the smallest value and of the largest finite value of each source.
+struct SelReq {
+  const float* src;
+  uint32_t mn, mx;
+  int64_t k;
 };
 
-constexpr int CITEMS = 8;
+__device__ __forceinline__ int bin_shift(uint32_t mn, uint32_t mx) {
+  int sh = 0;
+  while (((mx - mn) >> sh) >= (uint32_t)NBIN) ++sh;
+  return sh;
+}
+
+template <int NS>
+__device__ void hist_select(Smem& s, uint32_t* hist, unsigned long long* sbuf, SelReq* req,
+                            int64_t P, Key* out) {
+  uint32_t lo[NS], hi[NS];
+  int sh[NS];
+  int64_t k[NS];
+  bool pend[NS];
+#pragma unroll
+  for (int j = 0; j < NS; ++j) {
+    lo[j] = req[j].mn;
+    hi[j] = req[j].mx;
+    k[j] = req[j].k;
+    pend[j] = true;
+  }
+  const int64_t iters = (P + PT - 1) / PT;
+  for (int level = 0; level < 4; ++level) {
+    bool any = false;
+#pragma unroll
+    for (int j = 0; j < NS; ++j) any = any || pend[j];
+    if (!any) break;
+#pragma unroll
+    for (int j = 0; j < NS; ++j) sh[j] = pend[j] ? bin_shift(lo[j], hi[j]) : 0;
+    for (int i = threadIdx.x; i < NS * NBIN; i += PT) hist[i] = 0;
+    __syncthreads();
+    for (int64_t it = 0; it < iters; ++it) {
+      const int64_t p = it * PT + threadIdx.x;
+      if (p >= P) break;
+#pragma unroll
+      for (int j = 0; j < NS; ++j) {
+        if (!pend[j]) continue;
+        const uint32_t b = fbits(req[j].src[p]);
+        if (b >= lo[j] && b <= hi[j]) atomicAdd(&hist[j * NBIN + ((b - lo[j]) >> sh[j])], 1u);
+      }
+    }
+    __syncthreads();
+    // locate the bin of each pending source: warp j scans source j's 4096 bins
+    const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (wid < NS && pend[wid]) {
+      const int j = wid;
+      uint32_t sum = 0;
+      for (int i = 0; i < NBIN / 32; ++i) sum += hist[j * NBIN + lane * (NBIN / 32) + i];
+      uint32_t inc = sum;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        uint32_t y = __shfl_up_sync(0xffffffffu, inc, o);
+        if (lane >= o) inc += y;
+      }
+      const uint32_t exc = inc - sum;
+      const bool here = (int64_t)exc < k[j] && (int64_t)inc >= k[j];
+      const uint32_t bal = __ballot_sync(0xffffffffu, here);
+      if (bal == 0) {
+        if (lane == 0) { s.bin[j] = -1; s.below[j] = 0; s.bcnt[j] = 0; }
+      } else if (lane == __ffs(bal) - 1) {
+        int64_t below = exc;
+        int b = lane * (NBIN / 32);
+        for (;; ++b) {
+          const uint32_t c = hist[j * NBIN + b];
+          if (below + c >= k[j]) break;
+          below += c;
+        }
+        s.bin[j] = b;
+        s.below[j] = below;
+        s.bcnt[j] = hist[j * NBIN + b];
+      }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int j = 0; j < NS; ++j) {
+      if (!pend[j]) continue;
+      const int64_t b = s.bin[j];
+      const int64_t below = s.below[j];
+      const int64_t cntb = s.bcnt[j];
+      __syncthreads();
+      if (b < 0) {  // k-th element lies above the largest finite value: general fallback
+        out[j] = radix_select(s, reinterpret_cast<uint32_t*>(sbuf), req[j].src, P, req[j].k,
+                              false, 0);
+        pend[j] = false;
+        continue;
+      }
+      const uint32_t blo = lo[j] + ((uint32_t)b << sh[j]);
+      const uint32_t span = sh[j] >= 32 ? 0xFFFFFFFFu : ((1u << sh[j]) - 1u);
+      const uint32_t bhi = (hi[j] - blo) < span ? hi[j] : blo + span;
+      const int64_t kb = k[j] - below;
+      if (cntb <= SORT_CAP) {
+        // collect the bin's (value, index) keys and sort them
+        if (threadIdx.x == 0) s.ncol = 0;
+        __syncthreads();
+        for (int64_t it = 0; it < iters; ++it) {
+          const int64_t p = it * PT + threadIdx.x;
+          if (p >= P) break;
+          const uint32_t v = fbits(req[j].src[p]);
+          if (v >= blo && v <= bhi) {
+            const uint32_t at = atomicAdd(&s.ncol, 1u);
+            sbuf[at] = ((unsigned long long)v << 32) | (uint32_t)p;
+          }
+        }
+        __syncthreads();
+        const int nc = (int)s.ncol;
+        bitonic_sort(sbuf, nc);
+        const unsigned long long key = sbuf[kb - 1];
+        out[j] = Key{(uint32_t)(key >> 32), (uint32_t)key};
+        __syncthreads();
+        pend[j] = false;
+      } else if (sh[j] == 0) {
+        // one value repeated more than SORT_CAP times: select among its indices
+        out[j] = radix_select(s, reinterpret_cast<uint32_t*>(sbuf), req[j].src, P, kb, true, blo);
+        pend[j] = false;
+      } else {
+        lo[j] = blo;
+        hi[j] = bhi;
+        k[j] = kb;
+      }
+    }
+  }
+}
 
 // Ordered compaction of {p : pred(p)} into out (if non-null); returns the count.
 template <typename Pred>
@@ -250,7 +399,7 @@ __device__ int64_t compact(Smem& s, const Pred& pred, int64_t P, int32_t* out) {
     uint32_t bits = 0;
 #pragma unroll
     for (int i = 0; i < CITEMS; ++i) {
-      int64_t p = p0 + i;
+      const int64_t p = p0 + i;
       if (p < P && pred(p)) bits |= 1u << i;
     }
     uint32_t total;
@@ -266,25 +415,43 @@ __device__ int64_t compact(Smem& s, const Pred& pred, int64_t P, int32_t* out) {
   return base;
 }
 
-// Stable LSD radix sort of (keys, vals)[0..n) between the buffer pairs; returns 0 if the
-// result is in (ka, va), 1 if in (kb, vb).
-__device__ int radix_sort(Smem& s, uint32_t* ka, uint32_t* va, uint32_t* kb, uint32_t* vb,
-                          int64_t n) {
+struct ThrPred {
+  const float* D; double thr;
+  __device__ bool operator()(int64_t p) const { return (double)D[p] <= thr; }
+};
+
+template <int NAUX>
+struct RelaxPred {
+  const float* D; Key kD;
+  const float* aux[NAUX > 0 ? NAUX : 1];
+  Key ka[NAUX > 0 ? NAUX : 1];
+  __device__ bool operator()(int64_t p) const {
+    if (!key_le(fbits(D[p]), (uint32_t)p, kD)) return false;
+#pragma unroll
+    for (int a = 0; a < NAUX; ++a)
+      if (!key_le(fbits(aux[a][p]), (uint32_t)p, ka[a])) return false;
+    return true;
+  }
+};
+
+// Stable LSD radix sort of (keys, vals)[0..n) between the buffer pairs (global memory);
+// returns 0 if the result is in (ka, va), 1 if in (kb, vb).
+__device__ int radix_sort(Smem& s, uint32_t* wcnt, uint32_t* ka, uint32_t* va, uint32_t* kb,
+                          uint32_t* vb, int64_t n) {
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   int cur = 0;
   const int64_t ntiles = (n + PT - 1) / PT;
   for (int shift = 0; shift < 32; shift += 8) {
     uint32_t* ks = cur ? kb : ka; uint32_t* vs = cur ? vb : va;
     uint32_t* kd = cur ? ka : kb; uint32_t* vd = cur ? va : vb;
-    whist_zero(s);
+    whist_zero(wcnt);
     for (int64_t t = 0; t < ntiles; ++t) {
       int64_t i = t * PT + threadIdx.x;
       bool valid = i < n;
       uint32_t d = valid ? (ks[i] >> shift) & 255u : 0u;
-      whist_add(s, valid, d);
+      whist_add(wcnt, valid, d);
     }
-    whist_reduce(s);
-    // single-bucket pass: order unchanged, skip it
+    whist_reduce(s, wcnt);
     int single = 0;
     if (threadIdx.x < 256 && (int64_t)s.hist[threadIdx.x] == n) single = 1;
     if (__syncthreads_or(single)) continue;
@@ -294,7 +461,7 @@ __device__ int radix_sort(Smem& s, uint32_t* ka, uint32_t* va, uint32_t* kb, uin
     }
     __syncthreads();
     for (int64_t t = 0; t < ntiles; ++t) {
-      for (int i = threadIdx.x; i < NW * 256; i += PT) (&s.wcnt[0][0])[i] = 0;
+      for (int i = threadIdx.x; i < NW * 256; i += PT) wcnt[i] = 0;
       __syncthreads();
       int64_t i = t * PT + threadIdx.x;
       bool valid = i < n;
@@ -302,20 +469,20 @@ __device__ int radix_sort(Smem& s, uint32_t* ka, uint32_t* va, uint32_t* kb, uin
       uint32_t d = (k >> shift) & 255u;
       uint32_t peers = __match_any_sync(0xffffffffu, valid ? d : (0x10000u + lane));
       uint32_t rank = __popc(peers & lanemask_lt());
-      if (valid && lane == __ffs(peers) - 1) s.wcnt[wid][d] = __popc(peers);
+      if (valid && lane == __ffs(peers) - 1) wcnt[wid * 256 + d] = __popc(peers);
       __syncthreads();
       if (threadIdx.x < 256) {
         uint32_t run = s.base[threadIdx.x];
         for (int w = 0; w < NW; ++w) {
-          uint32_t c = s.wcnt[w][threadIdx.x];
-          s.wcnt[w][threadIdx.x] = run;
+          uint32_t c = wcnt[w * 256 + threadIdx.x];
+          wcnt[w * 256 + threadIdx.x] = run;
           run += c;
         }
         s.base[threadIdx.x] = run;
       }
       __syncthreads();
       if (valid) {
-        uint32_t dst = s.wcnt[wid][d] + rank;
+        uint32_t dst = wcnt[wid * 256 + d] + rank;
         kd[dst] = k;
         vd[dst] = v;
       }
@@ -327,16 +494,22 @@ __device__ int radix_sort(Smem& s, uint32_t* ka, uint32_t* va, uint32_t* kb, uin
 }
 
 // Dense ranks (1-based) of src[cand[i]], i < n, written to rank[i]; returns the sum of
-// (n - rank + 1) over i.
-__device__ unsigned long long dense_ranks(Smem& s, const float* __restrict__ src,
+// (n - rank + 1) over i. `rank` must not alias k0/v0/k1/v1.
+__device__ unsigned long long dense_ranks(Smem& s, unsigned long long* sbuf,
+                                          const float* __restrict__ src,
                                           const int32_t* __restrict__ cand, int64_t n,
                                           uint32_t* k0, uint32_t* v0, uint32_t* k1, uint32_t* v1,
-                                          uint32_t** rank_out) {
+                                          uint32_t* rank) {
   unsigned mn = 0xFFFFFFFFu, mx = 0u;
+  const bool small = n <= SORT_CAP;
   for (int64_t i = threadIdx.x; i < n; i += PT) {
-    uint32_t b = fbits(src[cand[i]]);
-    k0[i] = b;
-    v0[i] = (uint32_t)i;
+    const uint32_t b = fbits(src[cand[i]]);
+    if (small) {
+      sbuf[i] = ((unsigned long long)b << 32) | (uint32_t)i;
+    } else {
+      k0[i] = b;
+      v0[i] = (uint32_t)i;
+    }
     mn = min(mn, b);
     mx = max(mx, b);
   }
@@ -353,39 +526,56 @@ __device__ unsigned long long dense_ranks(Smem& s, const float* __restrict__ src
   const bool all_equal = s.flag != 0;
   __syncthreads();
   if (all_equal) {
-    for (int64_t i = threadIdx.x; i < n; i += PT) k1[i] = 1u;
+    for (int64_t i = threadIdx.x; i < n; i += PT) rank[i] = 1u;
     __syncthreads();
-    *rank_out = k1;
     return (unsigned long long)n * (unsigned long long)n;  // each term n - 1 + 1
   }
-  int where = radix_sort(s, k0, v0, k1, v1, n);
-  uint32_t* ks = where ? k1 : k0;
-  uint32_t* vs = where ? v1 : v0;
-  uint32_t* rk = where ? k0 : k1;  // free buffer receives ranks (indexed by candidate)
-  // inclusive scan of "value changes" in sorted order
+  const uint32_t* ks = nullptr;
+  const uint32_t* vs = nullptr;
+  if (small) {
+    bitonic_sort(sbuf, (int)n);
+  } else {
+    int where = radix_sort(s, reinterpret_cast<uint32_t*>(sbuf), k0, v0, k1, v1, n);
+    ks = where ? k1 : k0;
+    vs = where ? v1 : v0;
+  }
   uint32_t carry = 0;
   unsigned long long acc = 0;
   for (int64_t t0 = 0; t0 < n; t0 += PT) {
-    int64_t i = t0 + threadIdx.x;
-    uint32_t f = 0;
-    if (i < n) f = (i == 0 || ks[i] != ks[i - 1]) ? 1u : 0u;
-    uint32_t total;
-    uint32_t ex = block_excl_sum(s, f, total);
+    const int64_t i = t0 + threadIdx.x;
+    uint32_t f = 0, idx = 0;
     if (i < n) {
-      uint32_t r = carry + ex + f;
-      // the sort buffers are read before the rank buffer is written: rk aliases neither
-      rk[vs[i]] = r;
+      uint32_t cur, prev = 0;
+      if (small) {
+        cur = (uint32_t)(sbuf[i] >> 32);
+        if (i) prev = (uint32_t)(sbuf[i - 1] >> 32);
+        idx = (uint32_t)sbuf[i];
+      } else {
+        cur = ks[i];
+        if (i) prev = ks[i - 1];
+        idx = vs[i];
+      }
+      f = (i == 0 || cur != prev) ? 1u : 0u;
+    }
+    uint32_t total;
+    const uint32_t ex = block_excl_sum(s, f, total);
+    if (i < n) {
+      const uint32_t r = carry + ex + f;
+      rank[idx] = r;
       acc += (unsigned long long)(n - r + 1);
     }
     carry += total;
   }
   __syncthreads();
-  *rank_out = rk;
   return block_sum_u64(s, acc);
 }
 
+template <int NAUX>
 __global__ void __launch_bounds__(PT) pick_kernel(const PickArgs a) {
   __shared__ Smem s;
+  extern __shared__ __align__(16) unsigned char dyn[];
+  uint32_t* hist = reinterpret_cast<uint32_t*>(dyn);
+  unsigned long long* sbuf = reinterpret_cast<unsigned long long*>(dyn + 2 * NBIN * 4);
   const int r = blockIdx.x;
   const int64_t P = a.P;
   const float* D = a.D0 + r * a.D0_rs;
@@ -397,11 +587,17 @@ __global__ void __launch_bounds__(PT) pick_kernel(const PickArgs a) {
   uint32_t* v1 = a.v1 + r * P;
   double* w = a.w + r * P;
   double* prod = a.prod + r * P;
-  const float* aux[IQ_MAX_AUX];
-  for (int j = 0; j < a.naux; ++j) aux[j] = a.aux[j] + r * a.aux_rs[j];
+  uint32_t* rankbuf = reinterpret_cast<uint32_t*>(w);  // ranks live in w until weights are made
+  const float* aux[NAUX > 0 ? NAUX : 1];
+  const unsigned* amm[NAUX > 0 ? NAUX : 1];
+#pragma unroll
+  for (int j = 0; j < NAUX; ++j) {
+    aux[j] = a.aux[j] + r * a.aux_rs[j];
+    amm[j] = a.aux_mm[j] + r * a.aux_mm_rs[j];
+  }
 
   int64_t n;
-  if (a.naux == 0) {
+  if (NAUX == 0) {
     const float mn = __uint_as_float(mm[0]);
     const double thr = __dmul_rn(__dadd_rn(1.0, a.tol), (double)mn);
     ThrPred pr{D, thr};
@@ -414,19 +610,38 @@ __global__ void __launch_bounds__(PT) pick_kernel(const PickArgs a) {
     const bool allzero = mm[1] == 0u;
     const int64_t dbsize = allzero ? a.dbsize_zero : a.dbsize_norm;
     const int nseq = allzero ? a.nseq_zero : a.nseq_norm;
-    RelaxPred pr;
+    RelaxPred<NAUX> pr;
     pr.D = D;
-    pr.naux = a.naux;
-    for (int j = 0; j < a.naux; ++j) pr.aux[j] = aux[j];
-    pr.kD = select_kth(s, D, P, dbsize);
+#pragma unroll
+    for (int j = 0; j < NAUX; ++j) pr.aux[j] = aux[j];
     n = 0;
     int q = 0;
     for (; q < nseq && n == 0; ++q) {
       const int64_t sz = allzero ? a.seq_zero[q] : a.seq_norm[q];
-      for (int j = 0; j < a.naux; ++j) {
-        if (sz >= P) pr.ka[j] = Key{0xFFFFFFFFu, 0xFFFFFFFFu};
-        else if (sz <= 0) pr.ka[j] = Key{0u, 0u};  // nothing selected (never at valid sizes)
-        else pr.ka[j] = select_kth(s, aux[j], P, sz);
+      // selections of this round: D (first round only) and every auxiliary source
+      SelReq req[2];
+      Key res[2];
+      int j0 = 0;
+      if (q == 0) {
+        req[0] = SelReq{D, mm[0], mm[1], dbsize};
+        if (NAUX > 0 && sz > 0 && sz < P) {
+          req[1] = SelReq{aux[0], amm[0][0], amm[0][1], sz};
+          hist_select<2>(s, hist, sbuf, req, P, res);
+          pr.ka[0] = res[1];
+          j0 = 1;
+        } else {
+          hist_select<1>(s, hist, sbuf, req, P, res);
+        }
+        pr.kD = res[0];
+      }
+#pragma unroll
+      for (int j = 0; j < NAUX; ++j) {
+        if (j < j0) continue;
+        if (sz >= P) { pr.ka[j] = Key{0xFFFFFFFFu, 0xFFFFFFFFu}; continue; }
+        if (sz <= 0) { pr.ka[j] = Key{0u, 0u}; continue; }
+        req[0] = SelReq{aux[j], amm[j][0], amm[j][1], sz};
+        hist_select<1>(s, hist, sbuf, req, P, res);
+        pr.ka[j] = res[0];
       }
       // the compaction counts: an empty intersection moves on to the next softdbsize
       n = compact(s, pr, P, cand);
@@ -452,15 +667,14 @@ __global__ void __launch_bounds__(PT) pick_kernel(const PickArgs a) {
   const double inv_n = __ddiv_rn(1.0, dn);
   const double x0 = __ddiv_rn(__dsub_rn(1.0, inv_n), inv_n);
   for (int64_t i = threadIdx.x; i < n; i += PT) prod[i] = 1.0;
-  const int nsrc = 1 + a.naux;
-  for (int j = 0; j < nsrc; ++j) {
-    const float* src = j == 0 ? D : aux[j - 1];
+#pragma unroll 1
+  for (int j = 0; j <= NAUX; ++j) {
+    const float* src = j == 0 ? D : aux[j > 0 ? j - 1 : 0];
     __syncthreads();
-    uint32_t* rank;
-    unsigned long long S = dense_ranks(s, src, cand, n, k0, v0, k1, v1, &rank);
+    const unsigned long long S = dense_ranks(s, sbuf, src, cand, n, k0, v0, k1, v1, rankbuf);
     const double dS = (double)S;
     for (int64_t i = threadIdx.x; i < n; i += PT) {
-      const double Pi = __ddiv_rn((double)(n - (int64_t)rank[i] + 1), dS);
+      const double Pi = __ddiv_rn((double)(n - (int64_t)rankbuf[i] + 1), dS);
       const double X = __ddiv_rn(__dsub_rn(1.0, Pi), Pi);
       prod[i] = __dmul_rn(prod[i], __ddiv_rn(X, x0));
     }
@@ -499,6 +713,18 @@ __global__ void __launch_bounds__(PT) pick_kernel(const PickArgs a) {
   }
 }
 
+template <int NAUX>
+cudaError_t launch_pick_t(const PickArgs& a, int nreal, cudaStream_t st) {
+  static bool attr = false;
+  if (!attr) {
+    cudaFuncSetAttribute(pick_kernel<NAUX>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)DYN_BYTES);
+    attr = true;
+  }
+  pick_kernel<NAUX><<<nreal, PT, DYN_BYTES, st>>>(a);
+  return cudaGetLastError();
+}
+
 }  // namespace
 
 int iq_launch_pick(iq_ctx* ctx, const PickLaunch& L) {
@@ -508,7 +734,10 @@ int iq_launch_pick(iq_ctx* ctx, const PickLaunch& L) {
   a.real0 = L.real0;
   a.D0 = L.D0; a.D0_rs = L.D0_rstride; a.mm0 = L.mm0; a.mm0_rs = L.mm0_rstride;
   a.naux = L.naux;
-  for (int j = 0; j < IQ_MAX_AUX; ++j) { a.aux[j] = L.aux[j]; a.aux_rs[j] = L.aux_rstride[j]; }
+  for (int j = 0; j < IQ_MAX_AUX; ++j) {
+    a.aux[j] = L.aux[j]; a.aux_rs[j] = L.aux_rstride[j];
+    a.aux_mm[j] = L.aux_mm[j]; a.aux_mm_rs[j] = L.aux_mm_rstride[j];
+  }
   a.dbsize_norm = L.dbsize_norm; a.dbsize_zero = L.dbsize_zero;
   a.nseq_norm = L.nseq_norm; a.nseq_zero = L.nseq_zero;
   for (int q = 0; q < IQ_MAX_SEQ; ++q) { a.seq_norm[q] = L.seq_norm[q]; a.seq_zero[q] = L.seq_zero[q]; }
@@ -516,9 +745,19 @@ int iq_launch_pick(iq_ctx* ctx, const PickLaunch& L) {
   a.w = L.w; a.prod = L.prod; a.rind = L.rind; a.ncand = L.ncand; a.status = L.status;
   a.stats = L.stats;
   iq_timer_start(ctx, "pick");
-  pick_kernel<<<L.nreal, PT, 0, ctx->stream>>>(a);
+  cudaError_t e;
+  switch (L.naux) {
+    case 0: e = launch_pick_t<0>(a, L.nreal, ctx->stream); break;
+    case 1: e = launch_pick_t<1>(a, L.nreal, ctx->stream); break;
+    case 2: e = launch_pick_t<2>(a, L.nreal, ctx->stream); break;
+    case 3: e = launch_pick_t<3>(a, L.nreal, ctx->stream); break;
+    case 4: e = launch_pick_t<4>(a, L.nreal, ctx->stream); break;
+    case 5: e = launch_pick_t<5>(a, L.nreal, ctx->stream); break;
+    case 6: e = launch_pick_t<6>(a, L.nreal, ctx->stream); break;
+    default: e = launch_pick_t<7>(a, L.nreal, ctx->stream); break;
+  }
   iq_timer_stop(ctx, "pick", 4.0 * (double)L.P * (double)(1 + L.naux) * (double)L.nreal);
   iq_count(ctx);
-  IQ_CUDA_OK(cudaGetLastError());
+  if (e != cudaSuccess) return iq_set_error(IQ_ERR_CUDA, "pick launch: %s", cudaGetErrorString(e));
   return IQ_OK;
 }

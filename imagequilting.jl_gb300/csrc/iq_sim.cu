@@ -472,6 +472,7 @@ extern "C" int iq_simulate(iq_ctx* ctx, const iq_sim_params* p, const iq_hard_da
   std::vector<float*> d_aux(nsoft), d_auxti(nsoft);
   std::vector<double*> d_auxii(nsoft);
   float* d_soft = nullptr;
+  unsigned* d_softmm = nullptr;  // [min, max finite] bits of each soft map
   std::vector<int64_t> slot_of(g.ntot, -1);
   int64_t nslot = 0;
   if (nsoft > 0) {
@@ -489,8 +490,9 @@ extern "C" int iq_simulate(iq_ctx* ctx, const iq_sim_params* p, const iq_hard_da
     double* a_ii = (double*)iq_scratch(ctx, S_AUXII, sizeof(double) * iivol * nsoft);
     float* a_raw = (float*)iq_scratch(ctx, S_TMP1, sizeof(float) * auxvol);
     d_soft = (float*)iq_scratch(ctx, S_SOFT, sizeof(float) * P * nslot * nsoft);
+    d_softmm = (unsigned*)iq_scratch(ctx, S_SOFTB2, sizeof(unsigned) * 2 * nslot * nsoft);
     int64_t* d_starts = (int64_t*)iq_scratch(ctx, S_STARTS, sizeof(int64_t) * (nslot + 16));
-    if (!a_aux || !a_ti || !a_ii || !a_raw || !d_soft || !d_starts) return IQ_ERR_ALLOC;
+    if (!a_aux || !a_ti || !a_ii || !a_raw || !d_soft || !d_softmm || !d_starts) return IQ_ERR_ALLOC;
     for (int s = 0; s < nsoft; ++s) {
       Dim3 asz{1, 1, 1};
       int64_t ae[3] = {1, 1, 1};
@@ -525,6 +527,7 @@ extern "C" int iq_simulate(iq_ctx* ctx, const iq_sim_params* p, const iq_hard_da
         G.grid = d_aux[s]; G.grid_dims = psz; G.grid_stride = 0; G.starts = d_starts + b0;
         G.K = (int)T; G.klist = d_kl + (size_t)ncfg * T; G.ntmpl = nb; G.rpad = 16;
         G.tv = d_tv; G.b2 = d_b2;
+        G.minmax = d_softmm + 2 * ((int64_t)s * nslot + slot_of[tl[b0]]);
         RET_IF(iq_launch_gather(ctx, G));
         CorrLaunch C;
         C.img = d_auxti[s]; C.img_dims = ctx->ti; C.out_dims = distD; C.K = (int)T;
@@ -534,6 +537,7 @@ extern "C" int iq_simulate(iq_ctx* ctx, const iq_sim_params* p, const iq_hard_da
         C.disabled = d_dis;
         C.out = d_soft + ((int64_t)s * nslot + slot_of[tl[b0]]) * P;
         C.out_stride = P;
+        C.minmax = G.minmax;
         RET_IF(iq_launch_corr(ctx, C));
       }
       IQ_CUDA_OK(cudaStreamSynchronize(st));  // `starts` is a host vector
@@ -583,13 +587,17 @@ extern "C" int iq_simulate(iq_ctx* ctx, const iq_sim_params* p, const iq_hard_da
     int na = 0;
     if (s.hardtile) {
       L.D0 = d_Dh; L.D0_rstride = 0; L.mm0 = d_mmh; L.mm0_rstride = 0;
-      L.aux[na] = d_D; L.aux_rstride[na] = P; ++na;
+      L.aux[na] = d_D; L.aux_rstride[na] = P;
+      L.aux_mm[na] = d_mm; L.aux_mm_rstride[na] = 2;
+      ++na;
     } else {
       L.D0 = d_D; L.D0_rstride = P; L.mm0 = d_mm; L.mm0_rstride = 2;
     }
     for (int q = 0; q < nsoft; ++q) {
       L.aux[na] = d_soft + ((int64_t)q * nslot + slot_of[s.tile]) * P;
       L.aux_rstride[na] = 0;
+      L.aux_mm[na] = d_softmm + 2 * ((int64_t)q * nslot + slot_of[s.tile]);
+      L.aux_mm_rstride[na] = 0;
       ++na;
     }
     L.naux = na;
