@@ -340,6 +340,8 @@ def run_ours(args, W, dist, rank, world):
                                                  "pick.iterations", "pick.candidates")}
     counters = {k: {"mean": (v[2] / v[1]) if v[1] else None, "ctas": v[1]}
                 for k, v in counters.items()}
+    for k in ("graphcut.max_rounds", "graphcut.max_levels"):
+        counters[k] = ctx.profile_get(k)[2]
     ctx.profile(False)
     ms_max = reduce_max(dist, ms)
     barrier(dist)

@@ -75,6 +75,7 @@ SIGNATURES = {
                                       ctypes.POINTER(ctypes.c_double), c_i64p,
                                       ctypes.POINTER(ctypes.c_double)]),
     "iq_ctx_launches": (ctypes.c_int64, [ctypes.c_void_p]),
+    "iq_set_option": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_int64]),
 }
 
 _lib = None

@@ -101,6 +101,10 @@ class Context:
     def launches(self):
         return int(load().iq_ctx_launches(self.h))
 
+    def set_option(self, name, value):
+        """Set a tuning knob of this context (launch shapes; results do not change)."""
+        check(load().iq_set_option(self.h, name.encode(), int(value)))
+
 
 def default_context():
     ctx = getattr(_local, "ctx", None)

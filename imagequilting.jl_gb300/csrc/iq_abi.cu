@@ -90,10 +90,12 @@ extern "C" int iq_profile_get(iq_ctx* ctx, const char* kernel, double* ms_total,
   int64_t n = 0;
   // counters: "graphcut.rounds", "graphcut.levels" (work = total, launches = CTAs),
   // "pick.iterations", "pick.candidates" (work = total, launches = CTAs)
-  const char* names[4] = {"graphcut.rounds", "graphcut.levels", "pick.iterations", "pick.candidates"};
-  const int idx[4][2] = {{ST_CUT_ROUNDS, ST_CUT_CTAS}, {ST_CUT_LEVELS, ST_CUT_CTAS},
-                         {ST_PICK_ITERS, ST_PICK_CTAS}, {ST_PICK_CAND, ST_PICK_CTAS}};
-  for (int i = 0; i < 4; ++i)
+  const char* names[6] = {"graphcut.rounds", "graphcut.levels", "pick.iterations",
+                          "pick.candidates", "graphcut.max_rounds", "graphcut.max_levels"};
+  const int idx[6][2] = {{ST_CUT_ROUNDS, ST_CUT_CTAS}, {ST_CUT_LEVELS, ST_CUT_CTAS},
+                         {ST_PICK_ITERS, ST_PICK_CTAS}, {ST_PICK_CAND, ST_PICK_CTAS},
+                         {ST_CUT_MAXROUNDS, ST_CUT_CTAS}, {ST_CUT_MAXLEVELS, ST_CUT_CTAS}};
+  for (int i = 0; i < 6; ++i)
     if (!strcmp(kernel, names[i])) {
       unsigned long long h[ST_COUNT];
       IQ_CUDA_OK(cudaMemcpy(h, ctx->d_stats, sizeof(h), cudaMemcpyDeviceToHost));
@@ -172,6 +174,27 @@ extern "C" int iq_ctx_destroy(iq_ctx* ctx) {
 }
 
 extern "C" void* iq_ctx_stream(iq_ctx* ctx) { return ctx ? (void*)ctx->stream : nullptr; }
+
+extern "C" int iq_set_option(iq_ctx* ctx, const char* name, int64_t value) {
+  if (!ctx || !name) return iq_set_error(IQ_ERR_ARG, "null argument");
+  if (!strcmp(name, "graphcut.gr_period")) {
+    if (value < 1 || value > 1 << 20) return iq_set_error(IQ_ERR_ARG, "gr_period out of range");
+    ctx->cut_gr_period = (int)value;
+    return IQ_OK;
+  }
+  if (!strcmp(name, "graphcut.threads")) {
+    if (value != 256 && value != 512 && value != 1024)
+      return iq_set_error(IQ_ERR_ARG, "graphcut.threads must be 256, 512 or 1024");
+    ctx->cut_threads = (int)value;
+    return IQ_OK;
+  }
+  if (!strcmp(name, "sim.level_chunk")) {
+    if (value < 1 || value > 4096) return iq_set_error(IQ_ERR_ARG, "level_chunk out of range");
+    ctx->level_chunk = value;
+    return IQ_OK;
+  }
+  return iq_set_error(IQ_ERR_ARG, "unknown option '%s'", name);
+}
 
 // ---- training image --------------------------------------------------------------------
 static int read_dims(int32_t ndim, const int64_t* size, Dim3& d) {
@@ -271,17 +294,16 @@ extern "C" int iq_fastdistance(iq_ctx* ctx, const int64_t* tilesize, int32_t ntm
   if (K) IQ_CUDA_OK(cudaMemcpyAsync(d_kl, kl.data(), sizeof(uint32_t) * K, cudaMemcpyHostToDevice, ctx->stream));
   if ((rc = iq_launch_disabled(ctx, ctx->d_nanii, ctx->ti, t, d_dis))) return rc;
   GatherLaunch G;
-  G.grid = d_tmpl; G.grid_dims = t; G.grid_stride = T; G.start0 = 0;
-  G.K = K; G.klist = d_kl; G.ntmpl = ntmpl; G.rpad = rpad; G.tv = d_tv; G.b2 = d_b2;
+  G.grid = d_tmpl; G.grid_dims = t; G.grid_stride = T;
+  G.ntmpl = ntmpl; G.rpad = rpad;
+  G.t0 = GatherTask{d_kl, K, 0, nullptr, d_tv, d_b2, nullptr};
   if ((rc = iq_launch_gather(ctx, G))) return rc;
   CorrLaunch C;
-  C.img = ctx->d_ti; C.img_dims = ctx->ti; C.out_dims = od; C.K = K; C.klist = d_kl;
-  C.tv = d_tv; C.rpad = rpad; C.ntmpl = ntmpl; C.b2 = d_b2;
-  if (full) {
-    C.a2.ii = ctx->d_ti2ii;
-    C.a2.tile[0] = t.x; C.a2.tile[1] = t.y; C.a2.tile[2] = t.z;
-  }
-  C.disabled = d_dis; C.out = d_out; C.out_stride = P;
+  C.img = ctx->d_ti; C.img_dims = ctx->ti; C.out_dims = od; C.tile = t;
+  C.rpad = rpad; C.ntmpl = ntmpl; C.out_stride = P; C.disabled = d_dis;
+  // all-ones mask: A^2 from the integral image (the full tile, no inner box); otherwise summed
+  C.t0 = CorrTask{d_kl, K, d_tv, d_b2, full ? ctx->d_ti2ii : nullptr, {0, 0, 0}, {0, 0, 0},
+                  d_out, nullptr};
   if ((rc = iq_launch_corr(ctx, C))) return rc;
   IQ_CUDA_OK(cudaMemcpyAsync(out, d_out, sizeof(float) * P * ntmpl, cudaMemcpyDefault, ctx->stream));
   IQ_CUDA_OK(cudaStreamSynchronize(ctx->stream));
@@ -305,10 +327,6 @@ extern "C" int iq_finddisabled(iq_ctx* ctx, const int64_t* tilesize, uint8_t* ou
   IQ_CUDA_OK(cudaStreamSynchronize(ctx->stream));
   return IQ_OK;
 }
-
-// relaxation sizes of src/relaxation.jl:11-36 for a given npatterns
-void iq_relax_sizes(int64_t npat, double tol, int64_t& dbnorm, int64_t& dbzero, int& nnorm,
-                    int64_t* seqnorm, int& nzero, int64_t* seqzero);
 
 // ---- pick ------------------------------------------------------------------------------
 extern "C" int iq_pick(iq_ctx* ctx, const float* D, int64_t P, int32_t naux,
@@ -358,13 +376,15 @@ extern "C" int iq_pick(iq_ctx* ctx, const float* D, int64_t P, int32_t naux,
   IQ_CUDA_OK(cudaMemcpyAsync(d_mm, hmm.data(), sizeof(unsigned) * 2 * nsrc, cudaMemcpyHostToDevice, ctx->stream));
   IQ_CUDA_OK(cudaMemsetAsync(ctx->d_status, 0, sizeof(int), ctx->stream));
   PickLaunch L;
-  L.P = P; L.npat = npat; L.tol = tol; L.seed = seed; L.tile = tile; L.real0 = real; L.nreal = 1;
-  L.D0 = d_src; L.D0_rstride = 0; L.mm0 = d_mm; L.mm0_rstride = 0;
-  L.naux = naux;
+  L.P = P; L.npat = npat; L.tol = tol; L.seed = seed; L.real0 = real; L.nreal = 1; L.ntask = 1;
+  L.t0.D0 = d_src; L.t0.D0_rs = 0; L.t0.mm0 = d_mm; L.t0.mm0_rs = 0;
+  L.t0.naux = naux;
+  L.t0.tile = tile;
   for (int j = 0; j < naux; ++j) {
-    L.aux[j] = d_src + (j + 1) * P; L.aux_rstride[j] = 0;
-    L.aux_mm[j] = d_mm + 2 * (j + 1); L.aux_mm_rstride[j] = 0;
+    L.t0.aux[j] = d_src + (j + 1) * P; L.t0.aux_rs[j] = 0;
+    L.t0.aux_mm[j] = d_mm + 2 * (j + 1); L.t0.aux_mm_rs[j] = 0;
   }
+  L.naux_max = naux;
   if (naux > 0 && npat > 0)
     iq_relax_sizes(npat, tol, L.dbsize_norm, L.dbsize_zero, L.nseq_norm, L.seq_norm, L.nseq_zero,
                    L.seq_zero);
@@ -403,23 +423,27 @@ extern "C" int iq_graphcut(iq_ctx* ctx, const float* A, const float* B, int32_t 
   const int64_t n = d.vol();
   if (n >= ((int64_t)1 << 24)) return iq_set_error(IQ_ERR_LIMIT, "slab above 2^24 nodes");
   float* dA = (float*)iq_scratch(ctx, S_TMP0, sizeof(float) * n * 2);
-  uint8_t* dout = (uint8_t*)iq_scratch(ctx, S_CUTBUF, (size_t)n);
+  uint8_t* dout = (uint8_t*)iq_scratch(ctx, S_CUTBUF, (size_t)n * 6);
   void* scr = iq_scratch(ctx, S_CUTSCR, iq_cut_scratch_bytes(n));
   if (!dA || !dout || !scr) return IQ_ERR_ALLOC;
   IQ_CUDA_OK(cudaMemcpyAsync(dA, A, sizeof(float) * n, cudaMemcpyDefault, ctx->stream));
   IQ_CUDA_OK(cudaMemcpyAsync(dA + n, B, sizeof(float) * n, cudaMemcpyDefault, ctx->stream));
   IQ_CUDA_OK(cudaMemsetAsync(ctx->d_status, 0, sizeof(int), ctx->stream));
   CutLaunch L;
-  L.nslab = 1;
-  L.slab[0].dim = dim;
-  L.slab[0].next = 0;
-  L.slab[0].off[0] = L.slab[0].off[1] = L.slab[0].off[2] = 0;
-  L.slab[0].ext[0] = d.x; L.slab[0].ext[1] = d.y; L.slab[0].ext[2] = d.z;
-  L.nreal = 1;
+  L.t0.start = 0;
+  L.t0.nslab = 1;
+  L.t0.slab[0].dim = dim;
+  L.t0.slab[0].next = 0;
+  L.t0.slab[0].off[0] = L.t0.slab[0].off[1] = L.t0.slab[0].off[2] = 0;
+  L.t0.slab[0].ext[0] = d.x; L.t0.slab[0].ext[1] = d.y; L.t0.slab[0].ext[2] = d.z;
+  L.nreal = 1; L.ntask = 1;
   L.A = dA; L.B = dA + n;
   L.out = dout; L.slabmax = n;
   L.scratch = scr; L.scratch_per_cta = (int64_t)iq_cut_scratch_bytes(n);
   L.status = ctx->d_status;
+  L.stats = ctx->prof ? ctx->d_stats : nullptr;
+  L.gr_period = ctx->cut_gr_period;
+  L.threads = ctx->cut_threads;
   if ((rc = iq_launch_cut(ctx, L))) return rc;
   int st = 0;
   IQ_CUDA_OK(cudaMemcpyAsync(mask, dout, (size_t)n, cudaMemcpyDefault, ctx->stream));

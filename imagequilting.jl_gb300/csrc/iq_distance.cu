@@ -26,19 +26,12 @@ struct CorrArgs {
   const float* img;
   int64_t ix, iy;             // image extents (x, y)
   int64_t dx, dy, P;          // valid extents and their product
-  int K;
-  const uint32_t* klist;
-  const float* tv;
   int rpad, ntmpl;
-  const double* b2;
-  const double* ii;           // integral image (nullptr: direct A2)
   int64_t tx, ty, tz;         // tile
-  int64_t lox, loy, loz, hix, hiy, hiz;
-  int inner;                  // inner box non-empty
   const uint8_t* disabled;
-  float* out;
   int64_t out_stride;
-  unsigned* minmax;
+  CorrTask t0;                // used when tasks is null
+  const CorrTask* tasks;      // one task per blockIdx.z
 };
 
 __device__ __forceinline__ double box_sum(const double* __restrict__ ii, int64_t sx, int64_t sxy,
@@ -65,7 +58,8 @@ __global__ void __launch_bounds__(CORR_THREADS) corr_kernel(const CorrArgs a) {
 
   const int tid = threadIdx.x;
   const int rg = blockIdx.y;
-  const bool direct = a.ii == nullptr;
+  const CorrTask t = a.tasks ? a.tasks[blockIdx.z] : a.t0;
+  const bool direct = t.ii == nullptr;
   const int64_t pbase = (int64_t)blockIdx.x * (CORR_THREADS * PJ);
 
   const float* ptr[PJ];
@@ -89,16 +83,16 @@ __global__ void __launch_bounds__(CORR_THREADS) corr_kernel(const CorrArgs a) {
     for (int r = 0; r < RT; ++r) acc[j][r] = 0.f;
   }
 
-  for (int kc0 = 0; kc0 < a.K; kc0 += CORR_KC) {
-    const int nk = min(CORR_KC, a.K - kc0);
+  for (int kc0 = 0; kc0 < t.K; kc0 += CORR_KC) {
+    const int nk = min(CORR_KC, t.K - kc0);
     __syncthreads();
     for (int i = tid; i < nk; i += CORR_THREADS) {
-      uint32_t k = a.klist[kc0 + i];
+      uint32_t k = t.klist[kc0 + i];
       s_off[i] = (int32_t)(kx_of(k) + a.ix * (ky_of(k) + a.iy * (int64_t)kz_of(k)));
     }
     for (int i = tid; i < nk * RT; i += CORR_THREADS) {
       int kk = i / RT, r = i % RT;
-      s_tv[i] = a.tv[(int64_t)(kc0 + kk) * a.rpad + rg * RT + r];
+      s_tv[i] = t.tv[(int64_t)(kc0 + kk) * a.rpad + rg * RT + r];
     }
     __syncthreads();
 #pragma unroll 2
@@ -130,6 +124,7 @@ __global__ void __launch_bounds__(CORR_THREADS) corr_kernel(const CorrArgs a) {
 #pragma unroll
   for (int r = 0; r < RT; ++r) { mn[r] = 0x7F800000u; mx[r] = 0u; }
   const int64_t sx = a.ix + 1, sxy = (a.ix + 1) * (a.iy + 1);
+  const bool inner = t.hi[0] > t.lo[0] && t.hi[1] > t.lo[1] && t.hi[2] > t.lo[2];
 #pragma unroll
   for (int j = 0; j < PJ; ++j) {
     const int64_t p = pos[j];
@@ -140,30 +135,30 @@ __global__ void __launch_bounds__(CORR_THREADS) corr_kernel(const CorrArgs a) {
     } else {
       int64_t x = p % a.dx, row = p / a.dx;
       int64_t y = row % a.dy, z = row / a.dy;
-      A2 = box_sum(a.ii, sx, sxy, x, y, z, a.tx, a.ty, a.tz);
-      if (a.inner)
-        A2 -= box_sum(a.ii, sx, sxy, x + a.lox, y + a.loy, z + a.loz, a.hix - a.lox,
-                      a.hiy - a.loy, a.hiz - a.loz);
+      A2 = box_sum(t.ii, sx, sxy, x, y, z, a.tx, a.ty, a.tz);
+      if (inner)
+        A2 -= box_sum(t.ii, sx, sxy, x + t.lo[0], y + t.lo[1], z + t.lo[2], t.hi[0] - t.lo[0],
+                      t.hi[1] - t.lo[1], t.hi[2] - t.lo[2]);
     }
     const bool dis = a.disabled != nullptr && a.disabled[p];
 #pragma unroll
     for (int r = 0; r < RT; ++r) {
-      const int t = rg * RT + r;
-      if (t >= a.ntmpl) continue;
+      const int tt = rg * RT + r;
+      if (tt >= a.ntmpl) continue;
       float df;
       if (dis) {
         df = __int_as_float(0x7F800000);
       } else {
-        double d = A2 - 2.0 * (double)acc[j][r] + a.b2[t];
+        double d = A2 - 2.0 * (double)acc[j][r] + t.b2[tt];
         df = (float)fabs(d);
       }
-      a.out[(int64_t)t * a.out_stride + p] = df;
+      t.out[(int64_t)tt * a.out_stride + p] = df;
       unsigned b = __float_as_uint(df);
       mn[r] = min(mn[r], b);
       if (b < 0x7F800000u) mx[r] = max(mx[r], b);
     }
   }
-  if (a.minmax == nullptr) return;
+  if (t.minmax == nullptr) return;
   const int lane = tid & 31, warp = tid >> 5;
 #pragma unroll
   for (int r = 0; r < RT; ++r) {
@@ -173,23 +168,23 @@ __global__ void __launch_bounds__(CORR_THREADS) corr_kernel(const CorrArgs a) {
   }
   __syncthreads();
   if (tid < RT) {
-    const int t = rg * RT + tid;
-    if (t < a.ntmpl) {
+    const int tt = rg * RT + tid;
+    if (tt < a.ntmpl) {
       unsigned m1 = 0x7F800000u, m2 = 0u;
       for (int w = 0; w < CORR_THREADS / 32; ++w) {
         m1 = min(m1, s_min[w][tid]);
         m2 = max(m2, s_max[w][tid]);
       }
-      atomicMin(a.minmax + 2 * t, m1);
-      atomicMax(a.minmax + 2 * t + 1, m2);
+      atomicMin(t.minmax + 2 * tt, m1);
+      atomicMax(t.minmax + 2 * tt + 1, m2);
     }
   }
 }
 
 template <int RT, int PJ>
-void launch_corr_t(const CorrArgs& a, cudaStream_t s) {
+void launch_corr_t(const CorrArgs& a, int ntask, cudaStream_t s) {
   dim3 grid((unsigned)((a.P + CORR_THREADS * PJ - 1) / (CORR_THREADS * PJ)),
-            (unsigned)(a.rpad / RT));
+            (unsigned)(a.rpad / RT), (unsigned)ntask);
   corr_kernel<RT, PJ><<<grid, CORR_THREADS, 0, s>>>(a);
 }
 
@@ -199,36 +194,32 @@ struct GatherArgs {
   int64_t gx, gy;
   int64_t gstride;
   const int64_t* starts;
-  int64_t start0;
-  int K;
-  const uint32_t* klist;
-  const float* kval;
   int ntmpl, rpad;
-  float* tv;
-  double* b2;
-  unsigned* minmax;
+  GatherTask t0;
+  const GatherTask* tasks;
 };
 
 __global__ void gather_kernel(const GatherArgs g) {
   const int t = blockIdx.x;  // template (rpad blocks)
+  const GatherTask k = g.tasks ? g.tasks[blockIdx.y] : g.t0;
   __shared__ double s_red[32];
   double sq = 0.0;
   if (t < g.ntmpl) {
-    const int64_t st = g.starts ? g.starts[t] : g.start0;
+    const int64_t st = g.starts ? g.starts[t] : k.start;
     const float* base = g.grid ? g.grid + (int64_t)t * g.gstride + st : nullptr;
-    for (int k = threadIdx.x; k < g.K; k += blockDim.x) {
+    for (int i = threadIdx.x; i < k.K; i += blockDim.x) {
       float v;
-      if (g.kval) {
-        v = g.kval[k];
+      if (k.kval) {
+        v = k.kval[i];
       } else {
-        uint32_t kk = g.klist[k];
+        uint32_t kk = k.klist[i];
         v = base[kx_of(kk) + g.gx * (ky_of(kk) + g.gy * (int64_t)kz_of(kk))];
       }
-      g.tv[(int64_t)k * g.rpad + t] = v;
+      k.tv[(int64_t)i * g.rpad + t] = v;
       sq += (double)v * (double)v;
     }
   } else {
-    for (int k = threadIdx.x; k < g.K; k += blockDim.x) g.tv[(int64_t)k * g.rpad + t] = 0.f;
+    for (int i = threadIdx.x; i < k.K; i += blockDim.x) k.tv[(int64_t)i * g.rpad + t] = 0.f;
   }
   // block reduction of the squares (fixed order: warp shuffles then warps in order)
   for (int o = 16; o > 0; o >>= 1) sq += __shfl_down_sync(0xffffffffu, sq, o);
@@ -237,10 +228,10 @@ __global__ void gather_kernel(const GatherArgs g) {
   if (threadIdx.x == 0) {
     double s = 0.0;
     for (int w = 0; w < (int)(blockDim.x >> 5); ++w) s += s_red[w];
-    g.b2[t] = t < g.ntmpl ? s : 0.0;
-    if (g.minmax && t < g.ntmpl) {
-      g.minmax[2 * t] = 0x7F800000u;
-      g.minmax[2 * t + 1] = 0u;
+    k.b2[t] = t < g.ntmpl ? s : 0.0;
+    if (k.minmax && t < g.ntmpl) {
+      k.minmax[2 * t] = 0x7F800000u;
+      k.minmax[2 * t + 1] = 0u;
     }
   }
 }
@@ -320,54 +311,45 @@ int iq_launch_corr(iq_ctx* ctx, const CorrLaunch& L) {
   a.dx = L.out_dims.x;
   a.dy = L.out_dims.y;
   a.P = L.out_dims.vol();
-  a.K = L.K;
-  a.klist = L.klist;
-  a.tv = L.tv;
   a.rpad = L.rpad;
   a.ntmpl = L.ntmpl;
-  a.b2 = L.b2;
-  a.ii = L.a2.ii;
-  a.tx = L.a2.tile[0]; a.ty = L.a2.tile[1]; a.tz = L.a2.tile[2];
-  a.lox = L.a2.lo[0]; a.loy = L.a2.lo[1]; a.loz = L.a2.lo[2];
-  a.hix = L.a2.hi[0]; a.hiy = L.a2.hi[1]; a.hiz = L.a2.hi[2];
-  a.inner = (a.hix > a.lox && a.hiy > a.loy && a.hiz > a.loz) ? 1 : 0;
+  a.tx = L.tile.x; a.ty = L.tile.y; a.tz = L.tile.z;
   a.disabled = L.disabled;
-  a.out = L.out;
   a.out_stride = L.out_stride;
-  a.minmax = L.minmax;
-  if (a.P <= 0 || L.ntmpl <= 0) return IQ_OK;
+  a.t0 = L.t0;
+  a.tasks = L.tasks;
+  if (a.P <= 0 || L.ntmpl <= 0 || L.ntask <= 0) return IQ_OK;
   const int rt = iq_register_tile(L.rpad);
   iq_timer_start(ctx, "corr");
   switch (rt) {
-    case 16: launch_corr_t<16, 4>(a, ctx->stream); break;
-    case 8: launch_corr_t<8, 4>(a, ctx->stream); break;
-    case 4: launch_corr_t<4, 8>(a, ctx->stream); break;
-    case 2: launch_corr_t<2, 8>(a, ctx->stream); break;
-    default: launch_corr_t<1, 8>(a, ctx->stream); break;
+    case 16: launch_corr_t<16, 4>(a, L.ntask, ctx->stream); break;
+    case 8: launch_corr_t<8, 4>(a, L.ntask, ctx->stream); break;
+    case 4: launch_corr_t<4, 8>(a, L.ntask, ctx->stream); break;
+    case 2: launch_corr_t<2, 8>(a, L.ntask, ctx->stream); break;
+    default: launch_corr_t<1, 8>(a, L.ntask, ctx->stream); break;
   }
-  iq_timer_stop(ctx, "corr", 2.0 * (double)a.P * (double)a.K * (double)L.ntmpl);
+  const double flops = L.flops > 0 ? L.flops
+                                   : 2.0 * (double)a.P * (double)L.t0.K * (double)L.ntmpl;
+  iq_timer_stop(ctx, "corr", flops);
   iq_count(ctx);
   IQ_CUDA_OK(cudaGetLastError());
   return IQ_OK;
 }
 
 int iq_launch_gather(iq_ctx* ctx, const GatherLaunch& G) {
+  if (G.ntask <= 0) return IQ_OK;
   GatherArgs g;
   g.grid = G.grid;
   g.gx = G.grid_dims.x;
   g.gy = G.grid_dims.y;
   g.gstride = G.grid_stride;
   g.starts = G.starts;
-  g.start0 = G.start0;
-  g.K = G.K;
-  g.klist = G.klist;
-  g.kval = G.kval;
   g.ntmpl = G.ntmpl;
   g.rpad = G.rpad;
-  g.tv = G.tv;
-  g.b2 = G.b2;
-  g.minmax = G.minmax;
-  gather_kernel<<<G.rpad, 256, 0, ctx->stream>>>(g);
+  g.t0 = G.t0;
+  g.tasks = G.tasks;
+  dim3 grid((unsigned)G.rpad, (unsigned)G.ntask);
+  gather_kernel<<<grid, 256, 0, ctx->stream>>>(g);
   iq_count(ctx);
   IQ_CUDA_OK(cudaGetLastError());
   return IQ_OK;

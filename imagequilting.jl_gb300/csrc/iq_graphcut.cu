@@ -21,13 +21,13 @@
 
 namespace {
 
-constexpr int CUT_THREADS = 512;
-constexpr int GR_PERIOD = 32;
+constexpr int CUT_MAX_THREADS = 1024;
 
 struct CutArgs {
-  CutSlab slab[6];
-  int nslab;
-  const float* sim; int64_t sx, sy; int64_t sim_rs; int64_t tile_start;
+  StepTask t0;                 // used when tasks is null
+  const StepTask* tasks;
+  int nreal;                   // CTA (s, y): slab s of realization y % nreal of task y / nreal
+  const float* sim; int64_t sx, sy; int64_t sim_rs;
   const float* ti; int64_t tix, tiy; int64_t dx, dy;
   const int64_t* rind;
   const float* A; const float* B;
@@ -36,6 +36,7 @@ struct CutArgs {
   int* status;
   int round_cap;
   unsigned long long* stats;
+  int gr_period;
 };
 
 __device__ __forceinline__ long long dbits(double x) { return __double_as_longlong(x); }
@@ -104,11 +105,15 @@ __device__ int global_relabel(const Graph& g, int* hc) {
   return g.NH;
 }
 
-__global__ void __launch_bounds__(CUT_THREADS) cut_kernel(const CutArgs a) {
+__global__ void __launch_bounds__(CUT_MAX_THREADS) cut_kernel(const CutArgs a) {
   extern __shared__ __align__(16) char smem[];
   const int s_id = blockIdx.x;
-  const int r = blockIdx.y;
-  const CutSlab sl = a.slab[s_id];
+  const int y = blockIdx.y;
+  const int r = y % a.nreal;
+  const StepTask& tk = a.tasks ? a.tasks[y / a.nreal] : a.t0;
+  if (s_id >= tk.nslab) return;
+  const CutSlab sl = tk.slab[s_id];
+  const int64_t tile_start = tk.start;
   Graph g;
   g.ext[0] = (int)sl.ext[0]; g.ext[1] = (int)sl.ext[1]; g.ext[2] = (int)sl.ext[2];
   g.st[0] = 1; g.st[1] = g.ext[0]; g.st[2] = g.ext[0] * g.ext[1];
@@ -137,10 +142,10 @@ __global__ void __launch_bounds__(CUT_THREADS) cut_kernel(const CutArgs a) {
   // ---- load A (simulation grid) and B (training image at the drawn pattern) ----
   int64_t bstart = 0;
   if (!a.A) {
-    const int64_t ri = a.rind[r];
+    const int64_t ri = a.rind[y];
     if (ri < 0) {  // pick failed: no cut (status already set)
-      for (int64_t u = threadIdx.x; u < n; u += blockDim.x)
-        a.out[((int64_t)r * a.nslab + s_id) * a.slabmax + u] = 0;
+      for (int u = threadIdx.x; u < n; u += blockDim.x)
+        a.out[((int64_t)y * 6 + s_id) * a.slabmax + u] = 0;
       return;
     }
     const int64_t rx = ri % a.dx, rr = ri / a.dx, ry = rr % a.dy, rz = rr / a.dy;
@@ -162,7 +167,7 @@ __global__ void __launch_bounds__(CUT_THREADS) cut_kernel(const CutArgs a) {
       Bv[u] = a.B[u];
     } else {
       const int64_t lx = sl.off[0] + x, ly = sl.off[1] + y, lz = sl.off[2] + z;
-      Av[u] = a.sim[(int64_t)r * a.sim_rs + a.tile_start + lx + a.sx * (ly + a.sy * lz)];
+      Av[u] = a.sim[(int64_t)r * a.sim_rs + tile_start + lx + a.sx * (ly + a.sy * lz)];
       Bv[u] = a.ti[bstart + lx + a.tix * (ly + a.tiy * lz)];
     }
   }
@@ -277,7 +282,7 @@ __global__ void __launch_bounds__(CUT_THREADS) cut_kernel(const CutArgs a) {
       ++round;
       if (!active) break;
       if (round >= a.round_cap) { capped = true; break; }
-      if (round % GR_PERIOD == 0) {
+      if (round % a.gr_period == 0) {
         levels += global_relabel(g, g.h[cur]);
         __syncthreads();
       }
@@ -294,7 +299,7 @@ __global__ void __launch_bounds__(CUT_THREADS) cut_kernel(const CutArgs a) {
   }
   // ---- mask: not sink side ----
   const int* hc = g.h[cur];
-  uint8_t* out = a.out + ((int64_t)r * a.nslab + s_id) * a.slabmax;
+  uint8_t* out = a.out + ((int64_t)y * 6 + s_id) * a.slabmax;
   for (int u = threadIdx.x; u < n; u += blockDim.x) {
     const int k = g.kind(u);
     int M = k == 1 ? 1 : (k == 2 ? 0 : (hc[u] >= g.NH ? 1 : 0));
@@ -312,12 +317,13 @@ size_t iq_cut_scratch_bytes(int64_t nodes) {
 }
 
 int iq_launch_cut(iq_ctx* ctx, const CutLaunch& L) {
-  if (L.nslab <= 0 || L.nreal <= 0) return IQ_OK;
+  const int nslab_max = L.tasks ? L.nslab_max : L.t0.nslab;
+  if (nslab_max <= 0 || L.nreal <= 0 || L.ntask <= 0) return IQ_OK;
   CutArgs a;
-  for (int i = 0; i < 6; ++i) a.slab[i] = L.slab[i];
-  a.nslab = L.nslab;
+  a.t0 = L.t0;
+  a.tasks = L.tasks;
+  a.nreal = L.nreal;
   a.sim = L.sim; a.sx = L.sim_dims.x; a.sy = L.sim_dims.y; a.sim_rs = L.sim_rstride;
-  a.tile_start = L.tile_start;
   a.ti = L.ti; a.tix = L.ti_dims.x; a.tiy = L.ti_dims.y;
   a.dx = L.dist_dims.x; a.dy = L.dist_dims.y;
   a.rind = L.rind;
@@ -326,9 +332,8 @@ int iq_launch_cut(iq_ctx* ctx, const CutLaunch& L) {
   a.status = L.status;
   a.round_cap = L.round_cap;
   a.stats = L.stats;
-  int64_t nmax = 0;
-  for (int i = 0; i < L.nslab; ++i)
-    nmax = std::max<int64_t>(nmax, L.slab[i].ext[0] * L.slab[i].ext[1] * L.slab[i].ext[2]);
+  a.gr_period = L.gr_period > 0 ? L.gr_period : 32;
+  const int64_t nmax = L.slabmax;
   const size_t need = iq_cut_scratch_bytes(nmax);
   static int smem_limit = -1;
   if (smem_limit < 0) {
@@ -350,15 +355,11 @@ int iq_launch_cut(iq_ctx* ctx, const CutLaunch& L) {
     a.scratch = (char*)L.scratch;
     a.scratch_per_cta = L.scratch_per_cta;
   }
-  dim3 grid((unsigned)L.nslab, (unsigned)L.nreal);
+  const int threads = (L.threads == 256 || L.threads == 1024) ? L.threads : 512;
+  dim3 grid((unsigned)nslab_max, (unsigned)(L.ntask * L.nreal));
   iq_timer_start(ctx, "graphcut");
-  cut_kernel<<<grid, CUT_THREADS, dyn, ctx->stream>>>(a);
-  double edges = 0;
-  for (int i = 0; i < L.nslab; ++i) {
-    const int64_t* e = L.slab[i].ext;
-    edges += (double)((e[0] - 1) * e[1] * e[2] + e[0] * (e[1] - 1) * e[2] + e[0] * e[1] * (e[2] - 1));
-  }
-  iq_timer_stop(ctx, "graphcut", edges * L.nreal);
+  cut_kernel<<<grid, threads, dyn, ctx->stream>>>(a);
+  iq_timer_stop(ctx, "graphcut", 0);
   iq_count(ctx);
   IQ_CUDA_OK(cudaGetLastError());
   return IQ_OK;

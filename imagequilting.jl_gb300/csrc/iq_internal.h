@@ -1,4 +1,9 @@
 // Internal declarations shared by the translation units of libiqgpu.so.
+//
+// Kernels work on batches of "tasks": all the tiles of one dependency level of the tile path
+// (tiles whose regions do not overlap run together) times all realizations. A launch either
+// carries one task by value (t0, for the per-operation entry points) or points at a device
+// array of tasks uploaded once per simulation.
 #pragma once
 
 #include <map>
@@ -36,18 +41,23 @@ struct iq_ctx {
   std::map<std::string, IqTimer> timers;
   int64_t launches = 0;         // kernels launched by this context
   // device counters filled while profiling: [0] cut rounds, [1] cut BFS levels, [2] cut CTAs,
-  // [3] pick relaxation iterations, [4] pick candidates, [5] pick CTAs
+  // [3] pick relaxation iterations, [4] pick candidates, [5] pick CTAs, [6] max cut rounds,
+  // [7] max cut BFS levels
   unsigned long long* d_stats = nullptr;
+  // tuning knobs (iq_set_option)
+  int cut_gr_period = 32;
+  int cut_threads = 512;
+  int64_t level_chunk = 64;     // most tiles of one dependency level launched together
 };
 enum IqStat { ST_CUT_ROUNDS = 0, ST_CUT_LEVELS, ST_CUT_CTAS, ST_PICK_ITERS, ST_PICK_CAND,
-              ST_PICK_CTAS, ST_COUNT };
+              ST_PICK_CTAS, ST_CUT_MAXROUNDS, ST_CUT_MAXLEVELS, ST_COUNT };
 
 // scratch slot ids
 enum IqSlot {
   S_SIM = 0, S_CUT, S_D, S_DHARD, S_SOFT, S_TV, S_B2, S_KLIST, S_MINMAX, S_PICK_CAND,
   S_PICK_K0, S_PICK_V0, S_PICK_K1, S_PICK_V1, S_PICK_W, S_PICK_PROD, S_RIND, S_NCAND,
   S_CUTBUF, S_CUTSCR, S_DIS, S_AUX, S_AUXTI, S_AUXII, S_HARDLIST, S_HARDPTS, S_OUT,
-  S_TMP0, S_TMP1, S_TMP2, S_STARTS, S_SOFTTV, S_SOFTB2, S_VOX, S_COUNT
+  S_TMP0, S_TMP1, S_TMP2, S_STARTS, S_SOFTMM, S_TASKS, S_VOX, S_COUNT
 };
 
 // device scratch of at least `bytes` in slot `slot` (contents undefined); nullptr on failure
@@ -72,49 +82,55 @@ IQ_HD int kx_of(uint32_t k) { return (int)(k & 1023u); }
 IQ_HD int ky_of(uint32_t k) { return (int)((k >> 10) & 1023u); }
 IQ_HD int kz_of(uint32_t k) { return (int)(k >> 20); }
 
-// A^2 term of the distance: either the integral-image box difference (full tile minus an
-// inner box [lo, hi)), or summed directly over the offset list.
-struct A2Spec {
-  const double* ii = nullptr;  // integral image of img^2; nullptr => direct accumulation
-  int64_t tile[3] = {0, 0, 0};
-  int64_t lo[3] = {0, 0, 0};   // inner (excluded) box; empty when lo >= hi in some dim
-  int64_t hi[3] = {0, 0, 0};
+// One batch of templates that share a mask (one tile of a level).
+struct CorrTask {
+  const uint32_t* klist;  // K packed offsets of the mask
+  int K;
+  const float* tv;        // K x rpad template values (weights applied)
+  const double* b2;       // rpad: sum of squared template values
+  const double* ii;       // integral image of img^2 (A^2 = full tile - inner box); nullptr:
+                          // A^2 summed over the offset list
+  int64_t lo[3], hi[3];   // inner box excluded from the full tile (empty if lo >= hi)
+  float* out;             // ntmpl maps of out_stride floats
+  unsigned* minmax;       // ntmpl x [min bits, max finite bits] (nullable)
 };
 
 struct CorrLaunch {
   const float* img = nullptr;  // image, extents `img_dims`
   Dim3 img_dims{1, 1, 1};
   Dim3 out_dims{1, 1, 1};      // valid extent
-  int K = 0;                   // offsets in the mask
-  const uint32_t* klist = nullptr;  // K packed offsets
-  const float* tv = nullptr;   // K x rpad template values (weights applied)
+  Dim3 tile{1, 1, 1};
   int rpad = 0;                // row length of tv (multiple of the register tile)
-  int ntmpl = 0;               // templates actually computed (<= rpad)
-  const double* b2 = nullptr;  // per template: sum of squared template values
-  A2Spec a2;
-  const uint8_t* disabled = nullptr;  // 1 -> +Inf (nullable)
-  float* out = nullptr;        // ntmpl x P
+  int ntmpl = 0;               // templates computed per task (<= rpad)
   int64_t out_stride = 0;      // floats between templates in `out`
-  unsigned* minmax = nullptr;  // per template: [min bits, max finite bits] (nullable)
+  const uint8_t* disabled = nullptr;  // 1 -> +Inf (nullable)
+  int ntask = 1;
+  CorrTask t0{};               // the task when `tasks` is null
+  const CorrTask* tasks = nullptr;  // device array of ntask tasks
+  double flops = 0;            // algorithmic FLOPs of the launch (profiling)
 };
-
 int iq_launch_corr(iq_ctx* ctx, const CorrLaunch& L);
 
-// gather of template values tv[k][t] = grid_t[start_t + k] for the packed offsets
+// Gather of template values tv[k][t] = grid_t[start + k] for the packed offsets.
+struct GatherTask {
+  const uint32_t* klist;
+  int K;
+  int64_t start;          // linear origin of the tile in the grid
+  const float* kval;      // per-offset values instead of a grid (hard data); nullable
+  float* tv;              // K x rpad
+  double* b2;             // rpad
+  unsigned* minmax;       // reset to [+Inf bits, 0] per template (nullable)
+};
 struct GatherLaunch {
-  const float* grid = nullptr;  // base grid
+  const float* grid = nullptr;      // base grid
   Dim3 grid_dims{1, 1, 1};
-  int64_t grid_stride = 0;      // floats between consecutive templates' grids
-  const int64_t* starts = nullptr;  // per template start (linear), device; nullable
-  int64_t start0 = 0;           // start when `starts` is null
-  int K = 0;
-  const uint32_t* klist = nullptr;
-  const float* kval = nullptr;  // per-offset values instead of a grid (hard data); nullable
+  int64_t grid_stride = 0;          // floats between consecutive templates' grids
+  const int64_t* starts = nullptr;  // per template start (device), overrides task.start
   int ntmpl = 0;
   int rpad = 0;
-  float* tv = nullptr;          // K x rpad
-  double* b2 = nullptr;         // rpad
-  unsigned* minmax = nullptr;   // reset to [+Inf bits, 0] per template (nullable)
+  int ntask = 1;
+  GatherTask t0{};
+  const GatherTask* tasks = nullptr;
 };
 int iq_launch_gather(iq_ctx* ctx, const GatherLaunch& G);
 
@@ -128,40 +144,48 @@ int iq_launch_disabled(iq_ctx* ctx, const int32_t* d_nanii, Dim3 dims, Dim3 tile
 // ---------------------------------------------------------------------------------------
 // Pick (iq_pick.cu)
 // ---------------------------------------------------------------------------------------
+// Sources of one tile; realization r of the tile reads D0 + r * D0_rs etc.
+struct PickTask {
+  const float* D0; int64_t D0_rs;           // primary distance
+  const unsigned* mm0; int64_t mm0_rs;      // its [min, max finite] bits
+  int naux;                                 // 0: threshold pick, > 0: relaxation
+  const float* aux[IQ_MAX_AUX];
+  int64_t aux_rs[IQ_MAX_AUX];
+  const unsigned* aux_mm[IQ_MAX_AUX];
+  int64_t aux_mm_rs[IQ_MAX_AUX];
+  int64_t tile;                             // Philox counter of the draw
+};
+
 struct PickLaunch {
   int64_t P = 0;           // positions
   int64_t npat = 0;        // enabled positions (finite D)
   double tol = 0.1;
   uint64_t seed = 0;
-  int64_t tile = 0;        // tile linear index (Philox counter)
-  int64_t real0 = 0;       // realization index of CTA 0
-  int nreal = 0;           // CTAs
-  const float* D0 = nullptr;  int64_t D0_rstride = 0;  // primary source of CTA r
-  const unsigned* mm0 = nullptr; int64_t mm0_rstride = 0;  // its [min, max finite] bits
-  int naux = 0;
-  const float* aux[IQ_MAX_AUX] = {};
-  int64_t aux_rstride[IQ_MAX_AUX] = {};
-  const unsigned* aux_mm[IQ_MAX_AUX] = {};  // [min, max finite] bits of each source
-  int64_t aux_mm_rstride[IQ_MAX_AUX] = {};
+  int64_t real0 = 0;       // realization index of r = 0
+  int nreal = 0;           // realizations per task; CTA b handles task b / nreal, r = b % nreal
+  int ntask = 1;
+  int naux_max = 0;        // largest naux of the tasks
+  PickTask t0{};
+  const PickTask* tasks = nullptr;
   // relaxation sizes (src/relaxation.jl:11-36): normal and all-zero cases
   int64_t dbsize_norm = 0, dbsize_zero = 0;
   int nseq_norm = 0, nseq_zero = 0;
   int64_t seq_norm[IQ_MAX_SEQ] = {}, seq_zero[IQ_MAX_SEQ] = {};
-  // scratch, each nreal x P
+  // scratch, P entries per CTA
   int32_t* cand = nullptr;
   uint32_t *k0 = nullptr, *v0 = nullptr, *k1 = nullptr, *v1 = nullptr;
   double* w = nullptr;
   double* prod = nullptr;
-  // outputs
-  int64_t* rind = nullptr;   // per CTA
-  int64_t* ncand = nullptr;  // per CTA (nullable)
+  // outputs, one per CTA
+  int64_t* rind = nullptr;
+  int64_t* ncand = nullptr;  // nullable
   int* status = nullptr;
   unsigned long long* stats = nullptr;  // profiling counters (nullable)
 };
 int iq_launch_pick(iq_ctx* ctx, const PickLaunch& L);
 
 // ---------------------------------------------------------------------------------------
-// Graph cut (iq_graphcut.cu)
+// Graph cut (iq_graphcut.cu) and paste (iq_paste.cu)
 // ---------------------------------------------------------------------------------------
 struct CutSlab {
   int dim;          // cut dimension
@@ -170,42 +194,49 @@ struct CutSlab {
   int64_t ext[3];   // slab extents
 };
 
-struct CutLaunch {
-  int nslab = 0;
+// The overlap slabs of one tile.
+struct StepTask {
+  int64_t start;    // linear origin of the tile in the simulation grid
+  int nslab;
   CutSlab slab[6];
-  int nreal = 0;
-  // A: simulation grid of realization r at tile origin; B: TI at rind[r]
+};
+
+struct CutLaunch {
+  int nreal = 0;               // realizations per task; CTA y = task * nreal + r
+  int ntask = 1;
+  int nslab_max = 0;           // grid.x
+  StepTask t0{};
+  const StepTask* tasks = nullptr;
+  // A: simulation grid of realization r at the tile; B: TI at rind[task * nreal + r]
   const float* sim = nullptr; Dim3 sim_dims{1, 1, 1}; int64_t sim_rstride = 0;
-  int64_t tile_start = 0;     // linear index of the tile origin in sim
   const float* ti = nullptr;  Dim3 ti_dims{1, 1, 1};
   Dim3 dist_dims{1, 1, 1};
   const int64_t* rind = nullptr;
   // direct mode (iq_graphcut): A/B arrays of the slab itself
   const float* A = nullptr; const float* B = nullptr;
-  uint8_t* out = nullptr;      // nreal x nslab x slabmax bytes: keep-old flags
+  uint8_t* out = nullptr;      // (ntask * nreal) x 6 x slabmax bytes: keep-old flags
   int64_t slabmax = 0;
   void* scratch = nullptr;     // global scratch for slabs too large for shared memory
   int64_t scratch_per_cta = 0;
   int* status = nullptr;
   int round_cap = 1 << 18;
   unsigned long long* stats = nullptr;  // profiling counters (nullable)
+  int gr_period = 32;          // rounds between global relabels
+  int threads = 512;           // threads per CTA
 };
 int iq_launch_cut(iq_ctx* ctx, const CutLaunch& L);
 size_t iq_cut_scratch_bytes(int64_t nodes);
 
-// ---------------------------------------------------------------------------------------
-// Paste and finishing (iq_paste.cu)
-// ---------------------------------------------------------------------------------------
 struct PasteLaunch {
   int nreal = 0;
+  int ntask = 1;
+  StepTask t0{};
+  const StepTask* tasks = nullptr;
   float* sim = nullptr; Dim3 sim_dims{1, 1, 1}; int64_t sim_rstride = 0;
   float* cut = nullptr;       // debug cut grid (nullable)
-  int64_t tile_start = 0;
   Dim3 tile{1, 1, 1};
   const float* ti = nullptr; Dim3 ti_dims{1, 1, 1}; Dim3 dist_dims{1, 1, 1};
   const int64_t* rind = nullptr;
-  int nslab = 0;
-  CutSlab slab[6];
   const uint8_t* cutbuf = nullptr; int64_t slabmax = 0;
 };
 int iq_launch_paste(iq_ctx* ctx, const PasteLaunch& L);
@@ -221,3 +252,7 @@ int iq_launch_pad_symmetric(iq_ctx* ctx, const float* src, Dim3 src_dims, float*
                             Dim3 dst_dims);
 int iq_launch_prepare(iq_ctx* ctx, float* data, int64_t n, uint8_t* nanmask);
 int iq_launch_to_f32(iq_ctx* ctx, const double* src, float* dst, int64_t n);
+
+// relaxation sizes of src/relaxation.jl:11-36 for a given npatterns (iq_sim.cu)
+void iq_relax_sizes(int64_t npat, double tol, int64_t& dbnorm, int64_t& dbzero, int& nnorm,
+                    int64_t* seqnorm, int& nzero, int64_t* seqzero);

@@ -11,37 +11,40 @@ namespace {
 
 struct PasteArgs {
   int nreal;
+  StepTask t0;
+  const StepTask* tasks;
   float* sim; int64_t sx, sy, srs;
   float* cut;
-  int64_t tile_start;
   int64_t tx, ty, tz;
   const float* ti; int64_t tix, tiy; int64_t dx, dy;
   const int64_t* rind;
-  int nslab;
-  CutSlab slab[6];
   const uint8_t* cutbuf; int64_t slabmax;
 };
 
+// CTA row y: realization y % nreal of task y / nreal.
 __global__ void paste_kernel(const PasteArgs a) {
-  const int r = blockIdx.y;
+  const int y = blockIdx.y;
+  const int r = y % a.nreal;
+  const StepTask& tk = a.tasks ? a.tasks[y / a.nreal] : a.t0;
   const int64_t T = a.tx * a.ty * a.tz;
-  const int64_t ri = a.rind[r];
+  const int64_t ri = a.rind[y];
   if (ri < 0) return;
   const int64_t rx = ri % a.dx, rr = ri / a.dx, ry = rr % a.dy, rz = rr / a.dy;
   const int64_t bstart = rx + a.tix * (ry + a.tiy * rz);
+  const int nslab = tk.nslab;
   for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < T;
        k += (int64_t)gridDim.x * blockDim.x) {
     const int64_t kx = k % a.tx, kr = k / a.tx, ky = kr % a.ty, kz = kr / a.ty;
     bool keep = false;
-    for (int s = 0; s < a.nslab; ++s) {
-      const CutSlab& sl = a.slab[s];
+    for (int s = 0; s < nslab; ++s) {
+      const CutSlab& sl = tk.slab[s];
       const int64_t lx = kx - sl.off[0], ly = ky - sl.off[1], lz = kz - sl.off[2];
       if (lx < 0 || ly < 0 || lz < 0 || lx >= sl.ext[0] || ly >= sl.ext[1] || lz >= sl.ext[2])
         continue;
       const int64_t loc = lx + sl.ext[0] * (ly + sl.ext[1] * lz);
-      keep |= a.cutbuf[((int64_t)r * a.nslab + s) * a.slabmax + loc] != 0;
+      keep |= a.cutbuf[((int64_t)y * 6 + s) * a.slabmax + loc] != 0;
     }
-    const int64_t si = (int64_t)r * a.srs + a.tile_start + kx + a.sx * (ky + a.sy * kz);
+    const int64_t si = (int64_t)r * a.srs + tk.start + kx + a.sx * (ky + a.sy * kz);
     if (!keep) a.sim[si] = a.ti[bstart + kx + a.tix * (ky + a.tiy * kz)];
     if (a.cut) a.cut[si] = keep ? 1.f : 0.f;
   }
@@ -126,22 +129,22 @@ inline unsigned blocks_for(int64_t n, int threads = 256, int64_t cap = 8192) {
 }  // namespace
 
 int iq_launch_paste(iq_ctx* ctx, const PasteLaunch& L) {
+  if (L.ntask <= 0 || L.nreal <= 0) return IQ_OK;
   PasteArgs a;
   a.nreal = L.nreal;
+  a.t0 = L.t0;
+  a.tasks = L.tasks;
   a.sim = L.sim; a.sx = L.sim_dims.x; a.sy = L.sim_dims.y; a.srs = L.sim_rstride;
   a.cut = L.cut;
-  a.tile_start = L.tile_start;
   a.tx = L.tile.x; a.ty = L.tile.y; a.tz = L.tile.z;
   a.ti = L.ti; a.tix = L.ti_dims.x; a.tiy = L.ti_dims.y;
   a.dx = L.dist_dims.x; a.dy = L.dist_dims.y;
   a.rind = L.rind;
-  a.nslab = L.nslab;
-  for (int i = 0; i < 6; ++i) a.slab[i] = L.slab[i];
   a.cutbuf = L.cutbuf; a.slabmax = L.slabmax;
-  dim3 grid(blocks_for(L.tile.vol(), 256, 64), (unsigned)L.nreal);
+  dim3 grid(blocks_for(L.tile.vol(), 256, 64), (unsigned)(L.ntask * L.nreal));
   iq_timer_start(ctx, "paste");
   paste_kernel<<<grid, 256, 0, ctx->stream>>>(a);
-  iq_timer_stop(ctx, "paste", 4.0 * (double)L.tile.vol() * L.nreal);
+  iq_timer_stop(ctx, "paste", 4.0 * (double)L.tile.vol() * L.nreal * L.ntask);
   iq_count(ctx);
   IQ_CUDA_OK(cudaGetLastError());
   return IQ_OK;

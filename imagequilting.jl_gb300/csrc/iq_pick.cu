@@ -33,14 +33,10 @@ struct PickArgs {
   int64_t P, npat;
   double tol;
   uint64_t seed;
-  int64_t tile, real0;
-  const float* D0; int64_t D0_rs;
-  const unsigned* mm0; int64_t mm0_rs;
-  int naux;
-  const float* aux[IQ_MAX_AUX];
-  int64_t aux_rs[IQ_MAX_AUX];
-  const unsigned* aux_mm[IQ_MAX_AUX];
-  int64_t aux_mm_rs[IQ_MAX_AUX];
+  int64_t real0;
+  int nreal;
+  PickTask t0;
+  const PickTask* tasks;
   int64_t dbsize_norm, dbsize_zero;
   int nseq_norm, nseq_zero;
   int64_t seq_norm[IQ_MAX_SEQ], seq_zero[IQ_MAX_SEQ];
@@ -423,13 +419,14 @@ struct ThrPred {
 template <int NAUX>
 struct RelaxPred {
   const float* D; Key kD;
+  int naux;  // <= NAUX
   const float* aux[NAUX > 0 ? NAUX : 1];
   Key ka[NAUX > 0 ? NAUX : 1];
   __device__ bool operator()(int64_t p) const {
     if (!key_le(fbits(D[p]), (uint32_t)p, kD)) return false;
 #pragma unroll
     for (int a = 0; a < NAUX; ++a)
-      if (!key_le(fbits(aux[a][p]), (uint32_t)p, ka[a])) return false;
+      if (a < naux && !key_le(fbits(aux[a][p]), (uint32_t)p, ka[a])) return false;
     return true;
   }
 };
@@ -570,41 +567,46 @@ __device__ unsigned long long dense_ranks(Smem& s, unsigned long long* sbuf,
   return block_sum_u64(s, acc);
 }
 
+// One CTA per (task, realization): CTA b picks for realization b % nreal of task b / nreal.
+// NAUX is the largest number of auxiliary sources of the launch's tasks.
 template <int NAUX>
 __global__ void __launch_bounds__(PT) pick_kernel(const PickArgs a) {
   __shared__ Smem s;
   extern __shared__ __align__(16) unsigned char dyn[];
   uint32_t* hist = reinterpret_cast<uint32_t*>(dyn);
   unsigned long long* sbuf = reinterpret_cast<unsigned long long*>(dyn + 2 * NBIN * 4);
-  const int r = blockIdx.x;
+  const int b = blockIdx.x;
+  const int r = b % a.nreal;
+  const PickTask& tk = a.tasks ? a.tasks[b / a.nreal] : a.t0;
   const int64_t P = a.P;
-  const float* D = a.D0 + r * a.D0_rs;
-  const unsigned* mm = a.mm0 + r * a.mm0_rs;
-  int32_t* cand = a.cand + r * P;
-  uint32_t* k0 = a.k0 + r * P;
-  uint32_t* v0 = a.v0 + r * P;
-  uint32_t* k1 = a.k1 + r * P;
-  uint32_t* v1 = a.v1 + r * P;
-  double* w = a.w + r * P;
-  double* prod = a.prod + r * P;
+  const float* D = tk.D0 + r * tk.D0_rs;
+  const unsigned* mm = tk.mm0 + r * tk.mm0_rs;
+  const int naux = tk.naux < NAUX ? tk.naux : NAUX;
+  int32_t* cand = a.cand + b * P;
+  uint32_t* k0 = a.k0 + b * P;
+  uint32_t* v0 = a.v0 + b * P;
+  uint32_t* k1 = a.k1 + b * P;
+  uint32_t* v1 = a.v1 + b * P;
+  double* w = a.w + b * P;
+  double* prod = a.prod + b * P;
   uint32_t* rankbuf = reinterpret_cast<uint32_t*>(w);  // ranks live in w until weights are made
   const float* aux[NAUX > 0 ? NAUX : 1];
   const unsigned* amm[NAUX > 0 ? NAUX : 1];
 #pragma unroll
   for (int j = 0; j < NAUX; ++j) {
-    aux[j] = a.aux[j] + r * a.aux_rs[j];
-    amm[j] = a.aux_mm[j] + r * a.aux_mm_rs[j];
+    aux[j] = j < naux ? tk.aux[j] + r * tk.aux_rs[j] : nullptr;
+    amm[j] = j < naux ? tk.aux_mm[j] + r * tk.aux_mm_rs[j] : nullptr;
   }
 
   int64_t n;
-  if (NAUX == 0) {
+  if (naux == 0) {
     const float mn = __uint_as_float(mm[0]);
     const double thr = __dmul_rn(__dadd_rn(1.0, a.tol), (double)mn);
     ThrPred pr{D, thr};
     n = compact(s, pr, P, cand);
   } else {
     if (a.npat <= 0) {
-      if (threadIdx.x == 0) { iq_dev_fail(a.status, IQ_ERR_NOPATTERN); a.rind[r] = -1; }
+      if (threadIdx.x == 0) { iq_dev_fail(a.status, IQ_ERR_NOPATTERN); a.rind[b] = -1; }
       return;
     }
     const bool allzero = mm[1] == 0u;
@@ -612,8 +614,9 @@ __global__ void __launch_bounds__(PT) pick_kernel(const PickArgs a) {
     const int nseq = allzero ? a.nseq_zero : a.nseq_norm;
     RelaxPred<NAUX> pr;
     pr.D = D;
+    pr.naux = naux;
 #pragma unroll
-    for (int j = 0; j < NAUX; ++j) pr.aux[j] = aux[j];
+    for (int j = 0; j < NAUX; ++j) { pr.aux[j] = aux[j]; pr.ka[j] = Key{0xFFFFFFFFu, 0xFFFFFFFFu}; }
     n = 0;
     int q = 0;
     for (; q < nseq && n == 0; ++q) {
@@ -624,7 +627,7 @@ __global__ void __launch_bounds__(PT) pick_kernel(const PickArgs a) {
       int j0 = 0;
       if (q == 0) {
         req[0] = SelReq{D, mm[0], mm[1], dbsize};
-        if (NAUX > 0 && sz > 0 && sz < P) {
+        if (NAUX > 0 && naux > 0 && sz > 0 && sz < P) {
           req[1] = SelReq{aux[0], amm[0][0], amm[0][1], sz};
           hist_select<2>(s, hist, sbuf, req, P, res);
           pr.ka[0] = res[1];
@@ -636,7 +639,7 @@ __global__ void __launch_bounds__(PT) pick_kernel(const PickArgs a) {
       }
 #pragma unroll
       for (int j = 0; j < NAUX; ++j) {
-        if (j < j0) continue;
+        if (j < j0 || j >= naux) continue;
         if (sz >= P) { pr.ka[j] = Key{0xFFFFFFFFu, 0xFFFFFFFFu}; continue; }
         if (sz <= 0) { pr.ka[j] = Key{0u, 0u}; continue; }
         req[0] = SelReq{aux[j], amm[j][0], amm[j][1], sz};
@@ -649,10 +652,10 @@ __global__ void __launch_bounds__(PT) pick_kernel(const PickArgs a) {
     if (a.stats && threadIdx.x == 0) atomicAdd(a.stats + ST_PICK_ITERS, (unsigned long long)q);
   }
   if (n <= 0) {
-    if (threadIdx.x == 0) { iq_dev_fail(a.status, IQ_ERR_NOPATTERN); a.rind[r] = -1; }
+    if (threadIdx.x == 0) { iq_dev_fail(a.status, IQ_ERR_NOPATTERN); a.rind[b] = -1; }
     return;
   }
-  if (a.ncand && threadIdx.x == 0) a.ncand[r] = n;
+  if (a.ncand && threadIdx.x == 0) a.ncand[b] = n;
   if (a.stats && threadIdx.x == 0) {
     atomicAdd(a.stats + ST_PICK_CAND, (unsigned long long)n);
     atomicAdd(a.stats + ST_PICK_CTAS, 1ull);
@@ -660,7 +663,7 @@ __global__ void __launch_bounds__(PT) pick_kernel(const PickArgs a) {
 
   // ---- tau model weights ----
   if (n == 1) {
-    if (threadIdx.x == 0) { w[0] = 1.0; a.rind[r] = cand[0]; }
+    if (threadIdx.x == 0) { w[0] = 1.0; a.rind[b] = cand[0]; }
     return;
   }
   const double dn = (double)n;
@@ -668,7 +671,7 @@ __global__ void __launch_bounds__(PT) pick_kernel(const PickArgs a) {
   const double x0 = __ddiv_rn(__dsub_rn(1.0, inv_n), inv_n);
   for (int64_t i = threadIdx.x; i < n; i += PT) prod[i] = 1.0;
 #pragma unroll 1
-  for (int j = 0; j <= NAUX; ++j) {
+  for (int j = 0; j <= naux; ++j) {
     const float* src = j == 0 ? D : aux[j > 0 ? j - 1 : 0];
     __syncthreads();
     const unsigned long long S = dense_ranks(s, sbuf, src, cand, n, k0, v0, k1, v1, rankbuf);
@@ -697,7 +700,7 @@ __global__ void __launch_bounds__(PT) pick_kernel(const PickArgs a) {
   if (threadIdx.x == 0) {
     double run = 0.0;
     for (int64_t c = 0; c < nch; ++c) { run = __dadd_rn(run, csum[c]); csum[c] = run; }
-    const double u = iq_draw_uniform(a.seed, a.tile, a.real0 + r);
+    const double u = iq_draw_uniform(a.seed, tk.tile, a.real0 + r);
     const double t = __dmul_rn(u, run);
     int64_t c = 0;
     while (c < nch - 1 && csum[c] < t) ++c;
@@ -709,54 +712,54 @@ __global__ void __launch_bounds__(PT) pick_kernel(const PickArgs a) {
       part = __dadd_rn(part, w[i]);
       if (__dadd_rn(base, part) >= t) { pick = i; break; }
     }
-    a.rind[r] = cand[pick];
+    a.rind[b] = cand[pick];
   }
 }
 
 template <int NAUX>
-cudaError_t launch_pick_t(const PickArgs& a, int nreal, cudaStream_t st) {
+cudaError_t launch_pick_t(const PickArgs& a, int nblocks, cudaStream_t st) {
   static bool attr = false;
   if (!attr) {
     cudaFuncSetAttribute(pick_kernel<NAUX>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)DYN_BYTES);
     attr = true;
   }
-  pick_kernel<NAUX><<<nreal, PT, DYN_BYTES, st>>>(a);
+  pick_kernel<NAUX><<<nblocks, PT, DYN_BYTES, st>>>(a);
   return cudaGetLastError();
 }
 
 }  // namespace
 
 int iq_launch_pick(iq_ctx* ctx, const PickLaunch& L) {
-  if (L.naux > IQ_MAX_AUX) return iq_set_error(IQ_ERR_LIMIT, "too many auxiliary sources");
+  if (L.naux_max > IQ_MAX_AUX || L.t0.naux > IQ_MAX_AUX)
+    return iq_set_error(IQ_ERR_LIMIT, "too many auxiliary sources");
+  if (L.ntask <= 0 || L.nreal <= 0) return IQ_OK;
   PickArgs a;
-  a.P = L.P; a.npat = L.npat; a.tol = L.tol; a.seed = L.seed; a.tile = L.tile;
-  a.real0 = L.real0;
-  a.D0 = L.D0; a.D0_rs = L.D0_rstride; a.mm0 = L.mm0; a.mm0_rs = L.mm0_rstride;
-  a.naux = L.naux;
-  for (int j = 0; j < IQ_MAX_AUX; ++j) {
-    a.aux[j] = L.aux[j]; a.aux_rs[j] = L.aux_rstride[j];
-    a.aux_mm[j] = L.aux_mm[j]; a.aux_mm_rs[j] = L.aux_mm_rstride[j];
-  }
+  a.P = L.P; a.npat = L.npat; a.tol = L.tol; a.seed = L.seed; a.real0 = L.real0;
+  a.nreal = L.nreal;
+  a.t0 = L.t0;
+  a.tasks = L.tasks;
   a.dbsize_norm = L.dbsize_norm; a.dbsize_zero = L.dbsize_zero;
   a.nseq_norm = L.nseq_norm; a.nseq_zero = L.nseq_zero;
   for (int q = 0; q < IQ_MAX_SEQ; ++q) { a.seq_norm[q] = L.seq_norm[q]; a.seq_zero[q] = L.seq_zero[q]; }
   a.cand = L.cand; a.k0 = L.k0; a.v0 = L.v0; a.k1 = L.k1; a.v1 = L.v1;
   a.w = L.w; a.prod = L.prod; a.rind = L.rind; a.ncand = L.ncand; a.status = L.status;
   a.stats = L.stats;
+  const int naux = L.tasks ? L.naux_max : L.t0.naux;
+  const int nblocks = L.ntask * L.nreal;
   iq_timer_start(ctx, "pick");
   cudaError_t e;
-  switch (L.naux) {
-    case 0: e = launch_pick_t<0>(a, L.nreal, ctx->stream); break;
-    case 1: e = launch_pick_t<1>(a, L.nreal, ctx->stream); break;
-    case 2: e = launch_pick_t<2>(a, L.nreal, ctx->stream); break;
-    case 3: e = launch_pick_t<3>(a, L.nreal, ctx->stream); break;
-    case 4: e = launch_pick_t<4>(a, L.nreal, ctx->stream); break;
-    case 5: e = launch_pick_t<5>(a, L.nreal, ctx->stream); break;
-    case 6: e = launch_pick_t<6>(a, L.nreal, ctx->stream); break;
-    default: e = launch_pick_t<7>(a, L.nreal, ctx->stream); break;
+  switch (naux) {
+    case 0: e = launch_pick_t<0>(a, nblocks, ctx->stream); break;
+    case 1: e = launch_pick_t<1>(a, nblocks, ctx->stream); break;
+    case 2: e = launch_pick_t<2>(a, nblocks, ctx->stream); break;
+    case 3: e = launch_pick_t<3>(a, nblocks, ctx->stream); break;
+    case 4: e = launch_pick_t<4>(a, nblocks, ctx->stream); break;
+    case 5: e = launch_pick_t<5>(a, nblocks, ctx->stream); break;
+    case 6: e = launch_pick_t<6>(a, nblocks, ctx->stream); break;
+    default: e = launch_pick_t<7>(a, nblocks, ctx->stream); break;
   }
-  iq_timer_stop(ctx, "pick", 4.0 * (double)L.P * (double)(1 + L.naux) * (double)L.nreal);
+  iq_timer_stop(ctx, "pick", 4.0 * (double)L.P * (double)(1 + naux) * (double)nblocks);
   iq_count(ctx);
   if (e != cudaSuccess) return iq_set_error(IQ_ERR_CUDA, "pick launch: %s", cudaGetErrorString(e));
   return IQ_OK;

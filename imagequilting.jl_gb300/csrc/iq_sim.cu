@@ -335,8 +335,11 @@ extern "C" int iq_simulate(iq_ctx* ctx, const iq_sim_params* p, const iq_hard_da
     for (uint8_t v : hd) npat -= v;
   }
 
-  // ---- step plan: neighbour flags per step, distinct masks ----
-  struct Step { int64_t tile; int64_t start[3]; int cfg; bool hardtile; int nslab; CutSlab slab[6]; };
+  // ---- step plan: neighbour flags per step, distinct masks (src/iqsim.jl:172-205) ----
+  struct Step {
+    int64_t tile; int64_t start[3]; int64_t startlin; int cfg; bool hardtile;
+    int nslab; CutSlab slab[6]; int level; int64_t order;
+  };
   std::vector<Step> steps;
   std::vector<MaskCfg> cfgs;
   std::vector<uint8_t> pasted(g.ntot, 0);
@@ -344,6 +347,7 @@ extern "C" int iq_simulate(iq_ctx* ctx, const iq_sim_params* p, const iq_hard_da
     if (skipped[ind]) continue;
     Step s;
     s.tile = ind;
+    s.order = (int64_t)steps.size();
     int64_t ti3[3] = {ind % g.ntiles[0], (ind / g.ntiles[0]) % g.ntiles[1], ind / (g.ntiles[0] * g.ntiles[1])};
     MaskCfg m;
     s.nslab = 0;
@@ -360,6 +364,7 @@ extern "C" int iq_simulate(iq_ctx* ctx, const iq_sim_params* p, const iq_hard_da
       m.lo[d] = m.prev[d] ? g.ovl[d] : 0;
       m.hi[d] = m.next[d] ? g.spacing[d] : g.tile[d];
     }
+    s.startlin = s.start[0] + padD.x * (s.start[1] + padD.y * s.start[2]);
     for (int d = 0; d < 3; ++d) {
       for (int side = 0; side < 2; ++side) {
         if (!(side ? m.next[d] : m.prev[d])) continue;
@@ -371,7 +376,6 @@ extern "C" int iq_simulate(iq_ctx* ctx, const iq_sim_params* p, const iq_hard_da
         c.ext[d] = side ? g.tile[d] - g.spacing[d] : g.ovl[d];
       }
     }
-    // inner box volume (excluded from the mask)
     int64_t inner = 1;
     for (int d = 0; d < 3; ++d) inner *= std::max<int64_t>(m.hi[d] - m.lo[d], 0);
     m.K = (int)(T - inner);
@@ -387,6 +391,32 @@ extern "C" int iq_simulate(iq_ctx* ctx, const iq_sim_params* p, const iq_hard_da
     s.hardtile = has_data[ind] != 0;
     steps.push_back(s);
     pasted[ind] = 1;
+  }
+  // Dependency levels: a step must follow every earlier step of the path whose tile region
+  // overlaps its own (it reads what they paste and pastes over them). Steps of one level never
+  // overlap, so each level runs as one batch with results identical to the path order.
+  {
+    int64_t rng3[3];
+    for (int d = 0; d < 3; ++d)
+      rng3[d] = g.spacing[d] > 0 ? (g.tile[d] + g.spacing[d] - 1) / g.spacing[d] - 1 : 0;
+    std::vector<int> tile_level(g.ntot, -1);
+    for (Step& s : steps) {
+      const int64_t t3[3] = {s.tile % g.ntiles[0], (s.tile / g.ntiles[0]) % g.ntiles[1],
+                             s.tile / (g.ntiles[0] * g.ntiles[1])};
+      int lv = 0;
+      for (int64_t oz = -rng3[2]; oz <= rng3[2]; ++oz)
+        for (int64_t oy = -rng3[1]; oy <= rng3[1]; ++oy)
+          for (int64_t ox = -rng3[0]; ox <= rng3[0]; ++ox) {
+            const int64_t x = t3[0] + ox, y = t3[1] + oy, z = t3[2] + oz;
+            if (x < 0 || y < 0 || z < 0 || x >= g.ntiles[0] || y >= g.ntiles[1] || z >= g.ntiles[2]) continue;
+            const int l = tile_level[x + g.ntiles[0] * (y + g.ntiles[1] * z)];
+            if (l >= 0) lv = std::max(lv, l + 1);
+          }
+      s.level = lv;
+      tile_level[s.tile] = lv;
+    }
+    std::stable_sort(steps.begin(), steps.end(),
+                     [](const Step& a, const Step& b) { return a.level < b.level; });
   }
   // offset lists: one block of T entries per mask configuration, plus the full tile
   const int ncfg = (int)cfgs.size();
@@ -417,50 +447,67 @@ extern "C" int iq_simulate(iq_ctx* ctx, const iq_sim_params* p, const iq_hard_da
       hkv[hoff[t] + i] = tile_hard[t][i].second;
     }
 
-  // ---- device buffers ----
+  // ---- chunks: consecutive steps of one level, as many as memory allows ----
   const int rt = iq_register_tile(R);
   const int rpad = ((R + rt - 1) / rt) * rt;
-  const bool debug = p->debug != 0 && (cuts || voxs);
-  float* d_sim = (float*)iq_scratch(ctx, S_SIM, sizeof(float) * padvol * R);
-  float* d_cut = debug ? (float*)iq_scratch(ctx, S_CUT, sizeof(float) * padvol * R) : nullptr;
-  float* d_D = (float*)iq_scratch(ctx, S_D, sizeof(float) * P * R);
-  float* d_Dh = (float*)iq_scratch(ctx, S_DHARD, sizeof(float) * P);
-  // template values: the overlap batch (T x rpad), then the hard template (T x 1)
-  float* d_tv = (float*)iq_scratch(ctx, S_TV, sizeof(float) * T * (std::max(rpad, 16) + 1));
-  double* d_b2 = (double*)iq_scratch(ctx, S_B2, sizeof(double) * (std::max(rpad, 16) + 1));
-  uint32_t* d_kl = (uint32_t*)iq_scratch(ctx, S_KLIST, sizeof(uint32_t) * klist.size());
-  unsigned* d_mm = (unsigned*)iq_scratch(ctx, S_MINMAX, sizeof(unsigned) * 2 * (R + 1));
-  uint32_t* d_hk = (uint32_t*)iq_scratch(ctx, S_HARDLIST, sizeof(uint32_t) * hk.size());
-  float* d_hkv = (float*)iq_scratch(ctx, S_HARDPTS, sizeof(float) * hkv.size());
-  int32_t* d_cand = (int32_t*)iq_scratch(ctx, S_PICK_CAND, sizeof(int32_t) * P * R);
-  uint32_t* d_k0 = (uint32_t*)iq_scratch(ctx, S_PICK_K0, sizeof(uint32_t) * P * R);
-  uint32_t* d_v0 = (uint32_t*)iq_scratch(ctx, S_PICK_V0, sizeof(uint32_t) * P * R);
-  uint32_t* d_k1 = (uint32_t*)iq_scratch(ctx, S_PICK_K1, sizeof(uint32_t) * P * R);
-  uint32_t* d_v1 = (uint32_t*)iq_scratch(ctx, S_PICK_V1, sizeof(uint32_t) * P * R);
-  double* d_w = (double*)iq_scratch(ctx, S_PICK_W, sizeof(double) * P * R);
-  double* d_prod = (double*)iq_scratch(ctx, S_PICK_PROD, sizeof(double) * P * R);
-  int64_t* d_rind = (int64_t*)iq_scratch(ctx, S_RIND, sizeof(int64_t) * R);
-  int64_t* d_ncand = (int64_t*)iq_scratch(ctx, S_NCAND, sizeof(int64_t) * R);
   int64_t slabmax = 1;
   for (int d = 0; d < N; ++d) slabmax = std::max<int64_t>(slabmax, T / g.tile[d] * g.ovl[d]);
-  uint8_t* d_cutbuf = (uint8_t*)iq_scratch(ctx, S_CUTBUF, (size_t)R * 6 * slabmax);
-  if (!d_sim || (debug && !d_cut) || !d_D || !d_Dh || !d_tv || !d_b2 || !d_kl || !d_mm || !d_hk ||
-      !d_hkv || !d_cand || !d_k0 || !d_v0 || !d_k1 || !d_v1 || !d_w || !d_prod || !d_rind ||
-      !d_ncand || !d_cutbuf)
-    return IQ_ERR_ALLOC;
-  // global scratch for cut slabs that do not fit in shared memory
-  void* d_cutscr = nullptr;
   int64_t cutscr_per = 0;
   {
     int dev = 0, lim = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&lim, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-    if ((int64_t)iq_cut_scratch_bytes(slabmax) > lim) {
-      cutscr_per = (int64_t)iq_cut_scratch_bytes(slabmax);
-      d_cutscr = iq_scratch(ctx, S_CUTSCR, (size_t)cutscr_per * 6 * R);
-      if (!d_cutscr) return IQ_ERR_ALLOC;
-    }
+    if ((int64_t)iq_cut_scratch_bytes(slabmax) > lim) cutscr_per = (int64_t)iq_cut_scratch_bytes(slabmax);
   }
+  const int64_t per_step = (int64_t)R * P * (4 + 4 + 16 + 16) + P * 4 + T * (rpad + 1) * 4 +
+                           (int64_t)R * 6 * (slabmax + cutscr_per) + 4096;
+  size_t freeb = 0, totalb = 0;
+  cudaMemGetInfo(&freeb, &totalb);
+  int64_t chunk_max = std::max<int64_t>(1, std::min<int64_t>(ctx->level_chunk,
+                                                              (int64_t)(freeb / 2) / per_step));
+  std::vector<int64_t> cbeg;  // chunk boundaries into `steps`
+  for (size_t i = 0; i < steps.size();) {
+    size_t j = i + 1;
+    while (j < steps.size() && steps[j].level == steps[i].level && (int64_t)(j - i) < chunk_max) ++j;
+    cbeg.push_back((int64_t)i);
+    i = j;
+  }
+  cbeg.push_back((int64_t)steps.size());
+  const int64_t nchunk = (int64_t)cbeg.size() - 1;
+  int64_t cmax = 1;
+  for (int64_t c = 0; c < nchunk; ++c) cmax = std::max(cmax, cbeg[c + 1] - cbeg[c]);
+
+  // ---- device buffers ----
+  const bool debug = p->debug != 0 && (cuts || voxs);
+  float* d_sim = (float*)iq_scratch(ctx, S_SIM, sizeof(float) * padvol * R);
+  float* d_cut = debug ? (float*)iq_scratch(ctx, S_CUT, sizeof(float) * padvol * R) : nullptr;
+  float* d_D = (float*)iq_scratch(ctx, S_D, sizeof(float) * P * R * cmax);
+  float* d_Dh = (float*)iq_scratch(ctx, S_DHARD, sizeof(float) * P * cmax);
+  float* d_tv = (float*)iq_scratch(ctx, S_TV, sizeof(float) * T * (std::max(rpad, 16) * cmax + cmax));
+  double* d_b2 = (double*)iq_scratch(ctx, S_B2, sizeof(double) * (std::max(rpad, 16) * cmax + cmax));
+  uint32_t* d_kl = (uint32_t*)iq_scratch(ctx, S_KLIST, sizeof(uint32_t) * klist.size());
+  unsigned* d_mm = (unsigned*)iq_scratch(ctx, S_MINMAX, sizeof(unsigned) * 2 * (R + 1) * cmax);
+  uint32_t* d_hk = (uint32_t*)iq_scratch(ctx, S_HARDLIST, sizeof(uint32_t) * hk.size());
+  float* d_hkv = (float*)iq_scratch(ctx, S_HARDPTS, sizeof(float) * hkv.size());
+  const size_t pk = (size_t)P * R * cmax;
+  int32_t* d_cand = (int32_t*)iq_scratch(ctx, S_PICK_CAND, sizeof(int32_t) * pk);
+  uint32_t* d_k0 = (uint32_t*)iq_scratch(ctx, S_PICK_K0, sizeof(uint32_t) * pk);
+  uint32_t* d_v0 = (uint32_t*)iq_scratch(ctx, S_PICK_V0, sizeof(uint32_t) * pk);
+  uint32_t* d_k1 = (uint32_t*)iq_scratch(ctx, S_PICK_K1, sizeof(uint32_t) * pk);
+  uint32_t* d_v1 = (uint32_t*)iq_scratch(ctx, S_PICK_V1, sizeof(uint32_t) * pk);
+  double* d_w = (double*)iq_scratch(ctx, S_PICK_W, sizeof(double) * pk);
+  double* d_prod = (double*)iq_scratch(ctx, S_PICK_PROD, sizeof(double) * pk);
+  int64_t* d_rind = (int64_t*)iq_scratch(ctx, S_RIND, sizeof(int64_t) * R * cmax);
+  int64_t* d_ncand = (int64_t*)iq_scratch(ctx, S_NCAND, sizeof(int64_t) * R * cmax);
+  uint8_t* d_cutbuf = (uint8_t*)iq_scratch(ctx, S_CUTBUF, (size_t)R * cmax * 6 * slabmax);
+  void* d_cutscr = cutscr_per ? iq_scratch(ctx, S_CUTSCR, (size_t)cutscr_per * 6 * R * cmax) : nullptr;
+  if (!d_sim || (debug && !d_cut) || !d_D || !d_Dh || !d_tv || !d_b2 || !d_kl || !d_mm || !d_hk ||
+      !d_hkv || !d_cand || !d_k0 || !d_v0 || !d_k1 || !d_v1 || !d_w || !d_prod || !d_rind ||
+      !d_ncand || !d_cutbuf || (cutscr_per && !d_cutscr))
+    return IQ_ERR_ALLOC;
+  float* d_tvh = d_tv + (size_t)T * std::max(rpad, 16) * cmax;  // hard templates (T x 1 each)
+  double* d_b2h = d_b2 + (size_t)std::max(rpad, 16) * cmax;
+  unsigned* d_mmh = d_mm + 2 * R * cmax;
   IQ_CUDA_OK(cudaMemsetAsync(d_sim, 0, sizeof(float) * padvol * R, st));
   if (debug) IQ_CUDA_OK(cudaMemsetAsync(d_cut, 0, sizeof(float) * padvol * R, st));
   IQ_CUDA_OK(cudaMemcpyAsync(d_kl, klist.data(), sizeof(uint32_t) * klist.size(), cudaMemcpyHostToDevice, st));
@@ -479,7 +526,6 @@ extern "C" int iq_simulate(iq_ctx* ctx, const iq_sim_params* p, const iq_hard_da
     for (int64_t t = 0; t < g.ntot; ++t)
       if (!skipped[t]) slot_of[t] = nslot++;
     const int64_t tivol = ctx->ti.vol();
-    // one arena for all soft arrays
     int64_t amax[3] = {1, 1, 1};
     for (int s = 0; s < nsoft; ++s)
       for (int d = 0; d < N; ++d) amax[d] = std::max(amax[d], std::max(soft[s].auxsize[d], g.pad[d]));
@@ -490,15 +536,17 @@ extern "C" int iq_simulate(iq_ctx* ctx, const iq_sim_params* p, const iq_hard_da
     double* a_ii = (double*)iq_scratch(ctx, S_AUXII, sizeof(double) * iivol * nsoft);
     float* a_raw = (float*)iq_scratch(ctx, S_TMP1, sizeof(float) * auxvol);
     d_soft = (float*)iq_scratch(ctx, S_SOFT, sizeof(float) * P * nslot * nsoft);
-    d_softmm = (unsigned*)iq_scratch(ctx, S_SOFTB2, sizeof(unsigned) * 2 * nslot * nsoft);
+    d_softmm = (unsigned*)iq_scratch(ctx, S_SOFTMM, sizeof(unsigned) * 2 * nslot * nsoft);
     int64_t* d_starts = (int64_t*)iq_scratch(ctx, S_STARTS, sizeof(int64_t) * (nslot + 16));
     if (!a_aux || !a_ti || !a_ii || !a_raw || !d_soft || !d_softmm || !d_starts) return IQ_ERR_ALLOC;
+    std::vector<int64_t> tl;
+    for (int64_t t = 0; t < g.ntot; ++t)
+      if (!skipped[t]) tl.push_back(t);
     for (int s = 0; s < nsoft; ++s) {
-      Dim3 asz{1, 1, 1};
       int64_t ae[3] = {1, 1, 1};
       for (int d = 0; d < N; ++d) ae[d] = soft[s].auxsize[d];
-      asz = Dim3{ae[0], ae[1], ae[2]};
-      Dim3 psz{std::max(ae[0], g.pad[0]), std::max(ae[1], g.pad[1]), std::max(ae[2], g.pad[2])};
+      const Dim3 asz{ae[0], ae[1], ae[2]};
+      const Dim3 psz{std::max(ae[0], g.pad[0]), std::max(ae[1], g.pad[1]), std::max(ae[2], g.pad[2])};
       d_aux[s] = a_aux + auxvol * s;
       d_auxti[s] = a_ti + tivol * s;
       d_auxii[s] = a_ii + iivol * s;
@@ -507,10 +555,6 @@ extern "C" int iq_simulate(iq_ctx* ctx, const iq_sim_params* p, const iq_hard_da
       IQ_CUDA_OK(cudaMemcpyAsync(d_auxti[s], soft[s].auxti, sizeof(float) * tivol, cudaMemcpyDefault, st));
       RET_IF(iq_launch_prepare(ctx, d_auxti[s], tivol, nullptr));
       RET_IF(iq_build_integrals(ctx, d_auxti[s], ctx->ti, d_auxii[s], nullptr, nullptr));
-      // per-tile soft distance maps, 16 tiles per launch
-      std::vector<int64_t> tl;
-      for (int64_t t = 0; t < g.ntot; ++t)
-        if (!skipped[t]) tl.push_back(t);
       std::vector<int64_t> starts(tl.size());
       for (size_t i = 0; i < tl.size(); ++i) {
         const int64_t t = tl[i];
@@ -521,86 +565,136 @@ extern "C" int iq_simulate(iq_ctx* ctx, const iq_sim_params* p, const iq_hard_da
       }
       IQ_CUDA_OK(cudaMemcpyAsync(d_starts, starts.data(), sizeof(int64_t) * starts.size(),
                                  cudaMemcpyHostToDevice, st));
+      // per-tile soft distance maps, 16 tiles per launch
       for (size_t b0 = 0; b0 < tl.size(); b0 += 16) {
         const int nb = (int)std::min<size_t>(16, tl.size() - b0);
+        const int64_t slot0 = (int64_t)s * nslot + slot_of[tl[b0]];
         GatherLaunch G;
         G.grid = d_aux[s]; G.grid_dims = psz; G.grid_stride = 0; G.starts = d_starts + b0;
-        G.K = (int)T; G.klist = d_kl + (size_t)ncfg * T; G.ntmpl = nb; G.rpad = 16;
-        G.tv = d_tv; G.b2 = d_b2;
-        G.minmax = d_softmm + 2 * ((int64_t)s * nslot + slot_of[tl[b0]]);
+        G.ntmpl = nb; G.rpad = 16;
+        G.t0 = GatherTask{d_kl + (size_t)ncfg * T, (int)T, 0, nullptr, d_tv, d_b2, d_softmm + 2 * slot0};
         RET_IF(iq_launch_gather(ctx, G));
         CorrLaunch C;
-        C.img = d_auxti[s]; C.img_dims = ctx->ti; C.out_dims = distD; C.K = (int)T;
-        C.klist = d_kl + (size_t)ncfg * T; C.tv = d_tv; C.rpad = 16; C.ntmpl = nb; C.b2 = d_b2;
-        C.a2.ii = d_auxii[s];
-        C.a2.tile[0] = g.tile[0]; C.a2.tile[1] = g.tile[1]; C.a2.tile[2] = g.tile[2];
-        C.disabled = d_dis;
-        C.out = d_soft + ((int64_t)s * nslot + slot_of[tl[b0]]) * P;
-        C.out_stride = P;
-        C.minmax = G.minmax;
+        C.img = d_auxti[s]; C.img_dims = ctx->ti; C.out_dims = distD; C.tile = tileD;
+        C.rpad = 16; C.ntmpl = nb; C.out_stride = P; C.disabled = d_dis;
+        C.t0 = CorrTask{d_kl + (size_t)ncfg * T, (int)T, d_tv, d_b2, d_auxii[s], {0, 0, 0}, {0, 0, 0},
+                        d_soft + slot0 * P, d_softmm + 2 * slot0};
         RET_IF(iq_launch_corr(ctx, C));
       }
       IQ_CUDA_OK(cudaStreamSynchronize(st));  // `starts` is a host vector
     }
   }
 
-  // ---- the tile loop (src/iqsim.jl:172-285) ----
+  // ---- task descriptors of every step, uploaded once ----
+  const int64_t nsteps = (int64_t)steps.size();
+  std::vector<GatherTask> gt(nsteps), hgt;
+  std::vector<CorrTask> ct(nsteps), hct;
+  std::vector<PickTask> pt(nsteps);
+  std::vector<StepTask> stk(nsteps);
+  std::vector<int64_t> hbeg(nchunk + 1, 0);  // hard tasks of chunk c: [hbeg[c], hbeg[c+1])
+  std::vector<double> cflops(nchunk, 0.0);
+  std::vector<int> cslab(nchunk, 0), chard(nchunk, 0);
+  for (int64_t c = 0; c < nchunk; ++c) {
+    int hi = 0;
+    for (int64_t k = cbeg[c]; k < cbeg[c + 1]; ++k) {
+      const Step& s = steps[k];
+      const int64_t i = k - cbeg[c];
+      const MaskCfg& m = cfgs[s.cfg];
+      float* tv = d_tv + (size_t)i * T * rpad;
+      double* b2 = d_b2 + (size_t)i * rpad;
+      unsigned* mm = d_mm + (size_t)i * R * 2;
+      float* D = d_D + (size_t)i * R * P;
+      gt[k] = GatherTask{d_kl + (size_t)s.cfg * T, m.K, s.startlin, nullptr, tv, b2, mm};
+      ct[k] = CorrTask{d_kl + (size_t)s.cfg * T, m.K, tv, b2, ctx->d_ti2ii,
+                       {m.lo[0], m.lo[1], m.lo[2]}, {m.hi[0], m.hi[1], m.hi[2]}, D, mm};
+      cflops[c] += 2.0 * (double)P * (double)m.K * (double)R;
+      PickTask& q = pt[k];
+      memset(&q, 0, sizeof(q));
+      q.tile = s.tile;
+      int na = 0;
+      if (s.hardtile) {
+        const int64_t h0 = hoff[s.tile], hn = hoff[s.tile + 1] - hoff[s.tile];
+        float* tvh = d_tvh + (size_t)hi * T;
+        hgt.push_back(GatherTask{d_hk + h0, (int)hn, 0, d_hkv + h0, tvh, d_b2h + hi, d_mmh + 2 * hi});
+        hct.push_back(CorrTask{d_hk + h0, (int)hn, tvh, d_b2h + hi, nullptr, {0, 0, 0}, {0, 0, 0},
+                               d_Dh + (size_t)hi * P, d_mmh + 2 * hi});
+        cflops[c] += 2.0 * (double)P * (double)hn;
+        q.D0 = d_Dh + (size_t)hi * P; q.D0_rs = 0; q.mm0 = d_mmh + 2 * hi; q.mm0_rs = 0;
+        q.aux[na] = D; q.aux_rs[na] = P; q.aux_mm[na] = mm; q.aux_mm_rs[na] = 2;
+        ++na;
+        ++hi;
+        chard[c] = 1;
+      } else {
+        q.D0 = D; q.D0_rs = P; q.mm0 = mm; q.mm0_rs = 2;
+      }
+      for (int sv = 0; sv < nsoft; ++sv) {
+        const int64_t slot = (int64_t)sv * nslot + slot_of[s.tile];
+        q.aux[na] = d_soft + slot * P; q.aux_rs[na] = 0;
+        q.aux_mm[na] = d_softmm + 2 * slot; q.aux_mm_rs[na] = 0;
+        ++na;
+      }
+      q.naux = na;
+      StepTask& sk = stk[k];
+      sk.start = s.startlin;
+      sk.nslab = s.nslab;
+      for (int j = 0; j < 6; ++j) sk.slab[j] = s.slab[j];
+      cslab[c] = std::max(cslab[c], s.nslab);
+    }
+    hbeg[c + 1] = hbeg[c] + hi;
+  }
+  const size_t tbytes = sizeof(GatherTask) * (nsteps + hgt.size()) + sizeof(CorrTask) * (nsteps + hct.size()) +
+                        sizeof(PickTask) * nsteps + sizeof(StepTask) * nsteps + 6 * 256;
+  char* d_tasks = (char*)iq_scratch(ctx, S_TASKS, tbytes);
+  if (!d_tasks) return IQ_ERR_ALLOC;
+  size_t toff = 0;
+  auto put = [&](const void* src, size_t bytes) -> char* {
+    char* dst = d_tasks + toff;
+    if (bytes) cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, st);
+    toff += (bytes + 255) & ~(size_t)255;
+    return dst;
+  };
+  const GatherTask* d_gt = (const GatherTask*)put(gt.data(), sizeof(GatherTask) * nsteps);
+  const CorrTask* d_ct = (const CorrTask*)put(ct.data(), sizeof(CorrTask) * nsteps);
+  const GatherTask* d_hgt = (const GatherTask*)put(hgt.data(), sizeof(GatherTask) * hgt.size());
+  const CorrTask* d_hct = (const CorrTask*)put(hct.data(), sizeof(CorrTask) * hct.size());
+  const PickTask* d_pt = (const PickTask*)put(pt.data(), sizeof(PickTask) * nsteps);
+  const StepTask* d_st = (const StepTask*)put(stk.data(), sizeof(StepTask) * nsteps);
+  IQ_CUDA_OK(cudaGetLastError());
+
+  // ---- the tile loop (src/iqsim.jl:172-285), one dependency level chunk at a time ----
   int64_t dbn = 0, dbz = 0;
   int nsn = 0, nsz = 0;
   int64_t seqn[IQ_MAX_SEQ], seqz[IQ_MAX_SEQ];
   if (npat > 0) iq_relax_sizes(npat, p->tol, dbn, dbz, nsn, seqn, nsz, seqz);
-  unsigned* d_mmh = d_mm + 2 * R;
-  for (const Step& s : steps) {
-    const MaskCfg& m = cfgs[s.cfg];
-    const int64_t tstart = s.start[0] + padD.x * (s.start[1] + padD.y * s.start[2]);
-    // overlap distance of every realization
+  for (int64_t c = 0; c < nchunk; ++c) {
+    const int64_t k0 = cbeg[c];
+    const int m = (int)(cbeg[c + 1] - cbeg[c]);
+    // overlap distance of every realization of every tile of the chunk
     GatherLaunch G;
-    G.grid = d_sim; G.grid_dims = padD; G.grid_stride = padvol; G.start0 = tstart;
-    G.K = m.K; G.klist = d_kl + (size_t)s.cfg * T; G.ntmpl = R; G.rpad = rpad;
-    G.tv = d_tv; G.b2 = d_b2; G.minmax = d_mm;
+    G.grid = d_sim; G.grid_dims = padD; G.grid_stride = padvol; G.ntmpl = R; G.rpad = rpad;
+    G.ntask = m; G.tasks = d_gt + k0;
     RET_IF(iq_launch_gather(ctx, G));
     CorrLaunch C;
-    C.img = ctx->d_ti; C.img_dims = ctx->ti; C.out_dims = distD; C.K = m.K;
-    C.klist = d_kl + (size_t)s.cfg * T; C.tv = d_tv; C.rpad = rpad; C.ntmpl = R; C.b2 = d_b2;
-    C.a2.ii = ctx->d_ti2ii;
-    for (int d = 0; d < 3; ++d) { C.a2.tile[d] = g.tile[d]; C.a2.lo[d] = m.lo[d]; C.a2.hi[d] = m.hi[d]; }
-    C.disabled = d_dis; C.out = d_D; C.out_stride = P; C.minmax = d_mm;
+    C.img = ctx->d_ti; C.img_dims = ctx->ti; C.out_dims = distD; C.tile = tileD;
+    C.rpad = rpad; C.ntmpl = R; C.out_stride = P; C.disabled = d_dis;
+    C.ntask = m; C.tasks = d_ct + k0; C.flops = cflops[c];
     RET_IF(iq_launch_corr(ctx, C));
-    // hard distance of a data tile
-    if (s.hardtile) {
-      const int64_t h0 = hoff[s.tile], hn = hoff[s.tile + 1] - hoff[s.tile];
+    // hard distance of the data tiles of the chunk
+    const int nh_c = (int)(hbeg[c + 1] - hbeg[c]);
+    if (nh_c > 0) {
       GatherLaunch H;
-      H.K = (int)hn; H.klist = d_hk + h0; H.kval = d_hkv + h0; H.ntmpl = 1; H.rpad = 1;
-      H.tv = d_tv + (size_t)T * rpad; H.b2 = d_b2 + rpad; H.minmax = d_mmh;
-      // tv/b2 regions past the overlap batch
+      H.ntmpl = 1; H.rpad = 1; H.ntask = nh_c; H.tasks = d_hgt + hbeg[c];
       RET_IF(iq_launch_gather(ctx, H));
       CorrLaunch Ch;
-      Ch.img = ctx->d_ti; Ch.img_dims = ctx->ti; Ch.out_dims = distD; Ch.K = (int)hn;
-      Ch.klist = d_hk + h0; Ch.tv = H.tv; Ch.rpad = 1; Ch.ntmpl = 1; Ch.b2 = H.b2;
-      Ch.disabled = d_dis; Ch.out = d_Dh; Ch.out_stride = P; Ch.minmax = d_mmh;
+      Ch.img = ctx->d_ti; Ch.img_dims = ctx->ti; Ch.out_dims = distD; Ch.tile = tileD;
+      Ch.rpad = 1; Ch.ntmpl = 1; Ch.out_stride = P; Ch.disabled = d_dis;
+      Ch.ntask = nh_c; Ch.tasks = d_hct + hbeg[c]; Ch.flops = 1;
       RET_IF(iq_launch_corr(ctx, Ch));
     }
     // pick
     PickLaunch L;
-    L.P = P; L.npat = npat; L.tol = p->tol; L.seed = p->seed; L.tile = s.tile; L.real0 = 0;
-    L.nreal = R;
-    int na = 0;
-    if (s.hardtile) {
-      L.D0 = d_Dh; L.D0_rstride = 0; L.mm0 = d_mmh; L.mm0_rstride = 0;
-      L.aux[na] = d_D; L.aux_rstride[na] = P;
-      L.aux_mm[na] = d_mm; L.aux_mm_rstride[na] = 2;
-      ++na;
-    } else {
-      L.D0 = d_D; L.D0_rstride = P; L.mm0 = d_mm; L.mm0_rstride = 2;
-    }
-    for (int q = 0; q < nsoft; ++q) {
-      L.aux[na] = d_soft + ((int64_t)q * nslot + slot_of[s.tile]) * P;
-      L.aux_rstride[na] = 0;
-      L.aux_mm[na] = d_softmm + 2 * ((int64_t)q * nslot + slot_of[s.tile]);
-      L.aux_mm_rstride[na] = 0;
-      ++na;
-    }
-    L.naux = na;
+    L.P = P; L.npat = npat; L.tol = p->tol; L.seed = p->seed; L.real0 = 0; L.nreal = R;
+    L.ntask = m; L.tasks = d_pt + k0; L.naux_max = nsoft + chard[c];
     L.dbsize_norm = dbn; L.dbsize_zero = dbz; L.nseq_norm = nsn; L.nseq_zero = nsz;
     for (int q = 0; q < IQ_MAX_SEQ; ++q) { L.seq_norm[q] = q < nsn ? seqn[q] : 0; L.seq_zero[q] = q < nsz ? seqz[q] : 0; }
     L.cand = d_cand; L.k0 = d_k0; L.v0 = d_v0; L.k1 = d_k1; L.v1 = d_v1; L.w = d_w; L.prod = d_prod;
@@ -608,26 +702,25 @@ extern "C" int iq_simulate(iq_ctx* ctx, const iq_sim_params* p, const iq_hard_da
     L.stats = ctx->prof ? ctx->d_stats : nullptr;
     RET_IF(iq_launch_pick(ctx, L));
     // boundary cuts
-    if (s.nslab > 0) {
+    if (cslab[c] > 0) {
       CutLaunch K;
-      K.nslab = s.nslab;
-      for (int i = 0; i < s.nslab; ++i) K.slab[i] = s.slab[i];
-      K.nreal = R;
-      K.sim = d_sim; K.sim_dims = padD; K.sim_rstride = padvol; K.tile_start = tstart;
+      K.nreal = R; K.ntask = m; K.nslab_max = cslab[c]; K.tasks = d_st + k0;
+      K.sim = d_sim; K.sim_dims = padD; K.sim_rstride = padvol;
       K.ti = ctx->d_ti; K.ti_dims = ctx->ti; K.dist_dims = distD; K.rind = d_rind;
       K.out = d_cutbuf; K.slabmax = slabmax;
       K.scratch = d_cutscr; K.scratch_per_cta = cutscr_per;
       K.status = ctx->d_status;
       K.stats = ctx->prof ? ctx->d_stats : nullptr;
+      K.gr_period = ctx->cut_gr_period;
+      K.threads = ctx->cut_threads;
       RET_IF(iq_launch_cut(ctx, K));
     }
     // paste
     PasteLaunch Pl;
-    Pl.nreal = R; Pl.sim = d_sim; Pl.sim_dims = padD; Pl.sim_rstride = padvol; Pl.cut = d_cut;
-    Pl.tile_start = tstart; Pl.tile = tileD; Pl.ti = ctx->d_ti; Pl.ti_dims = ctx->ti;
-    Pl.dist_dims = distD; Pl.rind = d_rind; Pl.nslab = s.nslab;
-    for (int i = 0; i < s.nslab; ++i) Pl.slab[i] = s.slab[i];
-    Pl.cutbuf = d_cutbuf; Pl.slabmax = slabmax;
+    Pl.nreal = R; Pl.ntask = m; Pl.tasks = d_st + k0;
+    Pl.sim = d_sim; Pl.sim_dims = padD; Pl.sim_rstride = padvol; Pl.cut = d_cut;
+    Pl.tile = tileD; Pl.ti = ctx->d_ti; Pl.ti_dims = ctx->ti; Pl.dist_dims = distD;
+    Pl.rind = d_rind; Pl.cutbuf = d_cutbuf; Pl.slabmax = slabmax;
     RET_IF(iq_launch_paste(ctx, Pl));
   }
 

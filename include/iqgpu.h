@@ -153,6 +153,16 @@ int iq_profile_get(iq_ctx* ctx, const char* kernel, double* ms_total, int64_t* l
 /* Kernels this context has launched since it was created. */
 int64_t iq_ctx_launches(iq_ctx* ctx);
 
+/*
+ * Tuning knobs of a context (launch shapes and heuristics; results do not depend on them):
+ *   "graphcut.gr_period"  rounds between global relabels of the boundary cut (default 32)
+ *   "graphcut.threads"    threads per cut CTA: 256, 512 or 1024 (default 512)
+ *   "sim.level_chunk"     most tiles of one dependency level simulated together (default 64;
+ *                         1 processes the tile path one tile at a time)
+ * Returns IQ_ERR_ARG for an unknown name or an out-of-range value.
+ */
+int iq_set_option(iq_ctx* ctx, const char* name, int64_t value);
+
 #ifdef __cplusplus
 }
 #endif
