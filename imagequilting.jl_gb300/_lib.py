@@ -65,6 +65,11 @@ SIGNATURES = {
                                ctypes.POINTER(ctypes.c_void_p), ctypes.c_double, ctypes.c_uint64,
                                ctypes.c_int64, ctypes.c_int64, c_i64p, c_i64p, c_i64p,
                                ctypes.POINTER(ctypes.c_double), ctypes.c_int64]),
+    "iq_pick_noalloc": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int64, ctypes.c_int32,
+                                       ctypes.POINTER(ctypes.c_void_p), ctypes.c_double,
+                                       ctypes.c_uint64, ctypes.c_int64, ctypes.c_int64, c_i64p,
+                                       c_i64p, c_i64p, ctypes.POINTER(ctypes.c_double),
+                                       ctypes.c_int64, ctypes.c_void_p]),
     "iq_graphcut": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                                    ctypes.c_int32, c_i64p, ctypes.c_int32, ctypes.c_void_p]),
     "iq_finddisabled": (ctypes.c_int, [ctypes.c_void_p, c_i64p, ctypes.c_void_p]),

@@ -122,6 +122,23 @@ int iq_pick(iq_ctx* ctx, const float* D, int64_t P, int32_t naux, const float* c
             int64_t* out_ncand, int64_t* out_cands, double* out_weights, int64_t cap);
 
 /*
+ * iq_pick without any device allocation. No counterpart in the reference: for hosts that
+ * cannot call cudaMalloc (device memory owned by their own pool allocator, or loops that
+ * cannot afford its device-wide synchronization). Scratch lives in a file-scope __device__
+ * array of the library (about 13 MB, held by every GPU that loads it until exit), so:
+ *   - P <= 262144 positions and naux <= 3, else IQ_ERR_LIMIT;
+ *   - the first call on a device looks up the array (cudaGetSymbolAddress): make it before
+ *     any stream capture;
+ *   - all calls share the array; calls that overlap on the GPU race and must be serialized.
+ * D and Ds may be host or device memory; out_* are host memory. `stream` is a cudaStream_t
+ * (NULL: the legacy default stream). Results equal iq_pick's.
+ */
+int iq_pick_noalloc(const float* D, int64_t P, int32_t naux, const float* const* Ds, double tol,
+                    uint64_t seed, int64_t tile, int64_t real, int64_t* out_index,
+                    int64_t* out_ncand, int64_t* out_cands, double* out_weights, int64_t cap,
+                    void* stream);
+
+/*
  * Minimum-error boundary cut (src/graphcut.jl:5-84) of two arrays of extents `size` along
  * `dim` (0-based). mask[v] = 1 when voxel v stays on the source side (keeps A).
  */
