@@ -247,6 +247,9 @@ def run_ours(args, W, dist, rank, world):
     dev = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(dev)
     ctx = iq.Context(dev)
+    for opt in args.option:
+        name, val = opt.split("=", 1)
+        ctx.set_option(name, int(val))
     stream = torch.cuda.ExternalStream(ctx.stream, device=dev)
     N = W["ti"].ndim
     nreal = W["nreal"]
@@ -402,6 +405,7 @@ def run_ours(args, W, dist, rank, world):
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded Gaussian fields)",
             "config": {"workload": W["desc"], "global_batch": nreal * world,
+                       "options": args.option,
                        "voxels_per_step": voxels * world, "parallelism": "replicas x%d" % world,
                        "l2": "working set > L2 (simulation grids 350 MB, soft maps 1.6 GB)",
                        "form": "plain (FP32 direct correlation)"},
@@ -425,6 +429,8 @@ def main():
     ap.add_argument("--cpu-budget", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer arm")
+    ap.add_argument("--option", action="append", default=[],
+                    help="library tuning knob name=value (iq_set_option), repeatable")
     args = ap.parse_args()
     dist, rank, world = dist_setup()
     W = workload(args.workload)

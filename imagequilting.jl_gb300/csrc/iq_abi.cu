@@ -188,6 +188,11 @@ extern "C" int iq_set_option(iq_ctx* ctx, const char* name, int64_t value) {
     ctx->cut_threads = (int)value;
     return IQ_OK;
   }
+  if (!strcmp(name, "corr.variant")) {
+    if (value < 0 || value > 3) return iq_set_error(IQ_ERR_ARG, "corr.variant must be 0..3");
+    ctx->corr_variant = (int)value;
+    return IQ_OK;
+  }
   if (!strcmp(name, "sim.level_chunk")) {
     if (value < 1 || value > 4096) return iq_set_error(IQ_ERR_ARG, "level_chunk out of range");
     ctx->level_chunk = value;

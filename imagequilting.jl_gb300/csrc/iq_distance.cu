@@ -50,8 +50,8 @@ __device__ __forceinline__ double box_sum(const double* __restrict__ ii, int64_t
   return s;
 }
 
-template <int RT, int PJ>
-__global__ void __launch_bounds__(CORR_THREADS) corr_kernel(const CorrArgs a) {
+template <int RT, int PJ, int MINB>
+__global__ void __launch_bounds__(CORR_THREADS, MINB) corr_kernel(const CorrArgs a) {
   __shared__ int32_t s_off[CORR_KC];
   __shared__ __align__(16) float s_tv[CORR_KC * RT];
   __shared__ unsigned s_min[CORR_THREADS / 32][RT], s_max[CORR_THREADS / 32][RT];
@@ -181,11 +181,11 @@ __global__ void __launch_bounds__(CORR_THREADS) corr_kernel(const CorrArgs a) {
   }
 }
 
-template <int RT, int PJ>
+template <int RT, int PJ, int MINB = 1>
 void launch_corr_t(const CorrArgs& a, int ntask, cudaStream_t s) {
   dim3 grid((unsigned)((a.P + CORR_THREADS * PJ - 1) / (CORR_THREADS * PJ)),
             (unsigned)(a.rpad / RT), (unsigned)ntask);
-  corr_kernel<RT, PJ><<<grid, CORR_THREADS, 0, s>>>(a);
+  corr_kernel<RT, PJ, MINB><<<grid, CORR_THREADS, 0, s>>>(a);
 }
 
 // ---- gather of template values --------------------------------------------------------
@@ -322,7 +322,15 @@ int iq_launch_corr(iq_ctx* ctx, const CorrLaunch& L) {
   const int rt = iq_register_tile(L.rpad);
   iq_timer_start(ctx, "corr");
   switch (rt) {
-    case 16: launch_corr_t<16, 4>(a, L.ntask, ctx->stream); break;
+    case 16:
+      // launch shapes of the 16-template tile (register budget vs positions per thread)
+      switch (ctx->corr_variant) {
+        case 1: launch_corr_t<16, 4, 3>(a, L.ntask, ctx->stream); break;
+        case 2: launch_corr_t<16, 8, 2>(a, L.ntask, ctx->stream); break;
+        case 3: launch_corr_t<16, 2, 4>(a, L.ntask, ctx->stream); break;
+        default: launch_corr_t<16, 4>(a, L.ntask, ctx->stream); break;
+      }
+      break;
     case 8: launch_corr_t<8, 4>(a, L.ntask, ctx->stream); break;
     case 4: launch_corr_t<4, 8>(a, L.ntask, ctx->stream); break;
     case 2: launch_corr_t<2, 8>(a, L.ntask, ctx->stream); break;

@@ -58,6 +58,7 @@ struct Graph {
   double* ex;
   double* pamt;
   int* h[2];
+  int* front[2];  // BFS frontier lists
   signed char* pdir;
   uint8_t* info;  // bits 0-5: neighbour exists in direction 0..5; bits 6-7: kind
 
@@ -83,26 +84,53 @@ struct Graph {
   }
 };
 
-__device__ int global_relabel(const Graph& g, int* hc) {
-  for (int u = threadIdx.x; u < g.n; u += blockDim.x)
-    if (g.kind(u) == 0) hc[u] = g.NH;
+// Exact heights: breadth-first search from t over open arcs. Each level only examines the
+// neighbours of the previous level's frontier (frontier lists fa/fb, counters cnt[2]), so the
+// search costs O(edges) instead of O(nodes x levels). Heights are BFS distances, whatever
+// order the frontier is filled in. Returns the number of levels.
+__device__ int global_relabel(const Graph& g, int* hc, int* fa, int* fb, int* cnt) {
+  if (threadIdx.x == 0) { cnt[0] = 0; cnt[1] = 0; }
   __syncthreads();
-  for (int level = 0; level < g.NH; ++level) {
-    int any = 0;
-    for (int u = threadIdx.x; u < g.n; u += blockDim.x) {
-      if (g.kind(u) != 0 || hc[u] != g.NH) continue;
+  const int dsink = 2 * g.d + 1;  // direction towards the sink slice
+  for (int u = threadIdx.x; u < g.n; u += blockDim.x) {
+    if (g.kind(u) != 0) continue;
+    int h = g.NH;
+    int v;
+    if (g.nbr(u, dsink, v) && g.kind(v) == 2) {
+      double *ruv, *rvu;
+      g.arc(u, v, dsink, ruv, rvu);
+      if (g.open(ruv, rvu)) h = 1;
+    }
+    hc[u] = h;
+    if (h == 1) fa[atomicAdd(&cnt[0], 1)] = u;
+  }
+  __syncthreads();
+  int level = 1, cur = 0;
+  for (;;) {
+    const int nf = cnt[cur];
+    int* front = cur ? fb : fa;
+    int* next = cur ? fa : fb;
+    if (nf == 0) break;
+    if (threadIdx.x == 0) cnt[cur ^ 1] = 0;
+    __syncthreads();
+    for (int i = threadIdx.x; i < nf; i += blockDim.x) {
+      const int v = front[i];
       for (int dir = 0; dir < 6; ++dir) {
-        int v;
-        if (!g.nbr(u, dir, v)) continue;
-        if (g.height(hc, v) != level) continue;
+        int u;
+        if (!g.nbr(v, dir, u)) continue;
+        if (g.kind(u) != 0 || hc[u] != g.NH) continue;
         double *ruv, *rvu;
-        g.arc(u, v, dir, ruv, rvu);
-        if (g.open(ruv, rvu)) { hc[u] = level + 1; any = 1; break; }
+        g.arc(u, v, dir ^ 1, ruv, rvu);  // arc u -> v
+        if (!g.open(ruv, rvu)) continue;
+        if (atomicCAS(&hc[u], g.NH, level + 1) == g.NH) next[atomicAdd(&cnt[cur ^ 1], 1)] = u;
       }
     }
-    if (!__syncthreads_or(any)) return level + 1;
+    __syncthreads();
+    cur ^= 1;
+    ++level;
   }
-  return g.NH;
+  __syncthreads();
+  return level;
 }
 
 __global__ void __launch_bounds__(CUT_MAX_THREADS) cut_kernel(const CutArgs a) {
@@ -133,7 +161,10 @@ __global__ void __launch_bounds__(CUT_MAX_THREADS) cut_kernel(const CutArgs a) {
   int* ip = reinterpret_cast<int*>(dp + 8 * n);
   g.h[0] = ip;
   g.h[1] = ip + n;
-  g.pdir = reinterpret_cast<signed char*>(ip + 2 * n);
+  g.front[0] = ip + 2 * n;
+  g.front[1] = ip + 3 * n;
+  __shared__ int s_cnt[2];
+  g.pdir = reinterpret_cast<signed char*>(ip + 4 * n);
   g.info = reinterpret_cast<uint8_t*>(g.pdir + n);
   float* Av = reinterpret_cast<float*>(g.pamt);  // A and B alias pamt during set-up
   float* Bv = Av + n;                            // (8n bytes = pamt)
@@ -216,7 +247,7 @@ __global__ void __launch_bounds__(CUT_MAX_THREADS) cut_kernel(const CutArgs a) {
   int cur = 0;
   int round = 0, levels = 0;
   if (g.L > 2) {
-    levels += global_relabel(g, g.h[cur]);
+    levels += global_relabel(g, g.h[cur], g.front[0], g.front[1], s_cnt);
     bool capped = false;
     for (;;) {
       int* hc = g.h[cur];
@@ -283,11 +314,11 @@ __global__ void __launch_bounds__(CUT_MAX_THREADS) cut_kernel(const CutArgs a) {
       if (!active) break;
       if (round >= a.round_cap) { capped = true; break; }
       if (round % a.gr_period == 0) {
-        levels += global_relabel(g, g.h[cur]);
+        levels += global_relabel(g, g.h[cur], g.front[0], g.front[1], s_cnt);
         __syncthreads();
       }
     }
-    levels += global_relabel(g, g.h[cur]);
+    levels += global_relabel(g, g.h[cur], g.front[0], g.front[1], s_cnt);
     __syncthreads();
     if (capped && threadIdx.x == 0) iq_dev_fail(a.status, IQ_ERR_CUTCAP);
   }
@@ -296,6 +327,8 @@ __global__ void __launch_bounds__(CUT_MAX_THREADS) cut_kernel(const CutArgs a) {
     atomicAdd(a.stats + ST_CUT_ROUNDS, (unsigned long long)round);
     atomicAdd(a.stats + ST_CUT_LEVELS, (unsigned long long)levels);
     atomicAdd(a.stats + ST_CUT_CTAS, 1ull);
+    atomicMax(a.stats + ST_CUT_MAXROUNDS, (unsigned long long)round);
+    atomicMax(a.stats + ST_CUT_MAXLEVELS, (unsigned long long)levels);
   }
   // ---- mask: not sink side ----
   const int* hc = g.h[cur];
@@ -310,9 +343,9 @@ __global__ void __launch_bounds__(CUT_MAX_THREADS) cut_kernel(const CutArgs a) {
 }  // namespace
 
 size_t iq_cut_scratch_bytes(int64_t nodes) {
-  // rf, rb (6n doubles), ex, pamt (2n doubles), two heights (2n ints), push dir and node
-  // info (2n bytes)
-  size_t b = (size_t)nodes * (8 * 8 + 2 * 4 + 2);
+  // rf, rb (6n doubles), ex, pamt (2n doubles), two heights and two BFS frontiers (4n ints),
+  // push dir and node info (2n bytes)
+  size_t b = (size_t)nodes * (8 * 8 + 4 * 4 + 2);
   return (b + 255) & ~(size_t)255;
 }
 
@@ -337,11 +370,15 @@ int iq_launch_cut(iq_ctx* ctx, const CutLaunch& L) {
   const size_t need = iq_cut_scratch_bytes(nmax);
   static int smem_limit = -1;
   if (smem_limit < 0) {
+    // dynamic shared memory may use the opt-in maximum minus the kernel's static part
     int dev = 0, v = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-    smem_limit = v;
-    cudaFuncSetAttribute(cut_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, v);
+    IQ_CUDA_OK(cudaGetDevice(&dev));
+    IQ_CUDA_OK(cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+    cudaFuncAttributes fa;
+    IQ_CUDA_OK(cudaFuncGetAttributes(&fa, cut_kernel));
+    const int lim = v - (int)fa.sharedSizeBytes;
+    IQ_CUDA_OK(cudaFuncSetAttribute(cut_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, lim));
+    smem_limit = lim;
   }
   size_t dyn = 0;
   if ((int64_t)need <= smem_limit) {

@@ -48,6 +48,7 @@ struct iq_ctx {
   int cut_gr_period = 32;
   int cut_threads = 512;
   int64_t level_chunk = 64;     // most tiles of one dependency level launched together
+  int corr_variant = 1;         // launch shape of the 16-template correlation
 };
 enum IqStat { ST_CUT_ROUNDS = 0, ST_CUT_LEVELS, ST_CUT_CTAS, ST_PICK_ITERS, ST_PICK_CAND,
               ST_PICK_CTAS, ST_CUT_MAXROUNDS, ST_CUT_MAXLEVELS, ST_COUNT };

@@ -293,15 +293,23 @@ __device__ void hist_select(Smem& s, uint32_t* hist, unsigned long long* sbuf, S
     for (int j = 0; j < NS; ++j) sh[j] = pend[j] ? bin_shift(lo[j], hi[j]) : 0;
     for (int i = threadIdx.x; i < NS * NBIN; i += PT) hist[i] = 0;
     __syncthreads();
-    for (int64_t it = 0; it < iters; ++it) {
-      const int64_t p = it * PT + threadIdx.x;
-      if (p >= P) break;
+    for (int64_t it0 = 0; it0 < iters; it0 += 4) {
+      // four independent loads per source before the atomics (memory-level parallelism)
+      uint32_t bv[NS][4];
 #pragma unroll
-      for (int j = 0; j < NS; ++j) {
-        if (!pend[j]) continue;
-        const uint32_t b = fbits(req[j].src[p]);
-        if (b >= lo[j] && b <= hi[j]) atomicAdd(&hist[j * NBIN + ((b - lo[j]) >> sh[j])], 1u);
+      for (int u = 0; u < 4; ++u) {
+        const int64_t p = (it0 + u) * PT + threadIdx.x;
+#pragma unroll
+        for (int j = 0; j < NS; ++j)
+          bv[j][u] = (p < P && pend[j]) ? fbits(req[j].src[p]) : 0xFFFFFFFFu;
       }
+#pragma unroll
+      for (int u = 0; u < 4; ++u)
+#pragma unroll
+        for (int j = 0; j < NS; ++j) {
+          const uint32_t b = bv[j][u];
+          if (b >= lo[j] && b <= hi[j]) atomicAdd(&hist[j * NBIN + ((b - lo[j]) >> sh[j])], 1u);
+        }
     }
     __syncthreads();
     // locate the bin of each pending source: warp j scans source j's 4096 bins
@@ -356,13 +364,20 @@ __device__ void hist_select(Smem& s, uint32_t* hist, unsigned long long* sbuf, S
         // collect the bin's (value, index) keys and sort them
         if (threadIdx.x == 0) s.ncol = 0;
         __syncthreads();
-        for (int64_t it = 0; it < iters; ++it) {
-          const int64_t p = it * PT + threadIdx.x;
-          if (p >= P) break;
-          const uint32_t v = fbits(req[j].src[p]);
-          if (v >= blo && v <= bhi) {
-            const uint32_t at = atomicAdd(&s.ncol, 1u);
-            sbuf[at] = ((unsigned long long)v << 32) | (uint32_t)p;
+        for (int64_t it0 = 0; it0 < iters; it0 += 4) {
+          uint32_t vv[4];
+#pragma unroll
+          for (int u = 0; u < 4; ++u) {
+            const int64_t p = (it0 + u) * PT + threadIdx.x;
+            vv[u] = p < P ? fbits(req[j].src[p]) : 0xFFFFFFFFu;
+          }
+#pragma unroll
+          for (int u = 0; u < 4; ++u) {
+            const uint32_t v = vv[u];
+            if (v >= blo && v <= bhi) {
+              const uint32_t at = atomicAdd(&s.ncol, 1u);
+              sbuf[at] = ((unsigned long long)v << 32) | (uint32_t)((it0 + u) * PT + threadIdx.x);
+            }
           }
         }
         __syncthreads();
@@ -392,12 +407,7 @@ __device__ int64_t compact(Smem& s, const Pred& pred, int64_t P, int32_t* out) {
   const int64_t tile = (int64_t)PT * CITEMS;
   for (int64_t t0 = 0; t0 < P; t0 += tile) {
     const int64_t p0 = t0 + (int64_t)threadIdx.x * CITEMS;
-    uint32_t bits = 0;
-#pragma unroll
-    for (int i = 0; i < CITEMS; ++i) {
-      const int64_t p = p0 + i;
-      if (p < P && pred(p)) bits |= 1u << i;
-    }
+    const uint32_t bits = pred.eval8(p0, P);
     uint32_t total;
     uint32_t off = block_excl_sum(s, (uint32_t)__popc(bits), total);
     if (out) {
@@ -413,7 +423,17 @@ __device__ int64_t compact(Smem& s, const Pred& pred, int64_t P, int32_t* out) {
 
 struct ThrPred {
   const float* D; double thr;
-  __device__ bool operator()(int64_t p) const { return (double)D[p] <= thr; }
+  // bit i set when D[p0 + i] <= thr (positions past P excluded)
+  __device__ uint32_t eval8(int64_t p0, int64_t P) const {
+    float v[CITEMS];
+#pragma unroll
+    for (int i = 0; i < CITEMS; ++i) v[i] = p0 + i < P ? D[p0 + i] : __int_as_float(0x7F800000);
+    uint32_t bits = 0;
+#pragma unroll
+    for (int i = 0; i < CITEMS; ++i)
+      if (p0 + i < P && (double)v[i] <= thr) bits |= 1u << i;
+    return bits;
+  }
 };
 
 template <int NAUX>
@@ -422,12 +442,26 @@ struct RelaxPred {
   int naux;  // <= NAUX
   const float* aux[NAUX > 0 ? NAUX : 1];
   Key ka[NAUX > 0 ? NAUX : 1];
-  __device__ bool operator()(int64_t p) const {
-    if (!key_le(fbits(D[p]), (uint32_t)p, kD)) return false;
+  // bit i set when position p0 + i is in the top set of D and of every auxiliary source
+  __device__ uint32_t eval8(int64_t p0, int64_t P) const {
+    uint32_t b[CITEMS];
 #pragma unroll
-    for (int a = 0; a < NAUX; ++a)
-      if (a < naux && !key_le(fbits(aux[a][p]), (uint32_t)p, ka[a])) return false;
-    return true;
+    for (int i = 0; i < CITEMS; ++i) b[i] = p0 + i < P ? fbits(D[p0 + i]) : 0xFFFFFFFFu;
+    uint32_t bits = 0;
+#pragma unroll
+    for (int i = 0; i < CITEMS; ++i)
+      if (p0 + i < P && key_le(b[i], (uint32_t)(p0 + i), kD)) bits |= 1u << i;
+#pragma unroll
+    for (int a = 0; a < NAUX; ++a) {
+      if (a >= naux || !bits) continue;
+      uint32_t c[CITEMS];
+#pragma unroll
+      for (int i = 0; i < CITEMS; ++i) c[i] = (bits >> i & 1u) ? fbits(aux[a][p0 + i]) : 0u;
+#pragma unroll
+      for (int i = 0; i < CITEMS; ++i)
+        if ((bits >> i & 1u) && !key_le(c[i], (uint32_t)(p0 + i), ka[a])) bits &= ~(1u << i);
+    }
+    return bits;
   }
 };
 
@@ -720,8 +754,10 @@ template <int NAUX>
 cudaError_t launch_pick_t(const PickArgs& a, int nblocks, cudaStream_t st) {
   static bool attr = false;
   if (!attr) {
-    cudaFuncSetAttribute(pick_kernel<NAUX>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)DYN_BYTES);
+    cudaError_t e = cudaFuncSetAttribute(pick_kernel<NAUX>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)DYN_BYTES);
+    if (e != cudaSuccess) return e;
     attr = true;
   }
   pick_kernel<NAUX><<<nblocks, PT, DYN_BYTES, st>>>(a);

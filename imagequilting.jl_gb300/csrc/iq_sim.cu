@@ -457,6 +457,7 @@ extern "C" int iq_simulate(iq_ctx* ctx, const iq_sim_params* p, const iq_hard_da
     int dev = 0, lim = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&lim, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    lim -= 1024;  // the cut kernel's static shared memory
     if ((int64_t)iq_cut_scratch_bytes(slabmax) > lim) cutscr_per = (int64_t)iq_cut_scratch_bytes(slabmax);
   }
   const int64_t per_step = (int64_t)R * P * (4 + 4 + 16 + 16) + P * 4 + T * (rpad + 1) * 4 +

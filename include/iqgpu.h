@@ -174,6 +174,9 @@ int64_t iq_ctx_launches(iq_ctx* ctx);
  * Tuning knobs of a context (launch shapes and heuristics; results do not depend on them):
  *   "graphcut.gr_period"  rounds between global relabels of the boundary cut (default 32)
  *   "graphcut.threads"    threads per cut CTA: 256, 512 or 1024 (default 512)
+ *   "corr.variant"        launch shape of the 16-template correlation: 0 (4 positions per
+ *                         thread), 1 (same, 3 CTAs per SM; default), 2 (8 positions),
+ *                         3 (2 positions)
  *   "sim.level_chunk"     most tiles of one dependency level simulated together (default 64;
  *                         1 processes the tile path one tile at a time)
  * Returns IQ_ERR_ARG for an unknown name or an out-of-range value.
