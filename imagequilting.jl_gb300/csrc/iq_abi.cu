@@ -193,6 +193,15 @@ extern "C" int iq_set_option(iq_ctx* ctx, const char* name, int64_t value) {
     ctx->corr_variant = (int)value;
     return IQ_OK;
   }
+  if (!strcmp(name, "corr.engine")) {
+    if (value < 0 || value > 1) return iq_set_error(IQ_ERR_ARG, "corr.engine must be 0 or 1");
+    ctx->corr_engine = (int)value;
+    return IQ_OK;
+  }
+  if (!strcmp(name, "sim.max_steps")) {
+    ctx->max_steps = value < 0 ? -1 : value;
+    return IQ_OK;
+  }
   if (!strcmp(name, "sim.level_chunk")) {
     if (value < 1 || value > 4096) return iq_set_error(IQ_ERR_ARG, "level_chunk out of range");
     ctx->level_chunk = value;
@@ -254,9 +263,12 @@ extern "C" int iq_set_ti(iq_ctx* ctx, const void* ti, int32_t dtype, int32_t ndi
   IQ_CUDA_OK(cudaMemcpyAsync(&total, ctx->d_nanii + (d.x + 1) * (d.y + 1) * (d.z + 1) - 1,
                              sizeof(int32_t), cudaMemcpyDeviceToHost, ctx->stream));
   IQ_CUDA_OK(cudaStreamSynchronize(ctx->stream));
+  bool exact = false;
+  if ((rc = iq_tf32_exact(ctx, ctx->d_ti, n, exact))) return rc;
   ctx->ti = d;
   ctx->ndim = ndim;
   ctx->ti_nan = total;
+  ctx->ti_tf32 = exact;
   ctx->has_ti = true;
   return IQ_OK;
 }
@@ -284,17 +296,37 @@ extern "C" int iq_fastdistance(iq_ctx* ctx, const int64_t* tilesize, int32_t ntm
   for (int64_t k = 0; k < T; ++k)
     if (w[k]) kl.push_back(kpack(k % t.x, (k / t.x) % t.y, k / (t.x * t.y)));
   const int K = (int)kl.size();
+  // Is the mask the tile minus one box (the shape of every overlap mask)? Then the tensor-core
+  // kernel applies and A2 comes from the integral image.
+  int64_t blo[3] = {0, 0, 0}, bhi[3] = {0, 0, 0};
+  bool boxmask = true;
+  {
+    int64_t mn[3] = {t.x, t.y, t.z}, mx[3] = {-1, -1, -1}, nz = 0;
+    for (int64_t k = 0; k < T; ++k)
+      if (!w[k]) {
+        const int64_t c3[3] = {k % t.x, (k / t.x) % t.y, k / (t.x * t.y)};
+        for (int d = 0; d < 3; ++d) { mn[d] = std::min(mn[d], c3[d]); mx[d] = std::max(mx[d], c3[d]); }
+        ++nz;
+      }
+    if (nz > 0) {
+      const int64_t vol = (mx[0] - mn[0] + 1) * (mx[1] - mn[1] + 1) * (mx[2] - mn[2] + 1);
+      boxmask = vol == nz;
+      for (int d = 0; d < 3; ++d) { blo[d] = mn[d]; bhi[d] = mx[d] + 1; }
+    }
+  }
+  const bool use_tc = ctx->corr_engine == 1 && boxmask && K > 0;
   // A2 by integral image when the mask is all ones, else direct
   const bool full = K == T;
   const int rt = iq_register_tile(ntmpl);
   const int rpad = ((ntmpl + rt - 1) / rt) * rt;
   float* d_tmpl = (float*)iq_scratch(ctx, S_TMP2, sizeof(float) * T * ntmpl);
   uint32_t* d_kl = (uint32_t*)iq_scratch(ctx, S_KLIST, sizeof(uint32_t) * std::max(K, 1));
-  float* d_tv = (float*)iq_scratch(ctx, S_TV, sizeof(float) * std::max<int64_t>(K, 1) * rpad);
+  float* d_tv = use_tc ? nullptr
+                       : (float*)iq_scratch(ctx, S_TV, sizeof(float) * std::max<int64_t>(K, 1) * rpad);
   double* d_b2 = (double*)iq_scratch(ctx, S_B2, sizeof(double) * rpad);
   uint8_t* d_dis = (uint8_t*)iq_scratch(ctx, S_DIS, (size_t)P);
   float* d_out = (float*)iq_scratch(ctx, S_D, sizeof(float) * P * ntmpl);
-  if (!d_tmpl || !d_kl || !d_tv || !d_b2 || !d_dis || !d_out) return IQ_ERR_ALLOC;
+  if (!d_tmpl || !d_kl || (!use_tc && !d_tv) || !d_b2 || !d_dis || !d_out) return IQ_ERR_ALLOC;
   IQ_CUDA_OK(cudaMemcpyAsync(d_tmpl, tmpl, sizeof(float) * T * ntmpl, cudaMemcpyDefault, ctx->stream));
   if (K) IQ_CUDA_OK(cudaMemcpyAsync(d_kl, kl.data(), sizeof(uint32_t) * K, cudaMemcpyHostToDevice, ctx->stream));
   if ((rc = iq_launch_disabled(ctx, ctx->d_nanii, ctx->ti, t, d_dis))) return rc;
@@ -303,13 +335,53 @@ extern "C" int iq_fastdistance(iq_ctx* ctx, const int64_t* tilesize, int32_t ntm
   G.ntmpl = ntmpl; G.rpad = rpad;
   G.t0 = GatherTask{d_kl, K, 0, nullptr, d_tv, d_b2, nullptr};
   if ((rc = iq_launch_gather(ctx, G))) return rc;
-  CorrLaunch C;
-  C.img = ctx->d_ti; C.img_dims = ctx->ti; C.out_dims = od; C.tile = t;
-  C.rpad = rpad; C.ntmpl = ntmpl; C.out_stride = P; C.disabled = d_dis;
-  // all-ones mask: A^2 from the integral image (the full tile, no inner box); otherwise summed
-  C.t0 = CorrTask{d_kl, K, d_tv, d_b2, full ? ctx->d_ti2ii : nullptr, {0, 0, 0}, {0, 0, 0},
-                  d_out, nullptr};
-  if ((rc = iq_launch_corr(ctx, C))) return rc;
+  std::vector<TcCol> cols;
+  std::vector<uint32_t> stw;
+  if (use_tc) {
+    bool exact = false;
+    if (ctx->ti_tf32 && (rc = iq_tf32_exact(ctx, d_tmpl, T * ntmpl, exact))) return rc;
+    TcBox box0;
+    for (int d = 0; d < 3; ++d) { box0.lo[d] = (int32_t)blo[d]; box0.hi[d] = (int32_t)bhi[d]; }
+    TcStages stg;
+    iq_tc_stages(t, &box0, 1, stg);
+    const size_t ns = stg.word.size();
+    stw.resize(2 * ns);
+    for (size_t e = 0; e < ns; ++e) { stw[e] = stg.word[e]; stw[ns + e] = stg.prefix[e]; }
+    for (int32_t c0 = 0; c0 < ntmpl; c0 += IQ_TC_MAXN) {
+      const int nb = std::min<int32_t>(IQ_TC_MAXN, ntmpl - c0);
+      const int Np = (nb + 15) / 16 * 16;
+      for (int i = 0; i < Np; ++i)
+        cols.push_back(i < nb ? TcCol{(int64_t)(c0 + i) * T, d_out + (size_t)(c0 + i) * P, d_b2 + c0 + i, nullptr, 0, 0}
+                              : TcCol{-1, nullptr, nullptr, nullptr, 0, 0});
+    }
+    uint32_t* d_st = (uint32_t*)iq_scratch(ctx, S_TCSTAGE, sizeof(uint32_t) * std::max<size_t>(stw.size(), 1));
+    TcCol* d_cols = (TcCol*)iq_scratch(ctx, S_TCCOLS, sizeof(TcCol) * cols.size());
+    void* d_B = iq_scratch(ctx, S_TCB, (size_t)std::max<int64_t>(stg.nsteps, 1) * 64 * IQ_TC_MAXN);
+    if (!d_st || !d_cols || !d_B) return IQ_ERR_ALLOC;
+    IQ_CUDA_OK(cudaMemcpyAsync(d_st, stw.data(), sizeof(uint32_t) * stw.size(), cudaMemcpyHostToDevice, ctx->stream));
+    IQ_CUDA_OK(cudaMemcpyAsync(d_cols, cols.data(), sizeof(TcCol) * cols.size(), cudaMemcpyHostToDevice, ctx->stream));
+    size_t col0 = 0;
+    for (int32_t c0 = 0; c0 < ntmpl; c0 += IQ_TC_MAXN) {
+      const int nb = std::min<int32_t>(IQ_TC_MAXN, ntmpl - c0);
+      TcCorrLaunch L;
+      L.img = ctx->d_ti; L.img_dims = ctx->ti; L.out_dims = od; L.tile = t; L.ii = ctx->d_ti2ii;
+      L.nbox = 1; L.box[0] = box0;
+      L.disabled = d_dis;
+      L.stage_word = d_st; L.stage_prefix = d_st + ns; L.nstage = (int)ns; L.nsteps = stg.nsteps;
+      L.grid = d_tmpl; L.grid_dims = t; L.cols = d_cols + col0; L.N = (nb + 15) / 16 * 16;
+      L.B = d_B; L.exact = exact; L.flops = 2.0 * (double)P * (double)K * nb;
+      if ((rc = iq_launch_corr_tc(ctx, L))) return rc;
+      col0 += L.N;
+    }
+  } else {
+    CorrLaunch C;
+    C.img = ctx->d_ti; C.img_dims = ctx->ti; C.out_dims = od; C.tile = t;
+    C.rpad = rpad; C.ntmpl = ntmpl; C.out_stride = P; C.disabled = d_dis;
+    // all-ones mask: A^2 from the integral image (the full tile, no inner box); otherwise summed
+    C.t0 = CorrTask{d_kl, K, d_tv, d_b2, full ? ctx->d_ti2ii : nullptr, {0, 0, 0}, {0, 0, 0},
+                    d_out, nullptr};
+    if ((rc = iq_launch_corr(ctx, C))) return rc;
+  }
   IQ_CUDA_OK(cudaMemcpyAsync(out, d_out, sizeof(float) * P * ntmpl, cudaMemcpyDefault, ctx->stream));
   IQ_CUDA_OK(cudaStreamSynchronize(ctx->stream));
   return IQ_OK;

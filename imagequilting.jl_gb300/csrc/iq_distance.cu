@@ -34,22 +34,6 @@ struct CorrArgs {
   const CorrTask* tasks;      // one task per blockIdx.z
 };
 
-__device__ __forceinline__ double box_sum(const double* __restrict__ ii, int64_t sx, int64_t sxy,
-                                          int64_t x0, int64_t y0, int64_t z0, int64_t ex,
-                                          int64_t ey, int64_t ez) {
-  // sum over [x0, x0+ex) x [y0, y0+ey) x [z0, z0+ez) of an integral image with zero border
-  const int64_t x1 = x0 + ex, y1 = y0 + ey, z1 = z0 + ez;
-  double s = ii[x1 + sx * y1 + sxy * z1];
-  s -= ii[x0 + sx * y1 + sxy * z1];
-  s -= ii[x1 + sx * y0 + sxy * z1];
-  s += ii[x0 + sx * y0 + sxy * z1];
-  s -= ii[x1 + sx * y1 + sxy * z0];
-  s += ii[x0 + sx * y1 + sxy * z0];
-  s += ii[x1 + sx * y0 + sxy * z0];
-  s -= ii[x0 + sx * y0 + sxy * z0];
-  return s;
-}
-
 template <int RT, int PJ, int MINB>
 __global__ void __launch_bounds__(CORR_THREADS, MINB) corr_kernel(const CorrArgs a) {
   __shared__ int32_t s_off[CORR_KC];
@@ -135,9 +119,9 @@ __global__ void __launch_bounds__(CORR_THREADS, MINB) corr_kernel(const CorrArgs
     } else {
       int64_t x = p % a.dx, row = p / a.dx;
       int64_t y = row % a.dy, z = row / a.dy;
-      A2 = box_sum(t.ii, sx, sxy, x, y, z, a.tx, a.ty, a.tz);
+      A2 = iq_box_sum(t.ii, sx, sxy, x, y, z, a.tx, a.ty, a.tz);
       if (inner)
-        A2 -= box_sum(t.ii, sx, sxy, x + t.lo[0], y + t.lo[1], z + t.lo[2], t.hi[0] - t.lo[0],
+        A2 -= iq_box_sum(t.ii, sx, sxy, x + t.lo[0], y + t.lo[1], z + t.lo[2], t.hi[0] - t.lo[0],
                       t.hi[1] - t.lo[1], t.hi[2] - t.lo[2]);
     }
     const bool dis = a.disabled != nullptr && a.disabled[p];
@@ -215,10 +199,10 @@ __global__ void gather_kernel(const GatherArgs g) {
         uint32_t kk = k.klist[i];
         v = base[kx_of(kk) + g.gx * (ky_of(kk) + g.gy * (int64_t)kz_of(kk))];
       }
-      k.tv[(int64_t)i * g.rpad + t] = v;
+      if (k.tv) k.tv[(int64_t)i * g.rpad + t] = v;
       sq += (double)v * (double)v;
     }
-  } else {
+  } else if (k.tv) {
     for (int i = threadIdx.x; i < k.K; i += blockDim.x) k.tv[(int64_t)i * g.rpad + t] = 0.f;
   }
   // block reduction of the squares (fixed order: warp shuffles then warps in order)

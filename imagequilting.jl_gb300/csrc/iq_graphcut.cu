@@ -6,8 +6,12 @@
 // infinite source/sink slices follow the reference. The max-flow is a synchronous
 // push-relabel instead of Boykov-Kolmogorov:
 //   * the first slice along the cut dimension is contracted into s, the last into t;
+//   * capacities are rounded to multiples of q = 2^(ilogb(cmax) - 47), cmax the largest of
+//     the slab, so that every residual (<= 2 cmax) and excess (<= 12 cmax) is a multiple of q
+//     below 2^53 q and all flow arithmetic is exact (zero gradient sums give eps-denominator
+//     capacities ~2^52 times the others, which unquantized Float64 flows cannot resolve);
 //   * residuals are stored per directed arc in Float64; an arc is open when its residual is
-//     above 2^-30 of the larger residual of its edge (the oracle uses the same predicate);
+//     positive (the oracle quantizes and tests the same way);
 //   * each round: every active node pushes along its first admissible arc (h(u) = h(v) + 1),
 //     then every node gathers the flow pushed into it in a fixed order and relabels if it
 //     still has excess and no admissible arc -- deterministic, no atomics;
@@ -41,13 +45,6 @@ struct CutArgs {
 
 __device__ __forceinline__ long long dbits(double x) { return __double_as_longlong(x); }
 
-// saturation threshold of an edge, as bits: max(rf, rb) * 2^-30 (0 below 2^-992)
-__device__ __forceinline__ long long thr_bits(long long a, long long b) {
-  long long m = a > b ? a : b;
-  long long ex = m >> 52;
-  return ex <= 30 ? 0ll : m - (30ll << 52);
-}
-
 struct Graph {
   int n, ext[3], st[3];
   int d;          // cut dimension
@@ -78,9 +75,8 @@ struct Graph {
     if (dir & 1) { ruv = &rf[e][u]; rvu = &rb[e][u]; }
     else { ruv = &rb[e][v]; rvu = &rf[e][v]; }
   }
-  __device__ __forceinline__ bool open(const double* ruv, const double* rvu) const {
-    long long a = dbits(*ruv), b = dbits(*rvu);
-    return a > thr_bits(a, b);
+  __device__ __forceinline__ bool open(const double* ruv, const double*) const {
+    return dbits(*ruv) > 0;  // residuals are non-negative; +0 and -0 are closed
   }
 };
 
@@ -164,6 +160,8 @@ __global__ void __launch_bounds__(CUT_MAX_THREADS) cut_kernel(const CutArgs a) {
   g.front[0] = ip + 2 * n;
   g.front[1] = ip + 3 * n;
   __shared__ int s_cnt[2];
+  __shared__ unsigned long long s_cmax;  // bits of the largest capacity
+  if (threadIdx.x == 0) s_cmax = 0ull;
   g.pdir = reinterpret_cast<signed char*>(ip + 4 * n);
   g.info = reinterpret_cast<uint8_t*>(g.pdir + n);
   float* Av = reinterpret_cast<float*>(g.pamt);  // A and B alias pamt during set-up
@@ -225,9 +223,24 @@ __global__ void __launch_bounds__(CUT_MAX_THREADS) cut_kernel(const CutArgs a) {
       const double cap = __ddiv_rn((double)num, __dadd_rn((double)den, EPS));
       g.rf[e][u] = cap;
       g.rb[e][u] = cap;
+      atomicMax(&s_cmax, (unsigned long long)dbits(cap));
     }
   }
   __syncthreads();
+  // ---- round every capacity to a multiple of q = 2^(ilogb(cmax) - 47) (exact flows) ----
+  if (s_cmax != 0ull) {
+    int sh = ilogb(__longlong_as_double((long long)s_cmax)) - 47;
+    if (sh < -1074) sh = -1074;
+    for (int u = threadIdx.x; u < n; u += blockDim.x)
+      for (int e = 0; e < 3; ++e) {
+        int v;
+        if (!g.nbr(u, 2 * e + 1, v)) continue;
+        const double c = ldexp(rint(ldexp(g.rf[e][u], -sh)), sh);
+        g.rf[e][u] = c;
+        g.rb[e][u] = c;
+      }
+    __syncthreads();
+  }
 
   // ---- saturate the source slice: push c(s, v) into every interior node of slice 1 ----
   for (int u = threadIdx.x; u < n; u += blockDim.x) {

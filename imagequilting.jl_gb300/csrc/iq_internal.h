@@ -32,6 +32,7 @@ struct iq_ctx {
   double* d_ti2ii = nullptr;   // integral image of TI^2, (x+1)(y+1)(z+1) doubles
   int32_t* d_nanii = nullptr;  // integral image of the NaN indicator
   int64_t ti_nan = 0;          // number of NaN voxels
+  bool ti_tf32 = false;        // every prepared TI value is a TF32 value
   int* d_status = nullptr;     // device status word (first kernel error)
   // grow-only scratch buffers, by slot
   std::vector<void*> buf;
@@ -49,6 +50,8 @@ struct iq_ctx {
   int cut_threads = 512;
   int64_t level_chunk = 64;     // most tiles of one dependency level launched together
   int corr_variant = 1;         // launch shape of the 16-template correlation
+  int corr_engine = 1;          // 1: tensor-core (tcgen05) correlation for box masks, 0: SIMT
+  int64_t max_steps = -1;       // tiles simulated per realization (< 0: all)
 };
 enum IqStat { ST_CUT_ROUNDS = 0, ST_CUT_LEVELS, ST_CUT_CTAS, ST_PICK_ITERS, ST_PICK_CAND,
               ST_PICK_CTAS, ST_CUT_MAXROUNDS, ST_CUT_MAXLEVELS, ST_COUNT };
@@ -58,7 +61,8 @@ enum IqSlot {
   S_SIM = 0, S_CUT, S_D, S_DHARD, S_SOFT, S_TV, S_B2, S_KLIST, S_MINMAX, S_PICK_CAND,
   S_PICK_K0, S_PICK_V0, S_PICK_K1, S_PICK_V1, S_PICK_W, S_PICK_PROD, S_RIND, S_NCAND,
   S_CUTBUF, S_CUTSCR, S_DIS, S_AUX, S_AUXTI, S_AUXII, S_HARDLIST, S_HARDPTS, S_OUT,
-  S_TMP0, S_TMP1, S_TMP2, S_STARTS, S_SOFTMM, S_TASKS, S_VOX, S_COUNT
+  S_TMP0, S_TMP1, S_TMP2, S_STARTS, S_SOFTMM, S_TASKS, S_VOX, S_TCB, S_TCCOLS, S_TCSTAGE, S_TCB2, S_TCFLAG, S_TCSOFT,
+  S_COUNT
 };
 
 // device scratch of at least `bytes` in slot `slot` (contents undefined); nullptr on failure
@@ -136,6 +140,75 @@ struct GatherLaunch {
 int iq_launch_gather(iq_ctx* ctx, const GatherLaunch& G);
 
 int iq_register_tile(int ntmpl);  // register tile width used for `ntmpl` templates
+
+// Sum over [x0, x0+ex) x [y0, y0+ey) x [z0, z0+ez) of an integral image with a zero border
+// (row pitch sx, plane pitch sxy).
+__device__ __forceinline__ double iq_box_sum(const double* __restrict__ ii, int64_t sx, int64_t sxy,
+                                             int64_t x0, int64_t y0, int64_t z0, int64_t ex,
+                                             int64_t ey, int64_t ez) {
+  const int64_t x1 = x0 + ex, y1 = y0 + ey, z1 = z0 + ez;
+  double s = ii[x1 + sx * y1 + sxy * z1];
+  s -= ii[x0 + sx * y1 + sxy * z1];
+  s -= ii[x1 + sx * y0 + sxy * z1];
+  s += ii[x0 + sx * y0 + sxy * z1];
+  s -= ii[x1 + sx * y1 + sxy * z0];
+  s += ii[x0 + sx * y1 + sxy * z0];
+  s += ii[x1 + sx * y0 + sxy * z0];
+  s -= ii[x0 + sx * y0 + sxy * z0];
+  return s;
+}
+
+// ---- tensor-core correlation (iq_corr_tc.cu) ----
+constexpr int IQ_TC_MAXN = 256;   // columns (templates) per launch
+constexpr int IQ_TC_MAXBOX = 8;   // distinct masks per launch
+
+// A mask "tile minus the box [lo, hi)" (an empty box: the full tile).
+struct TcBox {
+  int32_t lo[3], hi[3];
+};
+
+// One column of the batched product: template n of a launch. Its values are read from
+// `grid + src + kx + gx * (ky + gy * kz)` inside mask `box` (src < 0: a padding column).
+struct TcCol {
+  int64_t src;
+  float* out;          // distance map of P floats
+  const double* b2;    // sum of squared template values over the mask (from the gather)
+  unsigned* mm;        // [min bits, max finite bits] (nullable)
+  int32_t box;         // index into the launch's boxes
+  int32_t pad_;
+};
+
+// Stage list of the union of some masks: one stage per (ky, kz) row and group of 24
+// x-offsets that any of the masks touches, word = ky | kz << 10 | g << 20 | stepmask << 26
+// (three 8-offset K-steps per group), prefix = K-steps before the stage.
+struct TcStages {
+  std::vector<uint32_t> word, prefix;
+  int64_t nsteps = 0;  // K-steps of all stages
+};
+void iq_tc_stages(Dim3 tile, const TcBox* boxes, int nbox, TcStages& out);
+
+struct TcCorrLaunch {
+  const float* img = nullptr; Dim3 img_dims{1, 1, 1};
+  Dim3 out_dims{1, 1, 1};
+  Dim3 tile{1, 1, 1};
+  const double* ii = nullptr;           // integral image of img^2 (required)
+  int nbox = 1;
+  TcBox box[IQ_TC_MAXBOX] = {};
+  const uint8_t* disabled = nullptr;
+  const uint32_t* stage_word = nullptr; // device copies of TcStages
+  const uint32_t* stage_prefix = nullptr;
+  int nstage = 0;
+  int64_t nsteps = 0;
+  const float* grid = nullptr; Dim3 grid_dims{1, 1, 1};  // template source
+  const TcCol* cols = nullptr;          // device array of N columns
+  int N = 0;                            // multiple of 16, at most 256
+  void* B = nullptr;                    // packed templates, nsteps * 64 * N bytes
+  bool exact = false;                   // img and templates are TF32 values: one MMA per step
+  double flops = 0;                     // algorithmic FLOPs (profiling)
+};
+int iq_launch_corr_tc(iq_ctx* ctx, const TcCorrLaunch& L);
+// true when every value of the device array is a TF32 value (low 13 mantissa bits zero)
+int iq_tf32_exact(iq_ctx* ctx, const float* d, int64_t n, bool& exact);
 
 // integral images and disabled windows
 int iq_build_integrals(iq_ctx* ctx, const float* d_img, Dim3 dims, double* d_sqii,

@@ -12,6 +12,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include <map>
 #include <cmath>
 #include <unordered_map>
 #include <vector>
@@ -392,6 +393,7 @@ extern "C" int iq_simulate(iq_ctx* ctx, const iq_sim_params* p, const iq_hard_da
     steps.push_back(s);
     pasted[ind] = 1;
   }
+  if (ctx->max_steps >= 0 && (int64_t)steps.size() > ctx->max_steps) steps.resize(ctx->max_steps);
   // Dependency levels: a step must follow every earlier step of the path whose tile region
   // overlaps its own (it reads what they paste and pastes over them). Steps of one level never
   // overlap, so each level runs as one batch with results identical to the path order.
@@ -436,6 +438,7 @@ extern "C" int iq_simulate(iq_ctx* ctx, const iq_sim_params* p, const iq_hard_da
           if (in) klist[(size_t)c * T + k++] = kpack(x, y, z);
         }
   }
+  const bool tc = ctx->corr_engine == 1;
   // hard lists of data tiles
   std::vector<int64_t> hoff(g.ntot + 1, 0);
   for (int64_t t = 0; t < g.ntot; ++t) hoff[t + 1] = hoff[t] + (int64_t)tile_hard[t].size();
@@ -515,6 +518,137 @@ extern "C" int iq_simulate(iq_ctx* ctx, const iq_sim_params* p, const iq_hard_da
   IQ_CUDA_OK(cudaMemcpyAsync(d_hk, hk.data(), sizeof(uint32_t) * hk.size(), cudaMemcpyHostToDevice, st));
   IQ_CUDA_OK(cudaMemcpyAsync(d_hkv, hkv.data(), sizeof(float) * hkv.size(), cudaMemcpyHostToDevice, st));
   IQ_CUDA_OK(cudaMemsetAsync(ctx->d_status, 0, sizeof(int), st));
+  // ---- tensor-core launches: union stage lists keyed by their set of masks ----
+  // Mask configuration c < ncfg is "tile minus [lo, hi)"; c == ncfg is the full tile.
+  auto cfg_box = [&](int c) {
+    TcBox b{};
+    if (c < ncfg)
+      for (int d = 0; d < 3; ++d) { b.lo[d] = (int32_t)cfgs[c].lo[d]; b.hi[d] = (int32_t)cfgs[c].hi[d]; }
+    return b;
+  };
+  struct TcStageRef { int64_t off; int nstage; int64_t nsteps; };
+  std::vector<uint32_t> tc_word, tc_pre;
+  std::map<std::vector<int>, TcStageRef> tc_stage_of;
+  auto stages_for = [&](const std::vector<int>& cfgset) -> TcStageRef {
+    auto it = tc_stage_of.find(cfgset);
+    if (it != tc_stage_of.end()) return it->second;
+    std::vector<TcBox> bx;
+    for (int c : cfgset) bx.push_back(cfg_box(c));
+    TcStages st;
+    iq_tc_stages(tileD, bx.data(), (int)bx.size(), st);
+    TcStageRef r{(int64_t)tc_word.size(), (int)st.word.size(), st.nsteps};
+    tc_word.insert(tc_word.end(), st.word.begin(), st.word.end());
+    tc_pre.insert(tc_pre.end(), st.prefix.begin(), st.prefix.end());
+    tc_stage_of[cfgset] = r;
+    return r;
+  };
+  struct TcRun {
+    int64_t chunk; size_t col0; int N; std::vector<int> cfgset; TcStageRef st; double flops;
+  };
+  std::vector<TcRun> tcruns;
+  std::vector<TcCol> tccols;
+  std::vector<int64_t> tcbeg(nchunk + 1, 0);
+  std::vector<uint8_t> chunk_tc(nchunk, 0);
+  // Chunks whose masks all have offsets run their overlap distances on the tensor cores:
+  // the (tile, realization) columns of the chunk, grouped by mask, in launches of at most
+  // 256 columns and 8 masks with balanced widths.
+  for (int64_t c = 0; c < nchunk && tc; ++c) {
+    bool ok = T > 0;
+    for (int64_t k = cbeg[c]; k < cbeg[c + 1] && ok; ++k) ok = cfgs[steps[k].cfg].K > 0;
+    chunk_tc[c] = ok;
+    if (ok) {
+      std::vector<std::pair<int, int64_t>> order;  // (cfg, step index in chunk) sorted by cfg
+      for (int64_t k = cbeg[c]; k < cbeg[c + 1]; ++k) order.push_back({steps[k].cfg, k - cbeg[c]});
+      std::stable_sort(order.begin(), order.end(),
+                       [](const std::pair<int, int64_t>& x, const std::pair<int, int64_t>& y) { return x.first < y.first; });
+      const int64_t ncols = (int64_t)order.size() * R;
+      const int64_t nl = (ncols + IQ_TC_MAXN - 1) / IQ_TC_MAXN;
+      const int64_t per = std::min<int64_t>(IQ_TC_MAXN, ((ncols + nl - 1) / nl + 15) / 16 * 16);
+      int64_t q = 0;
+      while (q < ncols) {
+        TcRun run;
+        run.chunk = c;
+        run.col0 = tccols.size();
+        int64_t cnt = 0;
+        double fl = 0;
+        while (q < ncols && cnt < per) {
+          const int cf = order[q / R].first;
+          int bid = -1;
+          for (size_t j = 0; j < run.cfgset.size(); ++j) if (run.cfgset[j] == cf) bid = (int)j;
+          if (bid < 0) {
+            if ((int)run.cfgset.size() == IQ_TC_MAXBOX) break;
+            run.cfgset.push_back(cf);
+            bid = (int)run.cfgset.size() - 1;
+          }
+          const int64_t i = order[q / R].second, r = q % R;
+          tccols.push_back(TcCol{r * padvol + steps[cbeg[c] + i].startlin,
+                                 d_D + ((size_t)i * R + r) * P, d_b2 + (size_t)i * rpad + r,
+                                 d_mm + (size_t)i * R * 2 + 2 * r, bid, 0});
+          fl += 2.0 * (double)P * (double)cfgs[cf].K;
+          ++cnt;
+          ++q;
+        }
+        for (; cnt % 16; ++cnt) tccols.push_back(TcCol{-1, nullptr, nullptr, nullptr, 0, 0});
+        run.N = (int)cnt;
+        run.st = stages_for(run.cfgset);
+        run.flops = fl;
+        tcruns.push_back(run);
+      }
+    }
+    tcbeg[c + 1] = (int64_t)tcruns.size();
+  }
+  const TcStageRef soft_st = (tc && nsoft > 0 && T > 0) ? stages_for(std::vector<int>{ncfg}) : TcStageRef{0, 0, 0};
+  // exactness: the simulation grid holds TI values and hard data only
+  bool sim_tf32 = ctx->ti_tf32;
+  for (int64_t i = 0; i < nh && sim_tf32; ++i) {
+    const float f = (float)hv[i];
+    uint32_t bits;
+    memcpy(&bits, &f, 4);
+    if (!std::isnan(f) && (bits & 0x1FFFu)) sim_tf32 = false;
+  }
+  uint32_t* d_tcst = nullptr;  // stage words of every list, then their prefixes
+  void* d_tcb = nullptr;        // packed templates of one launch
+  double* d_tcb2 = nullptr;     // squared sums of the soft templates of one launch
+  TcCol* d_tccols = nullptr;
+  if (tc && !tc_word.empty()) {
+    const size_t ns = tc_word.size();
+    std::vector<uint32_t> both(tc_word);
+    both.insert(both.end(), tc_pre.begin(), tc_pre.end());
+    int64_t bmax = 1;
+    for (const TcRun& u : tcruns) bmax = std::max<int64_t>(bmax, u.st.nsteps * 64 * u.N);
+    bmax = std::max<int64_t>(bmax, soft_st.nsteps * 64 * IQ_TC_MAXN);
+    d_tcst = (uint32_t*)iq_scratch(ctx, S_TCSTAGE, sizeof(uint32_t) * both.size());
+    d_tcb = iq_scratch(ctx, S_TCB, (size_t)bmax);
+    d_tcb2 = (double*)iq_scratch(ctx, S_TCB2, sizeof(double) * IQ_TC_MAXN);
+    if (!d_tcst || !d_tcb || !d_tcb2) return IQ_ERR_ALLOC;
+    IQ_CUDA_OK(cudaMemcpyAsync(d_tcst, both.data(), sizeof(uint32_t) * both.size(),
+                               cudaMemcpyHostToDevice, st));
+    IQ_CUDA_OK(cudaStreamSynchronize(st));  // `both` is a host vector
+    (void)ns;
+    if (!tccols.empty()) {
+      d_tccols = (TcCol*)iq_scratch(ctx, S_TCCOLS, sizeof(TcCol) * tccols.size());
+      if (!d_tccols) return IQ_ERR_ALLOC;
+      IQ_CUDA_OK(cudaMemcpyAsync(d_tccols, tccols.data(), sizeof(TcCol) * tccols.size(),
+                                 cudaMemcpyHostToDevice, st));
+    }
+  }
+  // one tensor-core launch over the columns cols[0..N) with the masks of `cfgset`
+  auto tc_launch = [&](const std::vector<int>& cfgset, const TcStageRef& sr, const float* img,
+                       const double* ii, const float* grid, Dim3 gdims, const TcCol* cols, int N,
+                       bool exact, double flops) -> int {
+    TcCorrLaunch L;
+    L.img = img; L.img_dims = ctx->ti; L.out_dims = distD; L.tile = tileD; L.ii = ii;
+    L.nbox = (int)cfgset.size();
+    for (int b = 0; b < L.nbox; ++b) L.box[b] = cfg_box(cfgset[b]);
+    L.disabled = d_dis;
+    L.stage_word = d_tcst + sr.off;
+    L.stage_prefix = d_tcst + tc_word.size() + sr.off;
+    L.nstage = sr.nstage;
+    L.nsteps = sr.nsteps;
+    L.grid = grid; L.grid_dims = gdims; L.cols = cols; L.N = N; L.B = d_tcb;
+    L.exact = exact; L.flops = flops;
+    return iq_launch_corr_tc(ctx, L);
+  };
 
   // ---- soft data: padded aux grids, auxTI integral images, per-tile distance maps ----
   std::vector<float*> d_aux(nsoft), d_auxti(nsoft);
@@ -566,21 +700,61 @@ extern "C" int iq_simulate(iq_ctx* ctx, const iq_sim_params* p, const iq_hard_da
       }
       IQ_CUDA_OK(cudaMemcpyAsync(d_starts, starts.data(), sizeof(int64_t) * starts.size(),
                                  cudaMemcpyHostToDevice, st));
-      // per-tile soft distance maps, 16 tiles per launch
-      for (size_t b0 = 0; b0 < tl.size(); b0 += 16) {
-        const int nb = (int)std::min<size_t>(16, tl.size() - b0);
-        const int64_t slot0 = (int64_t)s * nslot + slot_of[tl[b0]];
-        GatherLaunch G;
-        G.grid = d_aux[s]; G.grid_dims = psz; G.grid_stride = 0; G.starts = d_starts + b0;
-        G.ntmpl = nb; G.rpad = 16;
-        G.t0 = GatherTask{d_kl + (size_t)ncfg * T, (int)T, 0, nullptr, d_tv, d_b2, d_softmm + 2 * slot0};
-        RET_IF(iq_launch_gather(ctx, G));
-        CorrLaunch C;
-        C.img = d_auxti[s]; C.img_dims = ctx->ti; C.out_dims = distD; C.tile = tileD;
-        C.rpad = 16; C.ntmpl = nb; C.out_stride = P; C.disabled = d_dis;
-        C.t0 = CorrTask{d_kl + (size_t)ncfg * T, (int)T, d_tv, d_b2, d_auxii[s], {0, 0, 0}, {0, 0, 0},
-                        d_soft + slot0 * P, d_softmm + 2 * slot0};
-        RET_IF(iq_launch_corr(ctx, C));
+      if (tc && T > 0) {
+        // per-tile soft distance maps on the tensor cores, up to 256 tiles per launch
+        std::vector<TcCol> cols;
+        std::vector<std::pair<size_t, int>> launches;  // (first column, N)
+        for (size_t b0 = 0; b0 < tl.size(); b0 += IQ_TC_MAXN) {
+          const int nb = (int)std::min<size_t>(IQ_TC_MAXN, tl.size() - b0);
+          launches.push_back({cols.size(), (nb + 15) / 16 * 16});
+          for (int i = 0; i < launches.back().second; ++i) {
+            if (i < nb) {
+              const int64_t slot = (int64_t)s * nslot + slot_of[tl[b0 + i]];
+              cols.push_back(TcCol{starts[b0 + i], d_soft + slot * P, d_tcb2 + i, d_softmm + 2 * slot, 0, 0});
+            } else {
+              cols.push_back(TcCol{-1, nullptr, nullptr, nullptr, 0, 0});
+            }
+          }
+        }
+        bool exact = false, ea = false;
+        RET_IF(iq_tf32_exact(ctx, d_aux[s], psz.vol(), ea));
+        if (ea) RET_IF(iq_tf32_exact(ctx, d_auxti[s], tivol, exact));
+        TcCol* d_cols = (TcCol*)iq_scratch(ctx, S_TCSOFT, sizeof(TcCol) * cols.size());
+        if (!d_cols) return IQ_ERR_ALLOC;
+        IQ_CUDA_OK(cudaMemcpyAsync(d_cols, cols.data(), sizeof(TcCol) * cols.size(),
+                                   cudaMemcpyHostToDevice, st));
+        for (size_t l = 0; l < launches.size(); ++l) {
+          const size_t b0 = l * IQ_TC_MAXN;
+          const int nb = (int)std::min<size_t>(IQ_TC_MAXN, tl.size() - b0);
+          const int64_t slot0 = (int64_t)s * nslot + slot_of[tl[b0]];
+          GatherLaunch G;
+          G.grid = d_aux[s]; G.grid_dims = psz; G.grid_stride = 0; G.starts = d_starts + b0;
+          G.ntmpl = nb; G.rpad = nb;
+          G.t0 = GatherTask{d_kl + (size_t)ncfg * T, (int)T, 0, nullptr, nullptr, d_tcb2,
+                            d_softmm + 2 * slot0};
+          RET_IF(iq_launch_gather(ctx, G));
+          RET_IF(tc_launch(std::vector<int>{ncfg}, soft_st, d_auxti[s], d_auxii[s], d_aux[s], psz,
+                           d_cols + launches[l].first, launches[l].second, exact,
+                           2.0 * (double)P * (double)T * nb));
+        }
+        IQ_CUDA_OK(cudaStreamSynchronize(st));  // `cols` is a host vector
+      } else {
+        // per-tile soft distance maps, 16 tiles per launch
+        for (size_t b0 = 0; b0 < tl.size(); b0 += 16) {
+          const int nb = (int)std::min<size_t>(16, tl.size() - b0);
+          const int64_t slot0 = (int64_t)s * nslot + slot_of[tl[b0]];
+          GatherLaunch G;
+          G.grid = d_aux[s]; G.grid_dims = psz; G.grid_stride = 0; G.starts = d_starts + b0;
+          G.ntmpl = nb; G.rpad = 16;
+          G.t0 = GatherTask{d_kl + (size_t)ncfg * T, (int)T, 0, nullptr, d_tv, d_b2, d_softmm + 2 * slot0};
+          RET_IF(iq_launch_gather(ctx, G));
+          CorrLaunch C;
+          C.img = d_auxti[s]; C.img_dims = ctx->ti; C.out_dims = distD; C.tile = tileD;
+          C.rpad = 16; C.ntmpl = nb; C.out_stride = P; C.disabled = d_dis;
+          C.t0 = CorrTask{d_kl + (size_t)ncfg * T, (int)T, d_tv, d_b2, d_auxii[s], {0, 0, 0}, {0, 0, 0},
+                          d_soft + slot0 * P, d_softmm + 2 * slot0};
+          RET_IF(iq_launch_corr(ctx, C));
+        }
       }
       IQ_CUDA_OK(cudaStreamSynchronize(st));  // `starts` is a host vector
     }
@@ -643,6 +817,9 @@ extern "C" int iq_simulate(iq_ctx* ctx, const iq_sim_params* p, const iq_hard_da
     }
     hbeg[c + 1] = hbeg[c] + hi;
   }
+  for (int64_t c = 0; c < nchunk; ++c)
+    if (chunk_tc[c])
+      for (int64_t k = cbeg[c]; k < cbeg[c + 1]; ++k) gt[k].tv = nullptr;  // only B2 and min/max
   const size_t tbytes = sizeof(GatherTask) * (nsteps + hgt.size()) + sizeof(CorrTask) * (nsteps + hct.size()) +
                         sizeof(PickTask) * nsteps + sizeof(StepTask) * nsteps + 6 * 256;
   char* d_tasks = (char*)iq_scratch(ctx, S_TASKS, tbytes);
@@ -675,11 +852,19 @@ extern "C" int iq_simulate(iq_ctx* ctx, const iq_sim_params* p, const iq_hard_da
     G.grid = d_sim; G.grid_dims = padD; G.grid_stride = padvol; G.ntmpl = R; G.rpad = rpad;
     G.ntask = m; G.tasks = d_gt + k0;
     RET_IF(iq_launch_gather(ctx, G));
-    CorrLaunch C;
-    C.img = ctx->d_ti; C.img_dims = ctx->ti; C.out_dims = distD; C.tile = tileD;
-    C.rpad = rpad; C.ntmpl = R; C.out_stride = P; C.disabled = d_dis;
-    C.ntask = m; C.tasks = d_ct + k0; C.flops = cflops[c];
-    RET_IF(iq_launch_corr(ctx, C));
+    if (chunk_tc[c]) {
+      for (int64_t l = tcbeg[c]; l < tcbeg[c + 1]; ++l) {
+        const TcRun& u = tcruns[l];
+        RET_IF(tc_launch(u.cfgset, u.st, ctx->d_ti, ctx->d_ti2ii, d_sim, padD, d_tccols + u.col0, u.N,
+                         sim_tf32, u.flops));
+      }
+    } else {
+      CorrLaunch C;
+      C.img = ctx->d_ti; C.img_dims = ctx->ti; C.out_dims = distD; C.tile = tileD;
+      C.rpad = rpad; C.ntmpl = R; C.out_stride = P; C.disabled = d_dis;
+      C.ntask = m; C.tasks = d_ct + k0; C.flops = cflops[c];
+      RET_IF(iq_launch_corr(ctx, C));
+    }
     // hard distance of the data tiles of the chunk
     const int nh_c = (int)(hbeg[c + 1] - hbeg[c]);
     if (nh_c > 0) {

@@ -32,6 +32,7 @@ extern "C" {
 #define IQ_ERR_CUTCAP 5    /* graph cut hit its round limit */
 #define IQ_ERR_STATE 6     /* no training image set on the context */
 #define IQ_ERR_LIMIT 7     /* size beyond a stated maximum */
+#define IQ_ERR_TIMEOUT 8   /* a device-side wait ran past its time limit (the kernel returned) */
 
 #define IQ_F32 0
 #define IQ_F64 1
@@ -179,6 +180,10 @@ int64_t iq_ctx_launches(iq_ctx* ctx);
  *                         3 (2 positions)
  *   "sim.level_chunk"     most tiles of one dependency level simulated together (default 64;
  *                         1 processes the tile path one tile at a time)
+ *   "sim.max_steps"       simulate only the first n tiles of the path (< 0: all; default -1);
+ *                         for bounded samples and for locating the first differing tile
+ *   "corr.engine"         1: distance maps of "tile minus box" masks on the tensor cores
+ *                         (tcgen05, TF32 split in two halves; default), 0: SIMT FP32 kernel
  * Returns IQ_ERR_ARG for an unknown name or an out-of-range value.
  */
 int iq_set_option(iq_ctx* ctx, const char* name, int64_t value);

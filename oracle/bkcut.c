@@ -21,12 +21,16 @@
  * gradients and their sums are in the element type (float or double); the final sum with
  * eps() = 2^-52 and the division are in double (Julia promotes Float32 + Float64).
  *
- * Residual capacities are stored per directed lattice arc (r_fwd, r_bwd per edge). An arc is
- * open (residual) when r > thr(max(r_fwd, r_bwd)), thr(m) = m * 2^-30 (for m >= 2^-992,
- * else 0): flow left on an arc by rounding below 2^-30 of its capacity counts as saturated.
- * The GPU cut uses the same predicate; with it the sink tree at termination is the set of
- * nodes that can reach t in the residual graph, which is the same for every maximum flow.
- */
+ * Exact arithmetic. Where a gradient sum is zero the denominator is eps() and the capacity
+ * is ~2^52 times larger than its neighbours', so a Float64 max-flow cannot resolve the small
+ * arcs and different flow orders (BK here, push-relabel on the GPU, the Julia BK) stop at
+ * different minimum cuts. Every capacity is therefore rounded to a multiple of
+ * q = 2^(ilogb(cmax) - 47), cmax the largest capacity of the slab (round half to even). All
+ * residuals (<= 2 cmax) and node excesses (<= 12 cmax) are then multiples of q below 2^53 q,
+ * every push or augmentation is exact, an arc is open exactly when its residual is > 0, and
+ * the set of nodes that can reach t is the same for every maximum flow (and preflow): BK's
+ * sink tree at termination and the GPU's final breadth-first search both return it.
+  */
 #include <math.h>
 #include <stdint.h>
 #include <stdlib.h>
@@ -44,13 +48,14 @@ typedef struct {
 static inline uint64_t dbits(double x) { uint64_t u; memcpy(&u, &x, 8); return u; }
 static inline double bitsd(uint64_t u) { double x; memcpy(&x, &u, 8); return x; }
 
-/* Saturation threshold of an edge: max(r_fwd, r_bwd) * 2^-30, computed on the bits. */
-static inline double edge_thr(const edge_t *e) {
-    double m = e->r_ab > e->r_ba ? e->r_ab : e->r_ba;
-    uint64_t b = dbits(m);
-    uint64_t ex = b >> 52;
-    if (ex <= 30) return 0.0;
-    return bitsd(b - ((uint64_t)30 << 52));
+/* Round every capacity to a multiple of q = 2^(ilogb(cmax) - 47) (see the header). */
+static void quantize_caps(double *c, long long n, long long stride) {
+    double cmax = 0.0;
+    for (long long i = 0; i < n; i++) if (c[i * stride] > cmax) cmax = c[i * stride];
+    if (!(cmax > 0.0)) return;
+    int sh = ilogb(cmax) - 47;
+    if (sh < -1074) sh = -1074;
+    for (long long i = 0; i < n; i++) c[i * stride] = ldexp(rint(ldexp(c[i * stride], -sh)), sh);
 }
 
 /* graph with explicit terminals s = nvox, t = nvox + 1 */
@@ -66,9 +71,8 @@ typedef struct {
 } graph_t;
 
 /* residual capacity of arc p->q given an incidence entry of p */
-static inline double arc_res(const graph_t *g, int ent, int *q, double *thr) {
+static inline double arc_res(const graph_t *g, int ent, int *q) {
     const edge_t *e = &g->edges[ent >> 1];
-    *thr = edge_thr(e);
     if ((ent & 1) == 0) { *q = e->b; return e->r_ab; }
     *q = e->a; return e->r_ba;
 }
@@ -100,16 +104,13 @@ static void apush(bk_t *k, int v) {
 
 /* residual of the arc from x to y where y is a neighbour reached through x's entry ent */
 static inline int lattice_open(const graph_t *g, int ent_of_x, int *y) {
-    double thr;
-    double r = arc_res(g, ent_of_x, y, &thr);
-    return r > thr;
+    return arc_res(g, ent_of_x, y) > 0.0;
 }
 /* residual of the reverse arc (y -> x) for x's entry ent */
 static inline int lattice_open_rev(const graph_t *g, int ent_of_x) {
     const edge_t *e = &g->edges[ent_of_x >> 1];
-    double thr = edge_thr(e);
     double r = (ent_of_x & 1) == 0 ? e->r_ba : e->r_ab;
-    return r > thr;
+    return r > 0.0;
 }
 
 /* does node v trace back to its terminal through valid parent links? */
@@ -197,7 +198,7 @@ static int run_bk(graph_t *g, bk_t *k, long long max_aug) {
             else {
                 r = -1;
                 for (int j = g->inc_start[a]; j < g->inc_start[a + 1]; j++) {
-                    int q; double thr; double rr = arc_res(g, g->inc[j], &q, &thr);
+                    int q; double rr = arc_res(g, g->inc[j], &q);
                     if (q == b) { r = rr; break; }
                 }
             }
@@ -350,6 +351,13 @@ int oracle_graphcut(const void *A, const void *B, int elem, int nd, const long l
                     deg[u]++; deg[v]++;
                 }
     }
+    {
+        double *caps = (double *)malloc(sizeof(double) * (g.nedges + 1));
+        for (int i = 0; i < g.nedges; i++) caps[i] = g.edges[i].r_ab;
+        quantize_caps(caps, g.nedges, 1);
+        for (int i = 0; i < g.nedges; i++) { g.edges[i].r_ab = caps[i]; g.edges[i].r_ba = caps[i]; }
+        free(caps);
+    }
     g.inc_start = (int *)malloc(sizeof(int) * (g.n + 1));
     g.inc_start[0] = 0;
     for (int i = 0; i < g.n; i++) g.inc_start[i + 1] = g.inc_start[i] + deg[i];
@@ -409,7 +417,7 @@ int oracle_graphcut(const void *A, const void *B, int elem, int nd, const long l
     return rc;
 }
 
-/* Capacities only (for tests): writes one value per lattice edge in creation order
+/* Capacities only (for tests): writes one quantized value per lattice edge in creation order
  * (dims 0,1,2; within a dim, column-major over the lower node). Returns the edge count. */
 long long oracle_capacities(const void *A, const void *B, int elem, int nd, const long long *sz,
                             double *out) {
@@ -451,5 +459,6 @@ long long oracle_capacities(const void *A, const void *B, int elem, int nd, cons
                     n++;
                 }
     }
+    if (out) quantize_caps(out, n, 1);
     return n;
 }
