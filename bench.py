@@ -339,12 +339,19 @@ def run_ours(args, W, dist, rank, world):
     ms = e0.elapsed_time(e1)
     clk = clocks.stop()
     prof = {k: ctx.profile_get(k) for k in ("corr", "pick", "graphcut", "paste")}
+    mma = ctx.profile_get("corr.mma")
     counters = {k: ctx.profile_get(k) for k in ("graphcut.rounds", "graphcut.levels",
                                                  "pick.iterations", "pick.candidates")}
     counters = {k: {"mean": (v[2] / v[1]) if v[1] else None, "ctas": v[1]}
                 for k, v in counters.items()}
     for k in ("graphcut.max_rounds", "graphcut.max_levels"):
         counters[k] = ctx.profile_get(k)[2]
+    # tensor-core correlation: mean SM cycles per CTA in each phase
+    tc = {k: ctx.profile_get("corr." + k) for k in ("loop", "wait_full", "wait_afull",
+                                                    "wait_done", "producer_wait",
+                                                    "producer_loop", "epilogue", "issue",
+                                                    "mma_units")}
+    counters["corr_cycles_per_cta"] = {k: (v[2] / v[1]) if v[1] else None for k, v in tc.items()}
     ctx.profile(False)
     ms_max = reduce_max(dist, ms)
     barrier(dist)
@@ -385,12 +392,15 @@ def run_ours(args, W, dist, rank, world):
             "peak_kind": "%s (bf16 dense, burst)" % peak_kind,
             "flops_per_launch": corr_flops / corr_n if corr_n else None,
             "traffic": profile_traffic("corr", W["name"]),
-            "fp32_simt_peak_tflops_nominal": 2 * 152 * 128 * 2.07e9 / 1e12,
-            "note": "the correlation runs on the FP32 SIMT pipes in this version; frac is "
-                    "against the dense bf16 tensor peak"}
+            "mma_tflops_issued": (mma[2] / (corr_ms / 1e3) / 1e12) if corr_ms and mma[2] else None,
+            "note": "achieved = algorithmic FLOPs (2 x positions x mask offsets x templates) "
+                    "over the correlation's time; the tensor pipe issues TF32 MMAs (three per "
+                    "K-step for FP32 data: hi*hi + hi*lo + lo*hi) over padded positions and "
+                    "offsets, counted in mma_tflops_issued; TF32 runs at half the bf16 rate"}
     if roof["achieved"] is not None and roof["peak"]:
         roof["frac"] = roof["achieved"] / roof["peak"]
-        roof["frac_of_fp32_simt_nominal"] = roof["achieved"] / roof["fp32_simt_peak_tflops_nominal"]
+        if roof["mma_tflops_issued"]:
+            roof["mma_frac_of_tf32_peak"] = roof["mma_tflops_issued"] / (roof["peak"] / 2)
     kernel_share = {k: {"ms": round(v[0], 3), "launches": v[1],
                         "share_of_step": round(v[0] / ms, 4) if ms else None}
                     for k, v in prof.items()}
@@ -408,11 +418,12 @@ def run_ours(args, W, dist, rank, world):
                        "options": args.option,
                        "voxels_per_step": voxels * world, "parallelism": "replicas x%d" % world,
                        "l2": "working set > L2 (simulation grids 350 MB, soft maps 1.6 GB)",
-                       "form": "plain (FP32 direct correlation)"},
+                       "form": "plain (FP32 correlation as TF32x3 on the tensor cores)"},
             "roofline": roof, "dominant_kernel": dom, "kernels": kernel_share,
             "counters": counters,
             "cpu_baseline": cpu,
-            "e2e": {"value": e2e_value, "unit": "voxels/s", "h2d_bytes_per_step": int(h2d),
+            "e2e": None if args.no_e2e else
+                   {"value": e2e_value, "unit": "voxels/s", "h2d_bytes_per_step": int(h2d),
                     "d2h_bytes_per_step": int(d2h), "ms_per_step": ms_e2e_max / args.steps},
             "clocks": clk, "gpu_launches": int(launches)}
     print(json.dumps(line), flush=True)

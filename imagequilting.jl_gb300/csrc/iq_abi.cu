@@ -75,6 +75,8 @@ extern "C" int iq_profile(iq_ctx* ctx, int32_t enable) {
   if (!ctx) return iq_set_error(IQ_ERR_ARG, "null context");
   cudaStreamSynchronize(ctx->stream);
   for (auto& kv : ctx->timers) { kv.second.used = 0; kv.second.work = 0; }
+  ctx->prof_mma_flops = 0;
+  ctx->prof_mma_launches = 0;
   cudaMemsetAsync(ctx->d_stats, 0, sizeof(unsigned long long) * ST_COUNT, ctx->stream);
   ctx->prof = enable != 0;
   return IQ_OK;
@@ -89,13 +91,30 @@ extern "C" int iq_profile_get(iq_ctx* ctx, const char* kernel, double* ms_total,
   double ms = 0, wk = 0;
   int64_t n = 0;
   // counters: "graphcut.rounds", "graphcut.levels" (work = total, launches = CTAs),
-  // "pick.iterations", "pick.candidates" (work = total, launches = CTAs)
-  const char* names[6] = {"graphcut.rounds", "graphcut.levels", "pick.iterations",
-                          "pick.candidates", "graphcut.max_rounds", "graphcut.max_levels"};
-  const int idx[6][2] = {{ST_CUT_ROUNDS, ST_CUT_CTAS}, {ST_CUT_LEVELS, ST_CUT_CTAS},
-                         {ST_PICK_ITERS, ST_PICK_CTAS}, {ST_PICK_CAND, ST_PICK_CTAS},
-                         {ST_CUT_MAXROUNDS, ST_CUT_CTAS}, {ST_CUT_MAXLEVELS, ST_CUT_CTAS}};
-  for (int i = 0; i < 6; ++i)
+  // "pick.iterations", "pick.candidates" (work = total, launches = CTAs), "corr.mma" (work =
+  // tensor-pipe FLOPs issued, with the TF32 split and the padded positions and offsets)
+  if (!strcmp(kernel, "corr.mma")) {
+    if (ms_total) *ms_total = 0;
+    if (launches) *launches = ctx->prof_mma_launches;
+    if (work) *work = ctx->prof_mma_flops;
+    return IQ_OK;
+  }
+  // "corr.loop", "corr.wait_full", "corr.wait_afull", "corr.wait_done", "corr.producer_wait",
+  // "corr.producer_loop", "corr.epilogue" (work = SM cycles summed over CTAs, launches = CTAs)
+  const char* names[15] = {"graphcut.rounds", "graphcut.levels", "pick.iterations",
+                           "pick.candidates", "graphcut.max_rounds", "graphcut.max_levels",
+                           "corr.loop", "corr.wait_full", "corr.wait_afull", "corr.wait_done",
+                           "corr.producer_wait", "corr.producer_loop", "corr.epilogue",
+                           "corr.issue", "corr.mma_units"};
+  const int idx[15][2] = {{ST_CUT_ROUNDS, ST_CUT_CTAS}, {ST_CUT_LEVELS, ST_CUT_CTAS},
+                          {ST_PICK_ITERS, ST_PICK_CTAS}, {ST_PICK_CAND, ST_PICK_CTAS},
+                          {ST_CUT_MAXROUNDS, ST_CUT_CTAS}, {ST_CUT_MAXLEVELS, ST_CUT_CTAS},
+                          {ST_TC_LOOP, ST_TC_CTAS}, {ST_TC_WFULL, ST_TC_CTAS},
+                          {ST_TC_WAFULL, ST_TC_CTAS}, {ST_TC_WDONE, ST_TC_CTAS},
+                          {ST_TC_PWAIT, ST_TC_CTAS}, {ST_TC_PLOOP, ST_TC_CTAS},
+                          {ST_TC_EPI, ST_TC_CTAS}, {ST_TC_ISSUE, ST_TC_CTAS},
+                          {ST_TC_MMAU, ST_TC_CTAS}};
+  for (int i = 0; i < 15; ++i)
     if (!strcmp(kernel, names[i])) {
       unsigned long long h[ST_COUNT];
       IQ_CUDA_OK(cudaMemcpy(h, ctx->d_stats, sizeof(h), cudaMemcpyDeviceToHost));

@@ -28,13 +28,20 @@
 // K-step gives the same sums. The epilogue computes |(A2 + B2) - 2 AB| in FP32, exact for
 // integer data below 2^24 like the rest of the product.
 //
-// Pipeline. 256 threads, 3 shared-memory stages. Per stage all threads wait for the MMAs
-// that last read the buffer (tcgen05.commit -> mbarrier), thread 0 starts the bulk copy of B,
-// all threads write the A images from registers, and after a barrier thread 0 waits for the
-// copy and issues the stage's MMAs while the other threads load the next stage's TI values.
-// Each CTA owns 2 x 128 positions (two accumulators of N columns in TMEM). Every mbarrier
-// wait is bounded in time: on expiry the kernel records IQ_ERR_TIMEOUT, stops issuing work,
-// waits (bounded) for what it issued, frees its TMEM and returns.
+// Pipeline. 256 threads, 3 shared-memory stages, no CTA-wide barrier in the main loop:
+//   * warp 0, one lane: waits for a stage's B (mbarrier with transaction count) and A
+//     (mbarrier, one arrival per producer warp), issues its MMAs and commits them to the
+//     stage's "done" mbarrier -- nothing else, since the rate at which this one thread issues
+//     is what keeps the tensor pipe busy (a bulk-copy issue can stall it for hundreds of
+//     cycles);
+//   * warps 1-7: wait until the MMAs that last read a buffer are done; lane 0 of warp 1 starts
+//     the bulk copy of the stage's B into it; all write the stage's A images from registers,
+//     arrive, and load the TI values of the stage after next (two register sets, so the L2
+//     latency of a load has two stages to pass).
+// Each CTA owns 2 x 128 positions (two accumulators of N columns in TMEM); all 8 warps run
+// the epilogue. Every mbarrier wait is bounded in time: on expiry the kernel records
+// IQ_ERR_TIMEOUT, stops issuing work, waits (bounded) for what it issued, frees its TMEM and
+// returns.
 #include <float.h>
 
 #include <algorithm>
@@ -44,13 +51,16 @@
 namespace {
 
 constexpr int TC_THREADS = 256;
+constexpr int TC_PWARPS = 7;                   // producer warps (1..7)
+constexpr int TC_PTHREADS = 32 * TC_PWARPS;
 constexpr int TC_MB = 2;     // 128-position blocks per CTA
 constexpr int TC_NST = 3;    // pipeline stages
 constexpr int TC_STEPS = 3;  // 8-offset K-steps per stage (24 x-offsets)
 constexpr int TC_NQ = 32 * TC_MB + 2 * (TC_STEPS - 1);  // 128-byte blocks of one image
-constexpr int TC_UPT = (8 * TC_NQ + TC_THREADS - 1) / TC_THREADS;  // image rows per thread
+constexpr int TC_UPT = (8 * TC_NQ + TC_PTHREADS - 1) / TC_PTHREADS;  // image rows per thread
 constexpr int TC_GROUP = 8 * TC_STEPS;                  // x-offsets per stage
 constexpr unsigned long long TC_WAIT_NS = 2000000000ull; // bound of every wait
+constexpr int TC_SMW = 1024;  // stage words and prefixes kept in shared memory
 
 struct TcArgs {
   const float* img;
@@ -71,6 +81,7 @@ struct TcArgs {
   int exact;
   uint32_t tmem_cols;
   int* status;
+  unsigned long long* stats;  // profiling counters (nullable)
 };
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
@@ -91,6 +102,10 @@ __device__ __forceinline__ uint64_t make_desc(uint32_t saddr, uint32_t lbo, uint
   d |= (uint64_t)((sbo >> 4) & 0x3FFFu) << 32;
   d |= (uint64_t)1 << 46;
   return d;
+}
+
+__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
 }
 
 __device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
@@ -116,6 +131,16 @@ __device__ bool mbar_wait(uint32_t bar, uint32_t parity) {
     if (mbar_test(bar, parity)) return true;
     if ((it & 63u) == 0 && globaltimer() - t0 > TC_WAIT_NS) return false;
   }
+}
+
+// mbar_wait that adds the cycles it spent to *acc when profiling
+__device__ __forceinline__ bool mbar_wait_t(uint32_t bar, uint32_t parity, bool prof,
+                                            long long& acc) {
+  if (!prof) return mbar_wait(bar, parity);
+  const long long t = clock64();
+  const bool ok = mbar_wait(bar, parity);
+  acc += clock64() - t;
+  return ok;
 }
 
 __device__ __forceinline__ void bulk_g2s(uint32_t dst, const void* src, uint32_t bytes,
@@ -238,10 +263,19 @@ struct StageInfo {
   uint32_t pre;
 };
 
-__device__ __forceinline__ StageInfo stage_info(const TcArgs& a, int e, int64_t p0) {
+// stage e's word and prefix: from the shared-memory copy (first TC_SMW stages) or global
+__device__ __forceinline__ uint32_t stage_word(const TcArgs& a, const uint32_t* sw, int e) {
+  return e < TC_SMW ? sw[e] : __ldg(a.word + e);
+}
+__device__ __forceinline__ uint32_t stage_pre(const TcArgs& a, const uint32_t* sw, int e) {
+  return e < TC_SMW ? sw[TC_SMW + e] : __ldg(a.prefix + e);
+}
+
+__device__ __forceinline__ StageInfo stage_info(const TcArgs& a, const uint32_t* sw, int e,
+                                                int64_t p0) {
   StageInfo s;
-  const uint32_t w = __ldg(a.word + e);
-  s.pre = __ldg(a.prefix + e);
+  const uint32_t w = stage_word(a, sw, e);
+  s.pre = stage_pre(a, sw, e);
   const int ky = (int)(w & 1023u), kz = (int)((w >> 10) & 1023u), g = (int)((w >> 20) & 63u);
   s.smask = w >> 26;
   const int smax = 31 - __clz((int)s.smask);
@@ -250,11 +284,11 @@ __device__ __forceinline__ StageInfo stage_info(const TcArgs& a, int e, int64_t 
   return s;
 }
 
-__device__ __forceinline__ void stage_load(const TcArgs& a, const StageInfo& s, int tid,
+__device__ __forceinline__ void stage_load(const TcArgs& a, const StageInfo& s, int ptid,
                                            float (&v)[TC_UPT][4]) {
 #pragma unroll
   for (int i = 0; i < TC_UPT; ++i) {
-    const int u = tid + i * TC_THREADS;
+    const int u = ptid + i * TC_PTHREADS;
     if (u < s.nunits) {
       const int64_t base = s.e0 + 4 * (u >> 3) + (u & 7);
 #pragma unroll
@@ -278,8 +312,10 @@ __global__ void __launch_bounds__(TC_THREADS, 1) corr_tc_kernel(const TcArgs a) 
   int* s_box = reinterpret_cast<int*>(colbase + 28 * N);
   float* s_a2 = reinterpret_cast<float*>(colbase + 32 * N);  // [box][128 * TC_MB positions]
   uint64_t* bars = reinterpret_cast<uint64_t*>(s_a2 + IQ_TC_MAXBOX * 128 * TC_MB);
+  uint32_t* s_stage = reinterpret_cast<uint32_t*>(bars + 3 * TC_NST + 1);  // words, prefixes
+  // full[NST] (B copies), done[NST] (MMA commits), afull[NST] (A images), fin
   const uint32_t bar_full = smem_u32(bars), bar_done = bar_full + 8 * TC_NST,
-                 bar_fin = bar_full + 16 * TC_NST;
+                 bar_afull = bar_full + 16 * TC_NST, bar_fin = bar_full + 24 * TC_NST;
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   for (int n = tid; n < N; n += TC_THREADS) {
@@ -292,8 +328,14 @@ __global__ void __launch_bounds__(TC_THREADS, 1) corr_tc_kernel(const TcArgs a) 
     s_mn[n] = 0x7F800000u;
     s_mx[n] = 0u;
   }
+  for (int e = tid; e < a.nstage && e < TC_SMW; e += TC_THREADS) {
+    s_stage[e] = __ldg(a.word + e);
+    s_stage[TC_SMW + e] = __ldg(a.prefix + e);
+  }
   if (tid == 0) {
-    for (int i = 0; i < 2 * TC_NST + 1; ++i) mbar_init(bar_full + 8 * i, 1);
+    for (int i = 0; i < 2 * TC_NST; ++i) mbar_init(bar_full + 8 * i, 1);
+    for (int i = 0; i < TC_NST; ++i) mbar_init(bar_afull + 8 * i, TC_PWARPS);
+    mbar_init(bar_fin, 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   if (warp == 0) {
@@ -314,32 +356,111 @@ __global__ void __launch_bounds__(TC_THREADS, 1) corr_tc_kernel(const TcArgs a) 
   const uint32_t idesc = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(N >> 3) << 17) |
                          ((128u >> 4) << 24);
 
-  int fail = 0;     // this thread saw a wait expire
-  int pend_b = -1;  // thread 0: stage buffer with a bulk copy not yet waited for
-  uint32_t pend_par = 0;
+  int fail = 0;  // this thread saw a wait expire
   int aborted = 0;
-  float v[TC_UPT][4];
-  StageInfo si = stage_info(a, 0, p0);
-  stage_load(a, si, tid, v);
-  for (int e = 0; e < a.nstage; ++e) {
-    const int b = e % TC_NST;
-    const uint32_t use = (uint32_t)(e / TC_NST);
-    const uint32_t smask = si.smask;
-    const int nact = __popc(smask);
-    const uint32_t sb = sbase + b * stage_bytes;
-    const uint32_t sa_hi = sb + bbytes, sa_lo = sa_hi + TC_NQ * 128u;
-    // the MMAs that last read this buffer are done
-    if (use > 0 && !fail && !mbar_wait(bar_done + 8 * b, (use - 1) & 1u)) fail = 1;
-    if (tid == 0 && !fail) {
-      const uint32_t bytes = (uint32_t)nact * (a.exact ? 32u : 64u) * (uint32_t)N;
-      bulk_g2s(sb, a.B + (size_t)si.pre * 64 * N, bytes, bar_full + 8 * b);
-      pend_b = b;
-      pend_par = use & 1u;
+  if (warp == 0) {
+    if (lane == 0) {
+      // ---- copies and MMAs ----
+      // The issue rate of one thread bounds the tensor pipe, so the loop is lean: descriptors
+      // of buffer 0 are built once (a buffer or K-step is an offset added to the start field),
+      // the K-step and M-block loops are unrolled and the stage words sit in shared memory.
+      const uint64_t dA0 = make_desc(sbase + bbytes, 128u, 256u);
+      const uint64_t dL0 = make_desc(sbase + bbytes + TC_NQ * 128u, 128u, 256u);
+      const uint64_t dB0 = make_desc(sbase, 16u * N, 128u);
+      const uint32_t dbuf = stage_bytes >> 4, dstep = 2u * N;  // buffer, K-step B (16-byte units)
+      int e = 0;
+      int b = 0;
+      uint32_t par = 0;
+      const bool prof = a.stats != nullptr;
+      long long t_full = 0, t_afull = 0, t_done = 0, t_issue = 0;  // t_done: unused now
+      unsigned long long mmau = 0;
+      const long long t_loop0 = prof ? clock64() : 0;
+      for (; e < a.nstage; ++e) {
+        if (!mbar_wait_t(bar_full + 8 * b, par, prof, t_full) ||
+            !mbar_wait_t(bar_afull + 8 * b, par, prof, t_afull)) {
+          fail = 1;
+          break;
+        }
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        const long long t_i0 = prof ? clock64() : 0;
+        const uint32_t smask = stage_word(a, s_stage, e) >> 26;
+        const uint32_t nact = (uint32_t)__popc(smask);
+        const uint64_t dA = dA0 + (uint64_t)(b * dbuf), dL = dL0 + (uint64_t)(b * dbuf);
+        const uint64_t dB = dB0 + (uint64_t)(b * dbuf);
+        uint32_t act = 0;
+        uint32_t acc = e > 0 ? 1u : 0u;
+#pragma unroll
+        for (int s = 0; s < TC_STEPS; ++s) {
+          if (smask >> s & 1u) {
+            const uint64_t bh = dB + (uint64_t)(act * dstep), bl = dB + (uint64_t)((nact + act) * dstep);
+#pragma unroll
+            for (int mb = 0; mb < TC_MB; ++mb) {
+              const uint32_t ao = 8u * (32u * mb + 2u * s);  // 128 (32 mb + 2 s) bytes
+              const uint32_t d = tmem + (uint32_t)(mb * N);
+              mma_tf32(d, dA + ao, bh, idesc, acc);
+              if (!a.exact) {
+                mma_tf32(d, dA + ao, bl, idesc, 1u);
+                mma_tf32(d, dL + ao, bh, idesc, 1u);
+              }
+            }
+            ++act;
+            acc = 1u;
+          }
+        }
+        mma_commit(bar_done + 8 * b);
+        if (prof) {
+          t_issue += clock64() - t_i0;
+          mmau += (unsigned long long)nact * TC_MB * (a.exact ? 1 : 3) * N;
+        }
+        if (++b == TC_NST) { b = 0; par ^= 1u; }
+      }
+      if (prof) {
+        atomicAdd(a.stats + ST_TC_LOOP, (unsigned long long)(clock64() - t_loop0));
+        atomicAdd(a.stats + ST_TC_WFULL, (unsigned long long)t_full);
+        atomicAdd(a.stats + ST_TC_WAFULL, (unsigned long long)t_afull);
+        atomicAdd(a.stats + ST_TC_WDONE, (unsigned long long)t_done);
+        atomicAdd(a.stats + ST_TC_CTAS, 1ull);
+        atomicAdd(a.stats + ST_TC_ISSUE, (unsigned long long)t_issue);
+        atomicAdd(a.stats + ST_TC_MMAU, mmau);
+      }
+      // every MMA issued has completed (or the waits gave up)
+      if (a.nstage > 0) mma_commit(bar_fin);
+      else mbar_arrive(bar_fin);
     }
-    if (!fail) {
+    __syncwarp();
+  } else {
+    // ---- A images (TI values loaded two stages ahead, in two register sets) ----
+    const int ptid = tid - 32;
+    float va[TC_UPT][4], vb[TC_UPT][4];
+    StageInfo sa{}, sbi{};
+    if (a.nstage > 0) {
+      sa = stage_info(a, s_stage, 0, p0);
+      stage_load(a, sa, ptid, va);
+    }
+    if (a.nstage > 1) {
+      sbi = stage_info(a, s_stage, 1, p0);
+      stage_load(a, sbi, ptid, vb);
+    }
+    const bool prof = a.stats != nullptr && warp == 1 && lane == 0;
+    long long t_wait = 0;
+    const long long t_p0 = prof ? clock64() : 0;
+    // write stage e's images from v; false when the wait for the buffer gave up
+    const bool copier = warp == 1 && lane == 0;  // issues the B copies
+    int ncopied = 0;
+    auto build = [&](int e, const StageInfo& si, float (&v)[TC_UPT][4]) -> bool {
+      const int b = e % TC_NST;
+      const uint32_t use = (uint32_t)(e / TC_NST);
+      const bool ok = use == 0 || mbar_wait_t(bar_done + 8 * b, (use - 1) & 1u, prof, t_wait);
+      if (__any_sync(0xffffffffu, !ok)) return false;  // the warp leaves together
+      if (copier) {
+        const uint32_t bytes = (uint32_t)__popc(si.smask) * (a.exact ? 32u : 64u) * (uint32_t)N;
+        bulk_g2s(sbase + b * stage_bytes, a.B + (size_t)si.pre * 64 * N, bytes, bar_full + 8 * b);
+        ncopied = e + 1;
+      }
+      const uint32_t sa_hi = sbase + b * stage_bytes + bbytes, sa_lo = sa_hi + TC_NQ * 128u;
 #pragma unroll
       for (int i = 0; i < TC_UPT; ++i) {
-        const int u = tid + i * TC_THREADS;
+        const int u = ptid + i * TC_PTHREADS;
         if (u < si.nunits) {
           uint32_t h[4], l[4];
 #pragma unroll
@@ -348,56 +469,37 @@ __global__ void __launch_bounds__(TC_THREADS, 1) corr_tc_kernel(const TcArgs a) 
           if (!a.exact) st_shared_v4(sa_lo + 16u * u, l[0], l[1], l[2], l[3]);
         }
       }
-    }
-    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-    if (__syncthreads_or(fail)) {
-      aborted = 1;
-      break;
-    }
-    if (tid == 0) {
-      if (!mbar_wait(bar_full + 8 * b, use & 1u)) {
-        fail = 1;  // reaches every thread at the next barrier
-      } else {
-        pend_b = -1;
-        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        int act = 0;
-        for (int s = 0; s < TC_STEPS; ++s) {
-          if (!(smask >> s & 1u)) continue;
-          const uint32_t bh = sb + (uint32_t)act * 32u * N;
-          const uint32_t bl = sb + (uint32_t)(nact + act) * 32u * N;
-          ++act;
-          const uint64_t dbh = make_desc(bh, 16u * N, 128u), dbl = make_desc(bl, 16u * N, 128u);
-#pragma unroll
-          for (int mb = 0; mb < TC_MB; ++mb) {
-            const uint32_t aoff = 128u * (32u * mb + 2u * s);
-            const uint64_t dah = make_desc(sa_hi + aoff, 128u, 256u);
-            const uint32_t d = tmem + (uint32_t)(mb * N);
-            mma_tf32(d, dah, dbh, idesc, (e > 0 || act > 1) ? 1u : 0u);
-            if (!a.exact) {
-              const uint64_t dal = make_desc(sa_lo + aoff, 128u, 256u);
-              mma_tf32(d, dah, dbl, idesc, 1u);
-              mma_tf32(d, dal, dbh, idesc, 1u);
-            }
-          }
-        }
-        mma_commit(bar_done + 8 * b);
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      __syncwarp();
+      if (lane == 0) mbar_arrive(bar_afull + 8 * b);
+      return true;
+    };
+    for (int e = 0; e < a.nstage; e += 2) {
+      if (!build(e, sa, va)) { fail = 1; break; }
+      if (e + 2 < a.nstage) {
+        sa = stage_info(a, s_stage, e + 2, p0);
+        stage_load(a, sa, ptid, va);
+      }
+      if (e + 1 >= a.nstage) break;
+      if (!build(e + 1, sbi, vb)) { fail = 1; break; }
+      if (e + 3 < a.nstage) {
+        sbi = stage_info(a, s_stage, e + 3, p0);
+        stage_load(a, sbi, ptid, vb);
       }
     }
-    if (e + 1 < a.nstage) {
-      si = stage_info(a, e + 1, p0);
-      stage_load(a, si, tid, v);
+    if (copier)  // the last copies have landed (bounded waits) before the buffers go away
+      for (int st = ncopied - 1; st >= 0 && st >= ncopied - TC_NST; --st)
+        mbar_wait(bar_full + 8 * (st % TC_NST), (uint32_t)(st / TC_NST) & 1u);
+    if (prof) {
+      atomicAdd(a.stats + ST_TC_PWAIT, (unsigned long long)t_wait);
+      atomicAdd(a.stats + ST_TC_PLOOP, (unsigned long long)(clock64() - t_p0));
     }
-  }
-  if (!aborted && __syncthreads_or(fail)) aborted = 1;  // a copy wait of the last stage
-  // everything thread 0 issued has completed (or the wait gave up)
-  if (tid == 0) {
-    mma_commit(bar_fin);
-    if (pend_b >= 0) mbar_wait(bar_full + 8 * pend_b, pend_par);
   }
   if (!mbar_wait(bar_fin, 0)) fail = 1;
   if (__syncthreads_or(fail)) aborted = 1;
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
 
+  const long long t_epi0 = (a.stats && tid == 0) ? clock64() : 0;
   if (!aborted) {
     // A2 of each mask at each position, in FP64 from the integral image, stored as FP32
     const int lq = warp & 3, half = warp >> 2;
@@ -431,7 +533,12 @@ __global__ void __launch_bounds__(TC_THREADS, 1) corr_tc_kernel(const TcArgs a) 
 #pragma unroll 1
       for (int c0 = 16 * half; c0 < N; c0 += 32) {
         uint32_t r[16];
-        tmem_ld16(tmem + ((uint32_t)(32 * lq) << 16) + (uint32_t)(mb * N + c0), r);
+        if (a.nstage > 0) {
+          tmem_ld16(tmem + ((uint32_t)(32 * lq) << 16) + (uint32_t)(mb * N + c0), r);
+        } else {
+#pragma unroll
+          for (int j = 0; j < 16; ++j) r[j] = 0u;  // no offsets: AB = 0
+        }
 #pragma unroll
         for (int j = 0; j < 16; ++j) {
           const int n = c0 + j;
@@ -461,6 +568,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) corr_tc_kernel(const TcArgs a) 
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
+  if (a.stats && tid == 0) atomicAdd(a.stats + ST_TC_EPI, (unsigned long long)(clock64() - t_epi0));
   if (warp == 0)
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
                  "r"(a.tmem_cols));
@@ -477,7 +585,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) corr_tc_kernel(const TcArgs a) 
 
 size_t tc_smem_bytes(int N) {
   return (size_t)TC_NST * ((size_t)TC_STEPS * 64 * N + 2 * TC_NQ * 128) + 32 * (size_t)N +
-         4 * IQ_TC_MAXBOX * 128 * TC_MB + 8 * (2 * TC_NST + 1);
+         4 * IQ_TC_MAXBOX * 128 * TC_MB + 8 * (3 * TC_NST + 1) + 8 * TC_SMW;
 }
 
 __global__ void tf32_check_kernel(const float* __restrict__ d, int64_t n, int* flag) {
@@ -542,7 +650,7 @@ int iq_launch_corr_tc(iq_ctx* ctx, const TcCorrLaunch& L) {
   if (L.tile.x / TC_GROUP >= 64 || L.tile.y >= 1024 || L.tile.z >= 1024)
     return iq_set_error(IQ_ERR_LIMIT, "tensor-core correlation: tile too large");
   const Dim3 od = L.out_dims;
-  if (od.vol() <= 0 || L.nstage <= 0) return IQ_OK;
+  if (od.vol() <= 0) return IQ_OK;
   TcArgs a;
   a.img = L.img;
   a.ix = L.img_dims.x;
@@ -568,9 +676,10 @@ int iq_launch_corr_tc(iq_ctx* ctx, const TcCorrLaunch& L) {
   while (tc < (uint32_t)(TC_MB * L.N)) tc <<= 1;
   a.tmem_cols = tc;
   a.status = ctx->d_status;
+  a.stats = ctx->prof ? ctx->d_stats : nullptr;
 
   iq_timer_start(ctx, "corr");
-  {
+  if (L.nstage > 0) {  // no stages: every column's mask is empty and its products are zero
     PackArgs p;
     p.grid = L.grid; p.gx = L.grid_dims.x; p.gy = L.grid_dims.y; p.tx = L.tile.x;
     p.cols = L.cols; p.N = L.N;
@@ -586,6 +695,11 @@ int iq_launch_corr_tc(iq_ctx* ctx, const TcCorrLaunch& L) {
   IQ_CUDA_OK(cudaFuncSetAttribute(corr_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   (int)smem));
   const int64_t nblk = od.z * bpp;
+  if (ctx->prof) {
+    ctx->prof_mma_flops += 2.0 * (double)nblk * 128 * TC_MB * (double)L.nsteps * 8 * L.N *
+                           (L.exact ? 1 : 3);
+    ctx->prof_mma_launches += 1;
+  }
   corr_tc_kernel<<<(unsigned)nblk, TC_THREADS, smem, ctx->stream>>>(a);
   iq_count(ctx);
   iq_timer_stop(ctx, "corr", L.flops);

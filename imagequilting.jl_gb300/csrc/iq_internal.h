@@ -45,6 +45,8 @@ struct iq_ctx {
   // [3] pick relaxation iterations, [4] pick candidates, [5] pick CTAs, [6] max cut rounds,
   // [7] max cut BFS levels
   unsigned long long* d_stats = nullptr;
+  double prof_mma_flops = 0;    // tensor-pipe FLOPs issued by the correlation while profiling
+  int64_t prof_mma_launches = 0;
   // tuning knobs (iq_set_option)
   int cut_gr_period = 32;
   int cut_threads = 512;
@@ -54,7 +56,13 @@ struct iq_ctx {
   int64_t max_steps = -1;       // tiles simulated per realization (< 0: all)
 };
 enum IqStat { ST_CUT_ROUNDS = 0, ST_CUT_LEVELS, ST_CUT_CTAS, ST_PICK_ITERS, ST_PICK_CAND,
-              ST_PICK_CTAS, ST_CUT_MAXROUNDS, ST_CUT_MAXLEVELS, ST_COUNT };
+              ST_PICK_CTAS, ST_CUT_MAXROUNDS, ST_CUT_MAXLEVELS,
+              // tensor-core correlation, SM cycles summed over CTAs: issuer loop, issuer waits
+              // for B copies / A images / MMA completion (refills), producer (warp 1) waits
+              // and loop, epilogue; the CTA count; cycles inside the MMA issue blocks and the
+              // MMAs issued in units of one M=128 N=256 K=8 MMA (x 256)
+              ST_TC_LOOP, ST_TC_WFULL, ST_TC_WAFULL, ST_TC_WDONE, ST_TC_PWAIT, ST_TC_PLOOP,
+              ST_TC_EPI, ST_TC_CTAS, ST_TC_ISSUE, ST_TC_MMAU, ST_COUNT };
 
 // scratch slot ids
 enum IqSlot {

@@ -549,12 +549,12 @@ extern "C" int iq_simulate(iq_ctx* ctx, const iq_sim_params* p, const iq_hard_da
   std::vector<TcCol> tccols;
   std::vector<int64_t> tcbeg(nchunk + 1, 0);
   std::vector<uint8_t> chunk_tc(nchunk, 0);
-  // Chunks whose masks all have offsets run their overlap distances on the tensor cores:
-  // the (tile, realization) columns of the chunk, grouped by mask, in launches of at most
-  // 256 columns and 8 masks with balanced widths.
+  // Every chunk runs its overlap distances on the tensor cores: the (tile, realization)
+  // columns of the chunk, grouped by mask, in launches of at most 256 columns and 8 masks
+  // with balanced widths. A tile without pasted neighbours (mask box = the whole tile) gets
+  // zero templates and A2 = B2 = 0, i.e. D = 0 like the reference's empty overlap.
   for (int64_t c = 0; c < nchunk && tc; ++c) {
-    bool ok = T > 0;
-    for (int64_t k = cbeg[c]; k < cbeg[c + 1] && ok; ++k) ok = cfgs[steps[k].cfg].K > 0;
+    const bool ok = T > 0;
     chunk_tc[c] = ok;
     if (ok) {
       std::vector<std::pair<int, int64_t>> order;  // (cfg, step index in chunk) sorted by cfg
