@@ -137,18 +137,30 @@ def measured_peaks():
     return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0}, "fallback"
 
 
-def profile_traffic(kernel, workload_name):
-    """dram bytes per launch of `kernel` from a committed ncu summary, if one exists."""
+def profile_traffic(kernel, workload_name, columns=None):
+    """DRAM bytes per launch of `kernel` from a committed ncu summary, if one exists.
+
+    The summary gives `dram_bytes_per_launch:` of the captured launch and, for the correlation,
+    `columns_per_launch:` of that launch; the distance maps it writes dominate its traffic and
+    grow with the columns, so the figure is scaled to `columns` (this run's mean)."""
     fn = os.path.join(ROOT, "profiles", "%s_%s.txt" % (kernel, workload_name))
     if not os.path.exists(fn):
         return None
+    vals = {}
     for ln in open(fn):
-        if ln.startswith("dram_bytes_per_launch:"):
+        if ":" in ln:
+            k, v = ln.split(":", 1)
             try:
-                return float(ln.split(":", 1)[1].split()[0])
-            except ValueError:
-                return None
-    return None
+                vals[k.strip()] = float(v.split()[0])
+            except (ValueError, IndexError):
+                pass
+    b = vals.get("dram_bytes_per_launch")
+    if b is None:
+        return None
+    c = vals.get("columns_per_launch")
+    if c and columns:
+        b *= columns / c
+    return b
 
 
 def dist_setup():
@@ -340,6 +352,7 @@ def run_ours(args, W, dist, rank, world):
     clk = clocks.stop()
     prof = {k: ctx.profile_get(k) for k in ("corr", "pick", "graphcut", "paste")}
     mma = ctx.profile_get("corr.mma")
+    cols = ctx.profile_get("corr.columns")
     counters = {k: ctx.profile_get(k) for k in ("graphcut.rounds", "graphcut.levels",
                                                  "pick.iterations", "pick.candidates")}
     counters = {k: {"mean": (v[2] / v[1]) if v[1] else None, "ctas": v[1]}
@@ -391,7 +404,7 @@ def run_ours(args, W, dist, rank, world):
             "peak": peaks.get("bf16_tflops"), "unit": "TFLOP/s",
             "peak_kind": "%s (bf16 dense, burst)" % peak_kind,
             "flops_per_launch": corr_flops / corr_n if corr_n else None,
-            "traffic": profile_traffic("corr", W["name"]),
+            "traffic": profile_traffic("corr_tc_kernel", W["name"], cols[2] / cols[1] if cols[1] else None),
             "mma_tflops_issued": (mma[2] / (corr_ms / 1e3) / 1e12) if corr_ms and mma[2] else None,
             "note": "achieved = algorithmic FLOPs (2 x positions x mask offsets x templates) "
                     "over the correlation's time; the tensor pipe issues TF32 MMAs (three per "

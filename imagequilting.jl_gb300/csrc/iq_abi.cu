@@ -77,6 +77,7 @@ extern "C" int iq_profile(iq_ctx* ctx, int32_t enable) {
   for (auto& kv : ctx->timers) { kv.second.used = 0; kv.second.work = 0; }
   ctx->prof_mma_flops = 0;
   ctx->prof_mma_launches = 0;
+  ctx->prof_tc_cols = 0;
   cudaMemsetAsync(ctx->d_stats, 0, sizeof(unsigned long long) * ST_COUNT, ctx->stream);
   ctx->prof = enable != 0;
   return IQ_OK;
@@ -92,11 +93,12 @@ extern "C" int iq_profile_get(iq_ctx* ctx, const char* kernel, double* ms_total,
   int64_t n = 0;
   // counters: "graphcut.rounds", "graphcut.levels" (work = total, launches = CTAs),
   // "pick.iterations", "pick.candidates" (work = total, launches = CTAs), "corr.mma" (work =
-  // tensor-pipe FLOPs issued, with the TF32 split and the padded positions and offsets)
-  if (!strcmp(kernel, "corr.mma")) {
+  // tensor-pipe FLOPs issued, with the TF32 split and the padded positions and offsets),
+  // "corr.columns" (work = columns of the tensor-core launches, launches = their count)
+  if (!strcmp(kernel, "corr.mma") || !strcmp(kernel, "corr.columns")) {
     if (ms_total) *ms_total = 0;
     if (launches) *launches = ctx->prof_mma_launches;
-    if (work) *work = ctx->prof_mma_flops;
+    if (work) *work = kernel[5] == 'm' ? ctx->prof_mma_flops : ctx->prof_tc_cols;
     return IQ_OK;
   }
   // "corr.loop", "corr.wait_full", "corr.wait_afull", "corr.wait_done", "corr.producer_wait",

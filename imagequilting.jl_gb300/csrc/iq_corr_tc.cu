@@ -699,6 +699,7 @@ int iq_launch_corr_tc(iq_ctx* ctx, const TcCorrLaunch& L) {
     ctx->prof_mma_flops += 2.0 * (double)nblk * 128 * TC_MB * (double)L.nsteps * 8 * L.N *
                            (L.exact ? 1 : 3);
     ctx->prof_mma_launches += 1;
+    ctx->prof_tc_cols += L.N;
   }
   corr_tc_kernel<<<(unsigned)nblk, TC_THREADS, smem, ctx->stream>>>(a);
   iq_count(ctx);

@@ -47,6 +47,7 @@ struct iq_ctx {
   unsigned long long* d_stats = nullptr;
   double prof_mma_flops = 0;    // tensor-pipe FLOPs issued by the correlation while profiling
   int64_t prof_mma_launches = 0;
+  double prof_tc_cols = 0;      // columns (templates, with padding) of those launches
   // tuning knobs (iq_set_option)
   int cut_gr_period = 32;
   int cut_threads = 512;
