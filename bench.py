@@ -190,6 +190,17 @@ def barrier(dist):
         dist.barrier()
 
 
+def step_seed(step, rank):
+    """Seed of one simulation call: ranks shard the realizations (each rank's calls draw their
+    own Philox streams), so no data moves between ranks."""
+    return 1000 + 7919 * step + 104729 * rank
+
+
+def aggregate_rate(units_per_rank_step, steps, world, ms_max):
+    """Whole-job rate: the units every rank processed over the slowest rank's time."""
+    return units_per_rank_step * steps * world / (ms_max / 1e3)
+
+
 # ---------------------------------------------------------------------------------------
 # CPU oracle baseline (bounded sample)
 # ---------------------------------------------------------------------------------------
@@ -318,12 +329,12 @@ def run_ours(args, W, dist, rank, world):
     size = _lib.i64arr(ti_h.shape)
 
     def step_resident(i):
-        p.seed = 1000 + 7919 * i + 104729 * rank
+        p.seed = step_seed(i, rank)
         _lib.check(lib.iq_simulate(ctx.h, ctypes.byref(p), ctypes.byref(hd_dev), len(soft_d),
                                    sd_dev if soft_d else None, out_d.data_ptr(), None, None))
 
     def step_e2e(i):
-        p.seed = 1000 + 7919 * i + 104729 * rank
+        p.seed = step_seed(i, rank)
         _lib.check(lib.iq_set_ti(ctx.h, ti_h.ctypes.data, ti_dt, N, size))
         _lib.check(lib.iq_simulate(ctx.h, ctypes.byref(p), ctypes.byref(hd_host), len(soft_h),
                                    sd_host if soft_h else None, out_h.ctypes.data, None, None))
@@ -393,8 +404,8 @@ def run_ours(args, W, dist, rank, world):
     if rank != 0:
         ctx.close()
         return
-    value = voxels * args.steps * world / (ms_max / 1e3)
-    e2e_value = voxels * args.steps * world / (ms_e2e_max / 1e3)
+    value = aggregate_rate(voxels, args.steps, world, ms_max)
+    e2e_value = aggregate_rate(voxels, args.steps, world, ms_e2e_max)
     peaks, peak_kind = measured_peaks()
     shares = {k: v[0] for k, v in prof.items()}
     dom = max(shares, key=lambda k: shares[k])
