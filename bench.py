@@ -376,6 +376,9 @@ def run_ours(args, W, dist, rank, world):
                                                     "producer_loop", "epilogue", "issue",
                                                     "mma_units")}
     counters["corr_cycles_per_cta"] = {k: (v[2] / v[1]) if v[1] else None for k, v in tc.items()}
+    gc = {k: ctx.profile_get("graphcut." + k) for k in ("setup_cycles", "round_cycles",
+                                                        "relabel_cycles")}
+    counters["graphcut_cycles_per_cta"] = {k: (v[2] / v[1]) if v[1] else None for k, v in gc.items()}
     ctx.profile(False)
     ms_max = reduce_max(dist, ms)
     barrier(dist)

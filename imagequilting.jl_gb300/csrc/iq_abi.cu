@@ -103,20 +103,22 @@ extern "C" int iq_profile_get(iq_ctx* ctx, const char* kernel, double* ms_total,
   }
   // "corr.loop", "corr.wait_full", "corr.wait_afull", "corr.wait_done", "corr.producer_wait",
   // "corr.producer_loop", "corr.epilogue" (work = SM cycles summed over CTAs, launches = CTAs)
-  const char* names[15] = {"graphcut.rounds", "graphcut.levels", "pick.iterations",
+  const char* names[18] = {"graphcut.rounds", "graphcut.levels", "pick.iterations",
                            "pick.candidates", "graphcut.max_rounds", "graphcut.max_levels",
                            "corr.loop", "corr.wait_full", "corr.wait_afull", "corr.wait_done",
                            "corr.producer_wait", "corr.producer_loop", "corr.epilogue",
-                           "corr.issue", "corr.mma_units"};
-  const int idx[15][2] = {{ST_CUT_ROUNDS, ST_CUT_CTAS}, {ST_CUT_LEVELS, ST_CUT_CTAS},
+                           "corr.issue", "corr.mma_units", "graphcut.setup_cycles",
+                           "graphcut.round_cycles", "graphcut.relabel_cycles"};
+  const int idx[18][2] = {{ST_CUT_ROUNDS, ST_CUT_CTAS}, {ST_CUT_LEVELS, ST_CUT_CTAS},
                           {ST_PICK_ITERS, ST_PICK_CTAS}, {ST_PICK_CAND, ST_PICK_CTAS},
                           {ST_CUT_MAXROUNDS, ST_CUT_CTAS}, {ST_CUT_MAXLEVELS, ST_CUT_CTAS},
                           {ST_TC_LOOP, ST_TC_CTAS}, {ST_TC_WFULL, ST_TC_CTAS},
                           {ST_TC_WAFULL, ST_TC_CTAS}, {ST_TC_WDONE, ST_TC_CTAS},
                           {ST_TC_PWAIT, ST_TC_CTAS}, {ST_TC_PLOOP, ST_TC_CTAS},
                           {ST_TC_EPI, ST_TC_CTAS}, {ST_TC_ISSUE, ST_TC_CTAS},
-                          {ST_TC_MMAU, ST_TC_CTAS}};
-  for (int i = 0; i < 15; ++i)
+                          {ST_TC_MMAU, ST_TC_CTAS}, {ST_CUT_TSETUP, ST_CUT_CTAS},
+                          {ST_CUT_TROUNDS, ST_CUT_CTAS}, {ST_CUT_TGR, ST_CUT_CTAS}};
+  for (int i = 0; i < 18; ++i)
     if (!strcmp(kernel, names[i])) {
       unsigned long long h[ST_COUNT];
       IQ_CUDA_OK(cudaMemcpy(h, ctx->d_stats, sizeof(h), cudaMemcpyDeviceToHost));

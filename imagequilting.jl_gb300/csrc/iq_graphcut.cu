@@ -10,17 +10,19 @@
 //     the slab, so that every residual (<= 2 cmax) and excess (<= 12 cmax) is a multiple of q
 //     below 2^53 q and all flow arithmetic is exact (zero gradient sums give eps-denominator
 //     capacities ~2^52 times the others, which unquantized Float64 flows cannot resolve);
-//   * residuals are stored per directed arc in Float64; an arc is open when its residual is
-//     positive (the oracle quantizes and tests the same way);
-//   * each round: every active node pushes along its first admissible arc (h(u) = h(v) + 1),
-//     then every node gathers the flow pushed into it in a fixed order and relabels if it
-//     still has excess and no admissible arc -- deterministic, no atomics;
+//   * so residuals and excesses are kept as int64 counts of q (the same values as the exact
+//     Float64 arithmetic, without GB300's narrow FP64 pipe); an arc is open when its residual
+//     is positive (the oracle quantizes and tests the same way);
+//   * each round: every active node pushes along its admissible arcs (h(u) = h(v) + 1) while
+//     it has excess, adding to the receivers' excesses with integer atomics, then every node
+//     with excess and no admissible arc relabels. The flow found depends on the order of the
+//     atomics, the cut does not: integer sums are exact, and the set of nodes that can reach
+//     t is the same for every maximum preflow;
 //   * a global relabel (BFS from t over open arcs) runs at the start, every GR rounds and at
 //     the end; nodes that cannot reach t get height NH and stop being active.
 // At the end the nodes that can reach t are the sink side of the canonical minimum cut (the
 // same set for every maximum flow, which is what BK's sink tree holds at termination), and
-// mask = not sink side (graphcut.jl:75-81). Excess arithmetic uses __dadd/__dsub; every
-// comparison is done on the bit patterns of non-negative doubles (integer compares).
+// mask = not sink side (graphcut.jl:75-81).
 #include "iq_internal.h"
 
 namespace {
@@ -45,38 +47,42 @@ struct CutArgs {
 
 __device__ __forceinline__ long long dbits(double x) { return __double_as_longlong(x); }
 
+// Slab graph in shared memory. Everything a lookup needs is a scalar or one base pointer:
+// an array indexed by a run-time direction would live in local memory and cost a memory
+// access per arc.
 struct Graph {
-  int n, ext[3], st[3];
+  int n, s1, s2;  // nodes; strides of y and z (x has stride 1)
   int d;          // cut dimension
   int L;          // extent along d
   int NH;         // height of s (= number of interior nodes + 2)
-  double* rf[3];
-  double* rb[3];
-  double* ex;
-  double* pamt;
-  int* h[2];
-  int* front[2];  // BFS frontier lists
-  signed char* pdir;
+  // residuals in units of q: R[2e n + u] for the arc u -> u + stride(e), R[(2e+1) n + u] for
+  // the arc u + stride(e) -> u
+  long long* R;
+  long long* ex;  // excess
   uint8_t* info;  // bits 0-5: neighbour exists in direction 0..5; bits 6-7: kind
 
+  __device__ __forceinline__ int stride(int e) const { return e == 0 ? 1 : (e == 1 ? s1 : s2); }
   __device__ __forceinline__ int kind(int u) const { return info[u] >> 6; }  // 0 interior, 1 s, 2 t
   __device__ __forceinline__ bool nbr(int u, int dir, int& v) const {
     if (!(info[u] >> dir & 1)) return false;
-    v = (dir & 1) ? u + st[dir >> 1] : u - st[dir >> 1];
+    v = (dir & 1) ? u + stride(dir >> 1) : u - stride(dir >> 1);
     return true;
   }
-  __device__ __forceinline__ int height(const int* hc, int v) const {
+  template <typename HT>
+  __device__ __forceinline__ int height(const HT* hc, int v) const {
     int k = kind(v);
-    return k == 1 ? NH : (k == 2 ? 0 : hc[v]);
+    return k == 1 ? NH : (k == 2 ? 0 : (int)hc[v]);
   }
+  __device__ __forceinline__ long long& rf(int e, int u) const { return R[(2 * e) * n + u]; }
+  __device__ __forceinline__ long long& rb(int e, int u) const { return R[(2 * e + 1) * n + u]; }
   // residual u->v (and pointers to both arc residuals) for direction dir
-  __device__ __forceinline__ void arc(int u, int v, int dir, double*& ruv, double*& rvu) const {
+  __device__ __forceinline__ void arc(int u, int v, int dir, long long*& ruv, long long*& rvu) const {
     const int e = dir >> 1;
-    if (dir & 1) { ruv = &rf[e][u]; rvu = &rb[e][u]; }
-    else { ruv = &rb[e][v]; rvu = &rf[e][v]; }
+    if (dir & 1) { ruv = R + (2 * e) * n + u; rvu = R + (2 * e + 1) * n + u; }
+    else { ruv = R + (2 * e + 1) * n + v; rvu = R + (2 * e) * n + v; }
   }
-  __device__ __forceinline__ bool open(const double* ruv, const double*) const {
-    return dbits(*ruv) > 0;  // residuals are non-negative; +0 and -0 are closed
+  __device__ __forceinline__ bool open(const long long* ruv, const long long*) const {
+    return *ruv > 0;
   }
 };
 
@@ -84,7 +90,18 @@ struct Graph {
 // neighbours of the previous level's frontier (frontier lists fa/fb, counters cnt[2]), so the
 // search costs O(edges) instead of O(nodes x levels). Heights are BFS distances, whatever
 // order the frontier is filled in. Returns the number of levels.
-__device__ int global_relabel(const Graph& g, int* hc, int* fa, int* fb, int* cnt) {
+// heights and BFS frontier entries are HT: 16-bit for slabs below 32768 nodes (a smaller
+// shared-memory footprint, two CTAs per SM), else 32-bit
+__device__ __forceinline__ bool cas_height(short* p, int expect, int val) {
+  return atomicCAS(reinterpret_cast<unsigned short*>(p), (unsigned short)expect,
+                   (unsigned short)val) == (unsigned short)expect;
+}
+__device__ __forceinline__ bool cas_height(int* p, int expect, int val) {
+  return atomicCAS(p, expect, val) == expect;
+}
+
+template <typename HT>
+__device__ int global_relabel(const Graph& g, HT* hc, HT* fa, HT* fb, int* cnt) {
   if (threadIdx.x == 0) { cnt[0] = 0; cnt[1] = 0; }
   __syncthreads();
   const int dsink = 2 * g.d + 1;  // direction towards the sink slice
@@ -93,32 +110,33 @@ __device__ int global_relabel(const Graph& g, int* hc, int* fa, int* fb, int* cn
     int h = g.NH;
     int v;
     if (g.nbr(u, dsink, v) && g.kind(v) == 2) {
-      double *ruv, *rvu;
+      long long *ruv, *rvu;
       g.arc(u, v, dsink, ruv, rvu);
       if (g.open(ruv, rvu)) h = 1;
     }
-    hc[u] = h;
-    if (h == 1) fa[atomicAdd(&cnt[0], 1)] = u;
+    hc[u] = (HT)h;
+    if (h == 1) fa[atomicAdd(&cnt[0], 1)] = (HT)u;
   }
   __syncthreads();
   int level = 1, cur = 0;
   for (;;) {
     const int nf = cnt[cur];
-    int* front = cur ? fb : fa;
-    int* next = cur ? fa : fb;
+    HT* front = cur ? fb : fa;
+    HT* next = cur ? fa : fb;
     if (nf == 0) break;
     if (threadIdx.x == 0) cnt[cur ^ 1] = 0;
     __syncthreads();
     for (int i = threadIdx.x; i < nf; i += blockDim.x) {
       const int v = front[i];
+#pragma unroll
       for (int dir = 0; dir < 6; ++dir) {
         int u;
         if (!g.nbr(v, dir, u)) continue;
         if (g.kind(u) != 0 || hc[u] != g.NH) continue;
-        double *ruv, *rvu;
+        long long *ruv, *rvu;
         g.arc(u, v, dir ^ 1, ruv, rvu);  // arc u -> v
         if (!g.open(ruv, rvu)) continue;
-        if (atomicCAS(&hc[u], g.NH, level + 1) == g.NH) next[atomicAdd(&cnt[cur ^ 1], 1)] = u;
+        if (cas_height(&hc[u], g.NH, level + 1)) next[atomicAdd(&cnt[cur ^ 1], 1)] = (HT)u;
       }
     }
     __syncthreads();
@@ -129,6 +147,7 @@ __device__ int global_relabel(const Graph& g, int* hc, int* fa, int* fb, int* cn
   return level;
 }
 
+template <typename HT>
 __global__ void __launch_bounds__(CUT_MAX_THREADS) cut_kernel(const CutArgs a) {
   extern __shared__ __align__(16) char smem[];
   const int s_id = blockIdx.x;
@@ -138,35 +157,35 @@ __global__ void __launch_bounds__(CUT_MAX_THREADS) cut_kernel(const CutArgs a) {
   if (s_id >= tk.nslab) return;
   const CutSlab sl = tk.slab[s_id];
   const int64_t tile_start = tk.start;
+  const bool prof = a.stats != nullptr && threadIdx.x == 0;
+  const long long t_start = prof ? clock64() : 0;
+  long long t_gr = 0;
   Graph g;
-  g.ext[0] = (int)sl.ext[0]; g.ext[1] = (int)sl.ext[1]; g.ext[2] = (int)sl.ext[2];
-  g.st[0] = 1; g.st[1] = g.ext[0]; g.st[2] = g.ext[0] * g.ext[1];
-  g.n = g.ext[0] * g.ext[1] * g.ext[2];
+  const int ex0 = (int)sl.ext[0], ex1 = (int)sl.ext[1], ex2 = (int)sl.ext[2];
+  g.s1 = ex0; g.s2 = ex0 * ex1;
+  g.n = ex0 * ex1 * ex2;
   g.d = sl.dim;
-  g.L = g.ext[g.d];
+  g.L = g.d == 0 ? ex0 : (g.d == 1 ? ex1 : ex2);
   g.NH = g.n / g.L * (g.L > 2 ? g.L - 2 : 0) + 2;
   const int n = g.n;
 
   char* base = a.scratch ? a.scratch + (int64_t)(blockIdx.y * gridDim.x + blockIdx.x) *
                                            a.scratch_per_cta
                          : smem;
-  double* dp = reinterpret_cast<double*>(base);
-  for (int e = 0; e < 3; ++e) { g.rf[e] = dp + (2 * e) * n; g.rb[e] = dp + (2 * e + 1) * n; }
+  long long* dp = reinterpret_cast<long long*>(base);
+  g.R = dp;
   g.ex = dp + 6 * n;
-  g.pamt = dp + 7 * n;
-  int* ip = reinterpret_cast<int*>(dp + 8 * n);
-  g.h[0] = ip;
-  g.h[1] = ip + n;
-  g.front[0] = ip + 2 * n;
-  g.front[1] = ip + 3 * n;
+  HT* ip = reinterpret_cast<HT*>(dp + 7 * n);
+  HT* const h0 = ip;          // heights, double-buffered
+  HT* const h1 = ip + n;
+  HT* const fa = ip + 2 * n;  // BFS frontier lists
+  HT* const fb = ip + 3 * n;
   __shared__ int s_cnt[2];
   __shared__ unsigned long long s_cmax;  // bits of the largest capacity
   if (threadIdx.x == 0) s_cmax = 0ull;
-  g.pdir = reinterpret_cast<signed char*>(ip + 4 * n);
-  g.info = reinterpret_cast<uint8_t*>(g.pdir + n);
-  float* Av = reinterpret_cast<float*>(g.pamt);  // A and B alias pamt during set-up
-  float* Bv = Av + n;                            // (8n bytes = pamt)
-  // ex holds nothing yet either; B needs n floats after A: pamt is n doubles = 2n floats
+  g.info = reinterpret_cast<uint8_t*>(ip + 4 * n);
+  float* Av = reinterpret_cast<float*>(g.ex);  // A and B alias the excesses (8n bytes), which
+  float* Bv = Av + n;                          // are first written after the capacities
 
   // ---- load A (simulation grid) and B (training image at the drawn pattern) ----
   int64_t bstart = 0;
@@ -181,14 +200,15 @@ __global__ void __launch_bounds__(CUT_MAX_THREADS) cut_kernel(const CutArgs a) {
     bstart = rx + a.tix * (ry + a.tiy * rz);
   }
   for (int u = threadIdx.x; u < n; u += blockDim.x) {
-    const int x = u % g.ext[0], y = (u / g.ext[0]) % g.ext[1], z = u / g.st[2];
-    const int c[3] = {x, y, z};
+    const int x = u % ex0, y = (u / ex0) % ex1, z = u / g.s2;
     uint8_t inf = 0;
-    for (int e = 0; e < 3; ++e) {
-      if (c[e] > 0) inf |= (uint8_t)(1u << (2 * e));
-      if (c[e] + 1 < g.ext[e]) inf |= (uint8_t)(1u << (2 * e + 1));
-    }
-    const int cd = c[g.d];
+    if (x > 0) inf |= 1u;
+    if (x + 1 < ex0) inf |= 2u;
+    if (y > 0) inf |= 4u;
+    if (y + 1 < ex1) inf |= 8u;
+    if (z > 0) inf |= 16u;
+    if (z + 1 < ex2) inf |= 32u;
+    const int cd = g.d == 0 ? x : (g.d == 1 ? y : z);
     inf |= (uint8_t)((cd == 0 ? 1 : (cd == g.L - 1 ? 2 : 0)) << 6);
     g.info[u] = inf;
     if (a.A) {
@@ -205,11 +225,12 @@ __global__ void __launch_bounds__(CUT_MAX_THREADS) cut_kernel(const CutArgs a) {
   // ---- capacities (graphcut.jl:22-50) ----
   const double EPS = 2.220446049250313e-16;  // eps(Float64) = 2^-52
   for (int u = threadIdx.x; u < n; u += blockDim.x) {
+#pragma unroll
     for (int e = 0; e < 3; ++e) {
       int v;
       if (!g.nbr(u, 2 * e + 1, v)) continue;
       const bool ok = (g.info[v] >> (2 * e + 1)) & 1;
-      const int w = ok ? v + g.st[e] : v;
+      const int w = ok ? v + g.stride(e) : v;
       const float Du = fabsf(__fsub_rn(Av[u], Bv[u]));
       const float Dv = fabsf(__fsub_rn(Av[v], Bv[v]));
       const float gAu = fabsf(__fsub_rn(Av[v], Av[u]));
@@ -221,95 +242,106 @@ __global__ void __launch_bounds__(CUT_MAX_THREADS) cut_kernel(const CutArgs a) {
       den = __fadd_rn(den, gBu);
       den = __fadd_rn(den, gBv);
       const double cap = __ddiv_rn((double)num, __dadd_rn((double)den, EPS));
-      g.rf[e][u] = cap;
-      g.rb[e][u] = cap;
+      g.rf(e, u) = dbits(cap);  // the double's bits until the quantization below
       atomicMax(&s_cmax, (unsigned long long)dbits(cap));
     }
   }
   __syncthreads();
-  // ---- round every capacity to a multiple of q = 2^(ilogb(cmax) - 47) (exact flows) ----
-  if (s_cmax != 0ull) {
-    int sh = ilogb(__longlong_as_double((long long)s_cmax)) - 47;
+  // ---- capacities in units of q = 2^(ilogb(cmax) - 47), rounded half to even: the flows
+  // are then exact integers (<= 2^49 per arc), the same numbers the oracle's quantized
+  // Float64 arithmetic produces ----
+  {
+    int sh = s_cmax != 0ull ? ilogb(__longlong_as_double((long long)s_cmax)) - 47 : 0;
     if (sh < -1074) sh = -1074;
     for (int u = threadIdx.x; u < n; u += blockDim.x)
+#pragma unroll
       for (int e = 0; e < 3; ++e) {
         int v;
         if (!g.nbr(u, 2 * e + 1, v)) continue;
-        const double c = ldexp(rint(ldexp(g.rf[e][u], -sh)), sh);
-        g.rf[e][u] = c;
-        g.rb[e][u] = c;
+        const long long k = s_cmax != 0ull
+                                ? (long long)rint(ldexp(__longlong_as_double(g.rf(e, u)), -sh))
+                                : 0ll;
+        g.rf(e, u) = k;
+        g.rb(e, u) = k;
       }
     __syncthreads();
   }
 
   // ---- saturate the source slice: push c(s, v) into every interior node of slice 1 ----
   for (int u = threadIdx.x; u < n; u += blockDim.x) {
-    double e0 = 0.0;
-    if (g.kind(u) == 0 && g.kind(u - g.st[g.d]) == 1) {
-      const int sN = u - g.st[g.d];
-      const double c = g.rf[g.d][sN];
-      g.rf[g.d][sN] = 0.0;
-      g.rb[g.d][sN] = __dadd_rn(c, c);
+    long long e0 = 0;
+    if (g.kind(u) == 0 && g.kind(u - g.stride(g.d)) == 1) {
+      const int sN = u - g.stride(g.d);
+      const long long c = g.rf(g.d, sN);
+      g.rf(g.d, sN) = 0;
+      g.rb(g.d, sN) = 2 * c;
       e0 = c;
     }
     g.ex[u] = e0;
-    g.pdir[u] = -1;
   }
   __syncthreads();
 
   int cur = 0;
   int round = 0, levels = 0;
+  const long long t_setup = prof ? clock64() : 0;
+  auto relabel_all = [&]() {
+    const long long t = prof ? clock64() : 0;
+    levels += global_relabel(g, cur ? h1 : h0, fa, fb, s_cnt);
+    if (prof) t_gr += clock64() - t;
+  };
   if (g.L > 2) {
-    levels += global_relabel(g, g.h[cur], g.front[0], g.front[1], s_cnt);
+    relabel_all();
     bool capped = false;
     for (;;) {
-      int* hc = g.h[cur];
-      int* hn = g.h[cur ^ 1];
-      // push phase
+      HT* hc = cur ? h1 : h0;
+      HT* hn = cur ? h0 : h1;
+      // push phase: every active node pushes along all its admissible arcs while it has
+      // excess; the receivers' excesses are updated with integer atomics (exact in any
+      // order). Two ends of one edge never push on it in the same round (that would need
+      // h(u) = h(v) + 1 and h(v) = h(u) + 1), so each residual has one writer.
       for (int u = threadIdx.x; u < n; u += blockDim.x) {
-        signed char pd = -1;
-        if (g.kind(u) == 0 && dbits(g.ex[u]) > 0 && hc[u] < g.NH) {
-          const int hu = hc[u];
-          for (int dir = 0; dir < 6; ++dir) {
-            int v;
-            if (!g.nbr(u, dir, v)) continue;
-            if (hu != g.height(hc, v) + 1) continue;
-            double *ruv, *rvu;
-            g.arc(u, v, dir, ruv, rvu);
-            if (!g.open(ruv, rvu)) continue;
-            const double e = g.ex[u], rr = *ruv;
-            const double delta = dbits(e) < dbits(rr) ? e : rr;
-            *ruv = __dsub_rn(rr, delta);
-            *rvu = __dadd_rn(*rvu, delta);
-            g.ex[u] = __dsub_rn(e, delta);
-            g.pamt[u] = delta;
-            pd = (signed char)dir;
-            break;
-          }
+        if (g.kind(u) != 0) continue;
+        const int hu = hc[u];
+        long long e = g.ex[u];
+        if (e <= 0 || hu >= g.NH) continue;
+        const long long e0 = e;
+#pragma unroll
+        for (int dir = 0; dir < 6; ++dir) {
+          if (e <= 0) break;
+          int v;
+          if (!g.nbr(u, dir, v)) continue;
+          if (hu != g.height(hc, v) + 1) continue;
+          long long *ruv, *rvu;
+          g.arc(u, v, dir, ruv, rvu);
+          const long long rr = *ruv;
+          if (rr <= 0) continue;
+          const long long delta = e < rr ? e : rr;
+          *ruv = rr - delta;
+          *rvu += delta;
+          e -= delta;
+          if (g.kind(v) == 0) atomicAdd(reinterpret_cast<unsigned long long*>(&g.ex[v]),
+                                        (unsigned long long)delta);
         }
-        g.pdir[u] = pd;
+        if (e != e0)
+          atomicAdd(reinterpret_cast<unsigned long long*>(&g.ex[u]), (unsigned long long)(e - e0));
       }
       __syncthreads();
-      // gather + relabel phase
+      // relabel phase: a node left with excess and no admissible arc moves to 1 + the lowest
+      // neighbour it still has residual capacity to
       int active = 0;
       for (int u = threadIdx.x; u < n; u += blockDim.x) {
         if (g.kind(u) != 0) continue;
-        double e = g.ex[u];
-        for (int dir = 0; dir < 6; ++dir) {
-          int v;
-          if (!g.nbr(u, dir, v)) continue;
-          if (g.pdir[v] == (dir ^ 1) && g.kind(v) == 0) e = __dadd_rn(e, g.pamt[v]);
-        }
-        g.ex[u] = e;
+        const long long e = g.ex[u];
         int hu = hc[u];
         int hnew = hu;
-        if (dbits(e) > 0 && hu < g.NH) {
+        if (e > 0 && hu < g.NH) {
           bool adm = false;
           int mh = 0x7fffffff;
+#pragma unroll
           for (int dir = 0; dir < 6; ++dir) {
             int v;
             if (!g.nbr(u, dir, v)) continue;
-            double *ruv, *rvu;
+            long long *ruv, *rvu;
             g.arc(u, v, dir, ruv, rvu);
             if (!g.open(ruv, rvu)) continue;
             const int hv = g.height(hc, v);
@@ -318,8 +350,8 @@ __global__ void __launch_bounds__(CUT_MAX_THREADS) cut_kernel(const CutArgs a) {
           }
           if (!adm) hnew = mh >= g.NH - 1 ? g.NH : mh + 1;
         }
-        hn[u] = hnew;
-        if (dbits(e) > 0 && hnew < g.NH) active = 1;
+        hn[u] = (HT)hnew;
+        if (e > 0 && hnew < g.NH) active = 1;
       }
       active = __syncthreads_or(active);
       cur ^= 1;
@@ -327,16 +359,20 @@ __global__ void __launch_bounds__(CUT_MAX_THREADS) cut_kernel(const CutArgs a) {
       if (!active) break;
       if (round >= a.round_cap) { capped = true; break; }
       if (round % a.gr_period == 0) {
-        levels += global_relabel(g, g.h[cur], g.front[0], g.front[1], s_cnt);
+        relabel_all();
         __syncthreads();
       }
     }
-    levels += global_relabel(g, g.h[cur], g.front[0], g.front[1], s_cnt);
+    relabel_all();
     __syncthreads();
     if (capped && threadIdx.x == 0) iq_dev_fail(a.status, IQ_ERR_CUTCAP);
   }
 
   if (a.stats && threadIdx.x == 0) {
+    const long long t_end = clock64();
+    atomicAdd(a.stats + ST_CUT_TSETUP, (unsigned long long)(t_setup - t_start));
+    atomicAdd(a.stats + ST_CUT_TGR, (unsigned long long)t_gr);
+    atomicAdd(a.stats + ST_CUT_TROUNDS, (unsigned long long)(t_end - t_setup - t_gr));
     atomicAdd(a.stats + ST_CUT_ROUNDS, (unsigned long long)round);
     atomicAdd(a.stats + ST_CUT_LEVELS, (unsigned long long)levels);
     atomicAdd(a.stats + ST_CUT_CTAS, 1ull);
@@ -344,7 +380,7 @@ __global__ void __launch_bounds__(CUT_MAX_THREADS) cut_kernel(const CutArgs a) {
     atomicMax(a.stats + ST_CUT_MAXLEVELS, (unsigned long long)levels);
   }
   // ---- mask: not sink side ----
-  const int* hc = g.h[cur];
+  const HT* hc = cur ? h1 : h0;
   uint8_t* out = a.out + ((int64_t)y * 6 + s_id) * a.slabmax;
   for (int u = threadIdx.x; u < n; u += blockDim.x) {
     const int k = g.kind(u);
@@ -355,11 +391,18 @@ __global__ void __launch_bounds__(CUT_MAX_THREADS) cut_kernel(const CutArgs a) {
 
 }  // namespace
 
-size_t iq_cut_scratch_bytes(int64_t nodes) {
-  // rf, rb (6n doubles), ex, pamt (2n doubles), two heights and two BFS frontiers (4n ints),
-  // push dir and node info (2n bytes)
-  size_t b = (size_t)nodes * (8 * 8 + 4 * 4 + 2);
+namespace {
+size_t cut_bytes(int64_t nodes, int hbytes) {
+  // residuals (6n int64), excess (n int64), two heights and two BFS frontiers (4n HT), node
+  // info (n bytes)
+  size_t b = (size_t)nodes * (7 * 8 + 4 * hbytes + 1);
   return (b + 255) & ~(size_t)255;
+}
+constexpr int64_t CUT_SHORT_MAX = 32767;  // largest slab with 16-bit heights and indices
+}  // namespace
+
+size_t iq_cut_scratch_bytes(int64_t nodes) {
+  return cut_bytes(nodes, nodes <= CUT_SHORT_MAX ? 2 : 4);
 }
 
 int iq_launch_cut(iq_ctx* ctx, const CutLaunch& L) {
@@ -381,17 +424,18 @@ int iq_launch_cut(iq_ctx* ctx, const CutLaunch& L) {
   a.gr_period = L.gr_period > 0 ? L.gr_period : 32;
   const int64_t nmax = L.slabmax;
   const size_t need = iq_cut_scratch_bytes(nmax);
-  static int smem_limit = -1;
-  if (smem_limit < 0) {
+  const bool narrow = nmax <= CUT_SHORT_MAX;
+  auto kern = narrow ? cut_kernel<short> : cut_kernel<int>;
+  int smem_limit = 0;
+  {
     // dynamic shared memory may use the opt-in maximum minus the kernel's static part
     int dev = 0, v = 0;
     IQ_CUDA_OK(cudaGetDevice(&dev));
     IQ_CUDA_OK(cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
     cudaFuncAttributes fa;
-    IQ_CUDA_OK(cudaFuncGetAttributes(&fa, cut_kernel));
-    const int lim = v - (int)fa.sharedSizeBytes;
-    IQ_CUDA_OK(cudaFuncSetAttribute(cut_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, lim));
-    smem_limit = lim;
+    IQ_CUDA_OK(cudaFuncGetAttributes(&fa, kern));
+    smem_limit = v - (int)fa.sharedSizeBytes;
+    IQ_CUDA_OK(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_limit));
   }
   size_t dyn = 0;
   if ((int64_t)need <= smem_limit) {
@@ -408,7 +452,7 @@ int iq_launch_cut(iq_ctx* ctx, const CutLaunch& L) {
   const int threads = (L.threads == 256 || L.threads == 1024) ? L.threads : 512;
   dim3 grid((unsigned)nslab_max, (unsigned)(L.ntask * L.nreal));
   iq_timer_start(ctx, "graphcut");
-  cut_kernel<<<grid, threads, dyn, ctx->stream>>>(a);
+  kern<<<grid, threads, dyn, ctx->stream>>>(a);
   iq_timer_stop(ctx, "graphcut", 0);
   iq_count(ctx);
   IQ_CUDA_OK(cudaGetLastError());

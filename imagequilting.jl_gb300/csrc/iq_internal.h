@@ -63,7 +63,10 @@ enum IqStat { ST_CUT_ROUNDS = 0, ST_CUT_LEVELS, ST_CUT_CTAS, ST_PICK_ITERS, ST_P
               // and loop, epilogue; the CTA count; cycles inside the MMA issue blocks and the
               // MMAs issued in units of one M=128 N=256 K=8 MMA (x 256)
               ST_TC_LOOP, ST_TC_WFULL, ST_TC_WAFULL, ST_TC_WDONE, ST_TC_PWAIT, ST_TC_PLOOP,
-              ST_TC_EPI, ST_TC_CTAS, ST_TC_ISSUE, ST_TC_MMAU, ST_COUNT };
+              ST_TC_EPI, ST_TC_CTAS, ST_TC_ISSUE, ST_TC_MMAU,
+              // graph cut, SM cycles summed over CTAs: set-up (loads, capacities), push and
+              // relabel rounds, global relabels
+              ST_CUT_TSETUP, ST_CUT_TROUNDS, ST_CUT_TGR, ST_COUNT };
 
 // scratch slot ids
 enum IqSlot {
