@@ -217,7 +217,7 @@ extern "C" int iq_set_option(iq_ctx* ctx, const char* name, int64_t value) {
     return IQ_OK;
   }
   if (!strcmp(name, "corr.engine")) {
-    if (value < 0 || value > 1) return iq_set_error(IQ_ERR_ARG, "corr.engine must be 0 or 1");
+    if (value < 0 || value > 2) return iq_set_error(IQ_ERR_ARG, "corr.engine must be 0, 1 or 2");
     ctx->corr_engine = (int)value;
     return IQ_OK;
   }
@@ -286,12 +286,12 @@ extern "C" int iq_set_ti(iq_ctx* ctx, const void* ti, int32_t dtype, int32_t ndi
   IQ_CUDA_OK(cudaMemcpyAsync(&total, ctx->d_nanii + (d.x + 1) * (d.y + 1) * (d.z + 1) - 1,
                              sizeof(int32_t), cudaMemcpyDeviceToHost, ctx->stream));
   IQ_CUDA_OK(cudaStreamSynchronize(ctx->stream));
-  bool exact = false;
-  if ((rc = iq_tf32_exact(ctx, ctx->d_ti, n, exact))) return rc;
+  IqValueStats st;
+  if ((rc = iq_value_stats(ctx, ctx->d_ti, n, st))) return rc;
   ctx->ti = d;
   ctx->ndim = ndim;
   ctx->ti_nan = total;
-  ctx->ti_tf32 = exact;
+  ctx->ti_stats = st;
   ctx->has_ti = true;
   return IQ_OK;
 }
@@ -337,7 +337,7 @@ extern "C" int iq_fastdistance(iq_ctx* ctx, const int64_t* tilesize, int32_t ntm
       for (int d = 0; d < 3; ++d) { blo[d] = mn[d]; bhi[d] = mx[d] + 1; }
     }
   }
-  const bool use_tc = ctx->corr_engine == 1 && boxmask && K > 0;
+  const bool use_tc = ctx->corr_engine >= 1 && boxmask && K > 0;
   // A2 by integral image when the mask is all ones, else direct
   const bool full = K == T;
   const int rt = iq_register_tile(ntmpl);
@@ -361,15 +361,20 @@ extern "C" int iq_fastdistance(iq_ctx* ctx, const int64_t* tilesize, int32_t ntm
   std::vector<TcCol> cols;
   std::vector<uint32_t> stw;
   if (use_tc) {
-    bool exact = false;
-    if (ctx->ti_tf32 && (rc = iq_tf32_exact(ctx, d_tmpl, T * ntmpl, exact))) return rc;
+    IqValueStats tstats;
+    if ((rc = iq_value_stats(ctx, d_tmpl, T * ntmpl, tstats))) return rc;
     TcBox box0;
     for (int d = 0; d < 3; ++d) { box0.lo[d] = (int32_t)blo[d]; box0.hi[d] = (int32_t)bhi[d]; }
     TcStages stg;
     iq_tc_stages(t, &box0, 1, stg);
-    const size_t ns = stg.word.size();
-    stw.resize(2 * ns);
+    const size_t ns = stg.word.size(), n16 = stg.w16a.size();
+    stw.resize(2 * ns + 3 * n16);
     for (size_t e = 0; e < ns; ++e) { stw[e] = stg.word[e]; stw[ns + e] = stg.prefix[e]; }
+    for (size_t e = 0; e < n16; ++e) {
+      stw[2 * ns + e] = stg.w16a[e];
+      stw[2 * ns + n16 + e] = stg.w16b[e];
+      stw[2 * ns + 2 * n16 + e] = stg.pre16[e];
+    }
     for (int32_t c0 = 0; c0 < ntmpl; c0 += IQ_TC_MAXN) {
       const int nb = std::min<int32_t>(IQ_TC_MAXN, ntmpl - c0);
       const int Np = (nb + 15) / 16 * 16;
@@ -379,7 +384,8 @@ extern "C" int iq_fastdistance(iq_ctx* ctx, const int64_t* tilesize, int32_t ntm
     }
     uint32_t* d_st = (uint32_t*)iq_scratch(ctx, S_TCSTAGE, sizeof(uint32_t) * std::max<size_t>(stw.size(), 1));
     TcCol* d_cols = (TcCol*)iq_scratch(ctx, S_TCCOLS, sizeof(TcCol) * cols.size());
-    void* d_B = iq_scratch(ctx, S_TCB, (size_t)std::max<int64_t>(stg.nsteps, 1) * 64 * IQ_TC_MAXN);
+    void* d_B = iq_scratch(ctx, S_TCB, (size_t)std::max<int64_t>(std::max(stg.nsteps, stg.nsteps16), 1) *
+                                          64 * IQ_TC_MAXN);
     if (!d_st || !d_cols || !d_B) return IQ_ERR_ALLOC;
     IQ_CUDA_OK(cudaMemcpyAsync(d_st, stw.data(), sizeof(uint32_t) * stw.size(), cudaMemcpyHostToDevice, ctx->stream));
     IQ_CUDA_OK(cudaMemcpyAsync(d_cols, cols.data(), sizeof(TcCol) * cols.size(), cudaMemcpyHostToDevice, ctx->stream));
@@ -391,8 +397,10 @@ extern "C" int iq_fastdistance(iq_ctx* ctx, const int64_t* tilesize, int32_t ntm
       L.nbox = 1; L.box[0] = box0;
       L.disabled = d_dis;
       L.stage_word = d_st; L.stage_prefix = d_st + ns; L.nstage = (int)ns; L.nsteps = stg.nsteps;
+      L.stage16 = d_st + 2 * ns; L.nstage16 = (int)n16; L.nsteps16 = stg.nsteps16;
       L.grid = d_tmpl; L.grid_dims = t; L.cols = d_cols + col0; L.N = (nb + 15) / 16 * 16;
-      L.B = d_B; L.exact = exact; L.flops = 2.0 * (double)P * (double)K * nb;
+      L.B = d_B; L.img_stats = ctx->ti_stats; L.tmpl_stats = tstats;
+      L.flops = 2.0 * (double)P * (double)K * nb;
       if ((rc = iq_launch_corr_tc(ctx, L))) return rc;
       col0 += L.N;
     }

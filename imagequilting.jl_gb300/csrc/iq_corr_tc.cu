@@ -42,9 +42,12 @@
 // the epilogue. Every mbarrier wait is bounded in time: on expiry the kernel records
 // IQ_ERR_TIMEOUT, stops issuing work, waits (bounded) for what it issued, frees its TMEM and
 // returns.
+#include <cuda_fp16.h>
 #include <float.h>
 
 #include <algorithm>
+#include <cmath>
+#include <cstring>
 
 #include "iq_internal.h"
 
@@ -56,11 +59,25 @@ constexpr int TC_PTHREADS = 32 * TC_PWARPS;
 constexpr int TC_MB = 2;     // 128-position blocks per CTA
 constexpr int TC_NST = 3;    // pipeline stages
 constexpr int TC_STEPS = 3;  // 8-offset K-steps per stage (24 x-offsets)
-constexpr int TC_NQ = 32 * TC_MB + 2 * (TC_STEPS - 1);  // 128-byte blocks of one image
-constexpr int TC_UPT = (8 * TC_NQ + TC_PTHREADS - 1) / TC_PTHREADS;  // image rows per thread
-constexpr int TC_GROUP = 8 * TC_STEPS;                  // x-offsets per stage
+constexpr int TC_NQ = 32 * TC_MB + 2 * (TC_STEPS - 1);  // 128-byte blocks of one TF32 image
+constexpr int TC_GROUP = 8 * TC_STEPS;                  // x-offsets per row entry
 constexpr unsigned long long TC_WAIT_NS = 2000000000ull; // bound of every wait
-constexpr int TC_SMW = 1024;  // stage words and prefixes kept in shared memory
+constexpr int TC_SMW = 512;   // stage words and prefixes kept in shared memory
+// FP16 form: a stage is two row entries; an image row holds 8 halves, a row image has
+// 16 * TC_MB + 3 blocks of 128 bytes (the last one only read by a K-step's unused half)
+constexpr int F_CH = 3;                       // 8-offset chunks per row entry
+constexpr int F_NQ = 16 * TC_MB + F_CH;       // blocks of one FP16 row image
+constexpr int F_IMG = F_NQ * 128;             // bytes of one FP16 row image
+constexpr int F_ROWU = 8 * F_NQ;              // image rows of one row entry
+
+// A region of a stage: TF32 -> hi and lo images of one row entry; FP16 -> hi images of two
+// row entries, then their lo images
+template <bool F16> constexpr int a_region() { return F16 ? 4 * F_IMG : 2 * TC_NQ * 128; }
+template <bool F16> constexpr int stage_units() { return F16 ? 2 * F_ROWU : 8 * TC_NQ; }
+template <bool F16> constexpr int upt() {
+  return (stage_units<F16>() + TC_PTHREADS - 1) / TC_PTHREADS;  // image rows per thread
+}
+template <bool F16> constexpr int vpu() { return F16 ? 8 : 4; }  // values per image row
 
 struct TcArgs {
   const float* img;
@@ -73,12 +90,15 @@ struct TcArgs {
   TcBox box[IQ_TC_MAXBOX];
   const uint8_t* disabled;
   const uint32_t* word;
+  const uint32_t* wordb;      // FP16 form: second row entry of each stage (0 = none)
   const uint32_t* prefix;
   int nstage;
   const char* B;
   const TcCol* cols;
   int N;
   int exact;
+  float scale_a;              // FP16 form: 2^-kA applied to the image values
+  float ab2;                  // 2 * 2^(kA + kB): D = |A2 + B2 - ab2 * acc|
   uint32_t tmem_cols;
   int* status;
   unsigned long long* stats;  // profiling counters (nullable)
@@ -257,52 +277,116 @@ __global__ void tc_pack_kernel(const PackArgs p) {
 
 // ---- the GEMM ----
 struct StageInfo {
-  int64_t e0;   // TI index of image row 0
-  int nunits;   // 16-byte image rows to write
-  uint32_t smask;
-  uint32_t pre;
+  int64_t e0a, e0b;  // TI index of image row 0 of the stage's row entries
+  uint32_t ma, mb;   // their chunk masks (mb = 0: no second row entry)
+  uint32_t pre;      // K-steps before the stage
+  int nunits;        // 16-byte image rows to write
 };
 
-// stage e's word and prefix: from the shared-memory copy (first TC_SMW stages) or global
+// stage e's words and prefix: from the shared-memory copy (first TC_SMW stages) or global
 __device__ __forceinline__ uint32_t stage_word(const TcArgs& a, const uint32_t* sw, int e) {
   return e < TC_SMW ? sw[e] : __ldg(a.word + e);
+}
+__device__ __forceinline__ uint32_t stage_wordb(const TcArgs& a, const uint32_t* sw, int e) {
+  return e < TC_SMW ? sw[2 * TC_SMW + e] : __ldg(a.wordb + e);
 }
 __device__ __forceinline__ uint32_t stage_pre(const TcArgs& a, const uint32_t* sw, int e) {
   return e < TC_SMW ? sw[TC_SMW + e] : __ldg(a.prefix + e);
 }
 
+__device__ __forceinline__ int64_t row_e0(const TcArgs& a, uint32_t w, int64_t p0) {
+  const int ky = (int)(w & 1023u), kz = (int)((w >> 10) & 1023u), g = (int)((w >> 20) & 63u);
+  return p0 + (int64_t)TC_GROUP * g + a.ix * (ky + a.iy * (int64_t)kz);
+}
+
+// K-steps of a stage: TF32 -> one per active 8-offset step; FP16 -> the active 8-offset
+// chunks of the two row entries taken in pairs
+template <bool F16>
+__device__ __forceinline__ int stage_ksteps(uint32_t ma, uint32_t mb) {
+  return F16 ? (__popc(ma) + __popc(mb) + 1) >> 1 : __popc(ma);
+}
+
+template <bool F16>
 __device__ __forceinline__ StageInfo stage_info(const TcArgs& a, const uint32_t* sw, int e,
                                                 int64_t p0) {
   StageInfo s;
   const uint32_t w = stage_word(a, sw, e);
   s.pre = stage_pre(a, sw, e);
-  const int ky = (int)(w & 1023u), kz = (int)((w >> 10) & 1023u), g = (int)((w >> 20) & 63u);
-  s.smask = w >> 26;
-  const int smax = 31 - __clz((int)s.smask);
-  s.e0 = p0 + (int64_t)TC_GROUP * g + a.ix * (ky + a.iy * (int64_t)kz);
-  s.nunits = 8 * (32 * TC_MB + 2 * smax);
+  s.ma = w >> 26;
+  s.e0a = row_e0(a, w, p0);
+  if (F16) {
+    const uint32_t wb = stage_wordb(a, sw, e);
+    s.mb = wb >> 26;
+    s.e0b = s.mb ? row_e0(a, wb, p0) : s.e0a;
+    s.nunits = (s.mb ? 2 : 1) * F_ROWU;
+  } else {
+    s.mb = 0;
+    s.e0b = s.e0a;
+    const int smax = 31 - __clz((int)s.ma);
+    s.nunits = 8 * (32 * TC_MB + 2 * smax);
+  }
   return s;
 }
 
+// image row u of a stage: TF32 -> TI[e0 + 4 (u / 8) + u % 8 + 0..3]; FP16 -> row entry
+// u / F_ROWU, TI[e0 + 8 (v / 8) + v % 8 + 0..7] with v = u % F_ROWU
+template <bool F16>
+__device__ __forceinline__ int64_t unit_base(const StageInfo& s, int u) {
+  if (F16) {
+    const bool second = u >= F_ROWU;
+    const int v = second ? u - F_ROWU : u;
+    return (second ? s.e0b : s.e0a) + 8 * (v >> 3) + (v & 7);
+  }
+  return s.e0a + 4 * (u >> 3) + (u & 7);
+}
+
+template <bool F16>
 __device__ __forceinline__ void stage_load(const TcArgs& a, const StageInfo& s, int ptid,
-                                           float (&v)[TC_UPT][4]) {
+                                           float (&v)[upt<F16>()][vpu<F16>()]) {
 #pragma unroll
-  for (int i = 0; i < TC_UPT; ++i) {
+  for (int i = 0; i < upt<F16>(); ++i) {
     const int u = ptid + i * TC_PTHREADS;
     if (u < s.nunits) {
-      const int64_t base = s.e0 + 4 * (u >> 3) + (u & 7);
+      const int64_t base = unit_base<F16>(s, u);
 #pragma unroll
-      for (int c = 0; c < 4; ++c) v[i][c] = __ldg(a.img + min(base + c, a.nimg - 1));
+      for (int c = 0; c < vpu<F16>(); ++c) v[i][c] = __ldg(a.img + min(base + c, a.nimg - 1));
     }
   }
 }
 
+// v * scale = hi + lo, both FP16 (round to nearest even)
+__device__ __forceinline__ void f16_split(float v, float scale, uint16_t& hi, uint16_t& lo) {
+  const float x = v * scale;  // a power of two: exact
+  const __half h = __float2half_rn(x);
+  const __half l = __float2half_rn(__fsub_rn(x, __half2float(h)));
+  hi = __half_as_ushort(h);
+  lo = __half_as_ushort(l);
+}
+
+__device__ __forceinline__ void mma_f16(uint32_t d, uint64_t a, uint64_t b, uint32_t idesc,
+                                        uint32_t acc) {
+  asm volatile(
+      "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(d),
+      "l"(a), "l"(b), "r"(idesc), "r"(acc));
+}
+
+// chunk idx of an FP16 stage: byte offset of its core-matrix column inside the A hi region
+// (row entry a at 0, row entry b at F_IMG; chunk c is c blocks further)
+__device__ __forceinline__ uint32_t f16_chunk_off(uint32_t ma, uint32_t mb, int idx) {
+  const int na = __popc(ma);
+  return idx < na ? 128u * (uint32_t)nth_bit(ma, idx)
+                  : (uint32_t)F_IMG + 128u * (uint32_t)nth_bit(mb, idx - na);
+}
+
+template <bool F16>
 __global__ void __launch_bounds__(TC_THREADS, 1) corr_tc_kernel(const TcArgs a) {
   extern __shared__ __align__(1024) unsigned char smem[];
   __shared__ uint32_t s_tmem;
+  constexpr int UPT = upt<F16>(), VPU = vpu<F16>();
   const int N = a.N;
   const uint32_t bbytes = (uint32_t)TC_STEPS * 64u * (uint32_t)N;
-  const uint32_t stage_bytes = bbytes + 2u * TC_NQ * 128u;
+  const uint32_t stage_bytes = bbytes + (uint32_t)a_region<F16>();
   unsigned char* colbase = smem + TC_NST * stage_bytes;
   float** s_out = reinterpret_cast<float**>(colbase);
   unsigned** s_mmp = reinterpret_cast<unsigned**>(colbase + 8 * N);
@@ -312,7 +396,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1) corr_tc_kernel(const TcArgs a) 
   int* s_box = reinterpret_cast<int*>(colbase + 28 * N);
   float* s_a2 = reinterpret_cast<float*>(colbase + 32 * N);  // [box][128 * TC_MB positions]
   uint64_t* bars = reinterpret_cast<uint64_t*>(s_a2 + IQ_TC_MAXBOX * 128 * TC_MB);
-  uint32_t* s_stage = reinterpret_cast<uint32_t*>(bars + 3 * TC_NST + 1);  // words, prefixes
+  // stage words, prefixes, second words (FP16)
+  uint32_t* s_stage = reinterpret_cast<uint32_t*>(bars + 3 * TC_NST + 1);
   // full[NST] (B copies), done[NST] (MMA commits), afull[NST] (A images), fin
   const uint32_t bar_full = smem_u32(bars), bar_done = bar_full + 8 * TC_NST,
                  bar_afull = bar_full + 16 * TC_NST, bar_fin = bar_full + 24 * TC_NST;
@@ -331,6 +416,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) corr_tc_kernel(const TcArgs a) 
   for (int e = tid; e < a.nstage && e < TC_SMW; e += TC_THREADS) {
     s_stage[e] = __ldg(a.word + e);
     s_stage[TC_SMW + e] = __ldg(a.prefix + e);
+    if (F16) s_stage[2 * TC_SMW + e] = __ldg(a.wordb + e);
   }
   if (tid == 0) {
     for (int i = 0; i < 2 * TC_NST; ++i) mbar_init(bar_full + 8 * i, 1);
@@ -353,19 +439,19 @@ __global__ void __launch_bounds__(TC_THREADS, 1) corr_tc_kernel(const TcArgs a) 
   const int64_t zbase = z * a.ix * a.iy;
   const int64_t p0 = zbase + (int64_t)(blockIdx.x % a.bpp) * (128 * TC_MB);
   const uint32_t sbase = smem_u32(smem);
-  const uint32_t idesc = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(N >> 3) << 17) |
-                         ((128u >> 4) << 24);
+  // D F32; A, B: TF32 (2) or F16 (0); N >> 3 at bit 17, M >> 4 at bit 24
+  const uint32_t ab_fmt = F16 ? 0u : 2u;
+  const uint32_t idesc = (1u << 4) | (ab_fmt << 7) | (ab_fmt << 10) |
+                         ((uint32_t)(N >> 3) << 17) | ((128u >> 4) << 24);
 
   int fail = 0;  // this thread saw a wait expire
   int aborted = 0;
   if (warp == 0) {
     if (lane == 0) {
-      // ---- copies and MMAs ----
-      // The issue rate of one thread bounds the tensor pipe, so the loop is lean: descriptors
-      // of buffer 0 are built once (a buffer or K-step is an offset added to the start field),
-      // the K-step and M-block loops are unrolled and the stage words sit in shared memory.
-      const uint64_t dA0 = make_desc(sbase + bbytes, 128u, 256u);
-      const uint64_t dL0 = make_desc(sbase + bbytes + TC_NQ * 128u, 128u, 256u);
+      // ---- MMAs ----
+      // The issue rate of one thread bounds the tensor pipe, so the loop is lean: the B
+      // descriptor of buffer 0 is built once (a buffer or K-step is an offset added to the
+      // start field), the loops are unrolled and the stage words sit in shared memory.
       const uint64_t dB0 = make_desc(sbase, 16u * N, 128u);
       const uint32_t dbuf = stage_bytes >> 4, dstep = 2u * N;  // buffer, K-step B (16-byte units)
       int e = 0;
@@ -383,34 +469,64 @@ __global__ void __launch_bounds__(TC_THREADS, 1) corr_tc_kernel(const TcArgs a) 
         }
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
         const long long t_i0 = prof ? clock64() : 0;
-        const uint32_t smask = stage_word(a, s_stage, e) >> 26;
-        const uint32_t nact = (uint32_t)__popc(smask);
-        const uint64_t dA = dA0 + (uint64_t)(b * dbuf), dL = dL0 + (uint64_t)(b * dbuf);
+        const uint32_t ma = stage_word(a, s_stage, e) >> 26;
+        const uint32_t mb2 = F16 ? stage_wordb(a, s_stage, e) >> 26 : 0u;
+        const uint32_t nks = (uint32_t)stage_ksteps<F16>(ma, mb2);
+        const uint32_t sA = sbase + b * stage_bytes + bbytes;  // A region of this buffer
         const uint64_t dB = dB0 + (uint64_t)(b * dbuf);
-        uint32_t act = 0;
         uint32_t acc = e > 0 ? 1u : 0u;
+        if (F16) {
+          const int total = __popc(ma) + __popc(mb2);
 #pragma unroll
-        for (int s = 0; s < TC_STEPS; ++s) {
-          if (smask >> s & 1u) {
-            const uint64_t bh = dB + (uint64_t)(act * dstep), bl = dB + (uint64_t)((nact + act) * dstep);
+          for (int t = 0; t < TC_STEPS; ++t) {
+            if (t < (int)nks) {
+              const uint64_t bh = dB + (uint64_t)(t * dstep), bl = dB + (uint64_t)((nks + t) * dstep);
+              // two 8-offset chunks X, Y: the descriptor's leading offset joins them (the
+              // unused half of an odd last K-step reads the next block, its B half is zero)
+              const uint32_t ox = f16_chunk_off(ma, mb2, 2 * t);
+              const uint32_t lbo = 2 * t + 1 < total ? f16_chunk_off(ma, mb2, 2 * t + 1) - ox : 128u;
 #pragma unroll
-            for (int mb = 0; mb < TC_MB; ++mb) {
-              const uint32_t ao = 8u * (32u * mb + 2u * s);  // 128 (32 mb + 2 s) bytes
-              const uint32_t d = tmem + (uint32_t)(mb * N);
-              mma_tf32(d, dA + ao, bh, idesc, acc);
-              if (!a.exact) {
-                mma_tf32(d, dA + ao, bl, idesc, 1u);
-                mma_tf32(d, dL + ao, bh, idesc, 1u);
+              for (int mb = 0; mb < TC_MB; ++mb) {
+                const uint32_t ao = ox + 128u * 16u * mb;
+                const uint32_t d = tmem + (uint32_t)(mb * N);
+                const uint64_t dah = make_desc(sA + ao, lbo, 128u);
+                mma_f16(d, dah, bh, idesc, acc);
+                if (!a.exact) {
+                  const uint64_t dal = make_desc(sA + 2 * F_IMG + ao, lbo, 128u);
+                  mma_f16(d, dah, bl, idesc, 1u);
+                  mma_f16(d, dal, bh, idesc, 1u);
+                }
               }
+              acc = 1u;
             }
-            ++act;
-            acc = 1u;
+          }
+        } else {
+          const uint64_t dA = make_desc(sA, 128u, 256u);
+          const uint64_t dL = make_desc(sA + TC_NQ * 128u, 128u, 256u);
+          uint32_t act = 0;
+#pragma unroll
+          for (int s = 0; s < TC_STEPS; ++s) {
+            if (ma >> s & 1u) {
+              const uint64_t bh = dB + (uint64_t)(act * dstep), bl = dB + (uint64_t)((nks + act) * dstep);
+#pragma unroll
+              for (int mb = 0; mb < TC_MB; ++mb) {
+                const uint32_t ao = 8u * (32u * mb + 2u * s);  // 128 (32 mb + 2 s) bytes
+                const uint32_t d = tmem + (uint32_t)(mb * N);
+                mma_tf32(d, dA + ao, bh, idesc, acc);
+                if (!a.exact) {
+                  mma_tf32(d, dA + ao, bl, idesc, 1u);
+                  mma_tf32(d, dL + ao, bh, idesc, 1u);
+                }
+              }
+              ++act;
+              acc = 1u;
+            }
           }
         }
         mma_commit(bar_done + 8 * b);
         if (prof) {
           t_issue += clock64() - t_i0;
-          mmau += (unsigned long long)nact * TC_MB * (a.exact ? 1 : 3) * N;
+          mmau += (unsigned long long)nks * TC_MB * (a.exact ? 1 : 3) * N;
         }
         if (++b == TC_NST) { b = 0; par ^= 1u; }
       }
@@ -431,15 +547,15 @@ __global__ void __launch_bounds__(TC_THREADS, 1) corr_tc_kernel(const TcArgs a) 
   } else {
     // ---- A images (TI values loaded two stages ahead, in two register sets) ----
     const int ptid = tid - 32;
-    float va[TC_UPT][4], vb[TC_UPT][4];
+    float va[UPT][VPU], vb[UPT][VPU];
     StageInfo sa{}, sbi{};
     if (a.nstage > 0) {
-      sa = stage_info(a, s_stage, 0, p0);
-      stage_load(a, sa, ptid, va);
+      sa = stage_info<F16>(a, s_stage, 0, p0);
+      stage_load<F16>(a, sa, ptid, va);
     }
     if (a.nstage > 1) {
-      sbi = stage_info(a, s_stage, 1, p0);
-      stage_load(a, sbi, ptid, vb);
+      sbi = stage_info<F16>(a, s_stage, 1, p0);
+      stage_load<F16>(a, sbi, ptid, vb);
     }
     const bool prof = a.stats != nullptr && warp == 1 && lane == 0;
     long long t_wait = 0;
@@ -447,26 +563,43 @@ __global__ void __launch_bounds__(TC_THREADS, 1) corr_tc_kernel(const TcArgs a) 
     // write stage e's images from v; false when the wait for the buffer gave up
     const bool copier = warp == 1 && lane == 0;  // issues the B copies
     int ncopied = 0;
-    auto build = [&](int e, const StageInfo& si, float (&v)[TC_UPT][4]) -> bool {
+    auto build = [&](int e, const StageInfo& si, float (&v)[UPT][VPU]) -> bool {
       const int b = e % TC_NST;
       const uint32_t use = (uint32_t)(e / TC_NST);
       const bool ok = use == 0 || mbar_wait_t(bar_done + 8 * b, (use - 1) & 1u, prof, t_wait);
       if (__any_sync(0xffffffffu, !ok)) return false;  // the warp leaves together
       if (copier) {
-        const uint32_t bytes = (uint32_t)__popc(si.smask) * (a.exact ? 32u : 64u) * (uint32_t)N;
+        const uint32_t bytes =
+            (uint32_t)stage_ksteps<F16>(si.ma, si.mb) * (a.exact ? 32u : 64u) * (uint32_t)N;
         bulk_g2s(sbase + b * stage_bytes, a.B + (size_t)si.pre * 64 * N, bytes, bar_full + 8 * b);
         ncopied = e + 1;
       }
-      const uint32_t sa_hi = sbase + b * stage_bytes + bbytes, sa_lo = sa_hi + TC_NQ * 128u;
+      const uint32_t sA = sbase + b * stage_bytes + bbytes;
 #pragma unroll
-      for (int i = 0; i < TC_UPT; ++i) {
+      for (int i = 0; i < UPT; ++i) {
         const int u = ptid + i * TC_PTHREADS;
         if (u < si.nunits) {
-          uint32_t h[4], l[4];
+          if (F16) {
+            uint32_t h[4], l[4];
 #pragma unroll
-          for (int c = 0; c < 4; ++c) tf32_split(v[i][c], h[c], l[c]);
-          st_shared_v4(sa_hi + 16u * u, h[0], h[1], h[2], h[3]);
-          if (!a.exact) st_shared_v4(sa_lo + 16u * u, l[0], l[1], l[2], l[3]);
+            for (int c = 0; c < 4; ++c) {
+              uint16_t h0, l0, h1, l1;
+              f16_split(v[i][2 * c], a.scale_a, h0, l0);
+              f16_split(v[i][2 * c + 1], a.scale_a, h1, l1);
+              h[c] = (uint32_t)h0 | ((uint32_t)h1 << 16);
+              l[c] = (uint32_t)l0 | ((uint32_t)l1 << 16);
+            }
+            const bool second = u >= F_ROWU;
+            const uint32_t off = (second ? (uint32_t)F_IMG : 0u) + 16u * (uint32_t)(second ? u - F_ROWU : u);
+            st_shared_v4(sA + off, h[0], h[1], h[2], h[3]);
+            if (!a.exact) st_shared_v4(sA + 2 * F_IMG + off, l[0], l[1], l[2], l[3]);
+          } else {
+            uint32_t h[4], l[4];
+#pragma unroll
+            for (int c = 0; c < 4; ++c) tf32_split(v[i][c], h[c], l[c]);
+            st_shared_v4(sA + 16u * u, h[0], h[1], h[2], h[3]);
+            if (!a.exact) st_shared_v4(sA + TC_NQ * 128u + 16u * u, l[0], l[1], l[2], l[3]);
+          }
         }
       }
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
@@ -477,14 +610,14 @@ __global__ void __launch_bounds__(TC_THREADS, 1) corr_tc_kernel(const TcArgs a) 
     for (int e = 0; e < a.nstage; e += 2) {
       if (!build(e, sa, va)) { fail = 1; break; }
       if (e + 2 < a.nstage) {
-        sa = stage_info(a, s_stage, e + 2, p0);
-        stage_load(a, sa, ptid, va);
+        sa = stage_info<F16>(a, s_stage, e + 2, p0);
+        stage_load<F16>(a, sa, ptid, va);
       }
       if (e + 1 >= a.nstage) break;
       if (!build(e + 1, sbi, vb)) { fail = 1; break; }
       if (e + 3 < a.nstage) {
-        sbi = stage_info(a, s_stage, e + 3, p0);
-        stage_load(a, sbi, ptid, vb);
+        sbi = stage_info<F16>(a, s_stage, e + 3, p0);
+        stage_load<F16>(a, sbi, ptid, vb);
       }
     }
     if (copier)  // the last copies have landed (bounded waits) before the buffers go away
@@ -550,7 +683,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) corr_tc_kernel(const TcArgs a) 
               df = __int_as_float(0x7F800000);
             } else {
               const float s2 = __fadd_rn(s_a2[s_box[n] * 128 * TC_MB + m], s_b2[n]);
-              df = fabsf(__fmaf_rn(-2.f, __uint_as_float(r[j]), s2));
+              df = fabsf(__fmaf_rn(-a.ab2, __uint_as_float(r[j]), s2));
             }
             o[pout] = df;
             mnb = __float_as_uint(df);
@@ -583,17 +716,96 @@ __global__ void __launch_bounds__(TC_THREADS, 1) corr_tc_kernel(const TcArgs a) 
   }
 }
 
+template <bool F16>
 size_t tc_smem_bytes(int N) {
-  return (size_t)TC_NST * ((size_t)TC_STEPS * 64 * N + 2 * TC_NQ * 128) + 32 * (size_t)N +
-         4 * IQ_TC_MAXBOX * 128 * TC_MB + 8 * (3 * TC_NST + 1) + 8 * TC_SMW;
+  return (size_t)TC_NST * ((size_t)TC_STEPS * 64 * N + a_region<F16>()) + 32 * (size_t)N +
+         4 * IQ_TC_MAXBOX * 128 * TC_MB + 8 * (3 * TC_NST + 1) + 12 * TC_SMW;
 }
 
-__global__ void tf32_check_kernel(const float* __restrict__ d, int64_t n, int* flag) {
-  unsigned bad = 0;
+// [largest magnitude bits, smallest exponent + 256 of a nonzero magnitude, OR of the low 13
+// mantissa bits] over the finite values
+__global__ void value_stats_kernel(const float* __restrict__ d, int64_t n, unsigned* out) {
+  unsigned amax = 0, minx = 0xFFFFFFFFu, low = 0;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
-       i += (int64_t)gridDim.x * blockDim.x)
-    bad |= __float_as_uint(d[i]) & 0x1FFFu;
-  if (__syncthreads_or(bad != 0) && threadIdx.x == 0) atomicOr(flag, 1);
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const unsigned b = __float_as_uint(d[i]) & 0x7FFFFFFFu;
+    if (b >= 0x7F800000u) continue;  // NaN, Inf
+    amax = max(amax, b);
+    if (b) {
+      const unsigned ex = b >> 23;  // biased exponent; 0 for subnormals
+      minx = min(minx, (ex ? ex : 1u) - 127u + 256u);
+    }
+    low |= b & 0x1FFFu;
+  }
+  amax = __reduce_max_sync(0xffffffffu, amax);
+  minx = __reduce_min_sync(0xffffffffu, minx);
+  low = __reduce_or_sync(0xffffffffu, low);
+  if ((threadIdx.x & 31) == 0) {
+    atomicMax(out, amax);
+    atomicMin(out + 1, minx);
+    atomicOr(out + 2, low);
+  }
+}
+
+// ---- packing of the templates, FP16 form ----
+struct Pack16Args {
+  const float* grid;
+  int64_t gx, gy, tx;
+  const TcCol* cols;
+  int N;
+  const uint32_t* wa;
+  const uint32_t* wb;
+  const uint32_t* prefix;
+  int nstage;
+  TcBox box[IQ_TC_MAXBOX];
+  float scale_b;  // 2^-kB
+  char* B;
+};
+
+// Stage e occupies prefix[e] * 64N bytes: the FP16 high halves of its nks K-steps (32N bytes
+// each: chunk half jj = 0..1, template n, 8 halves), then the low halves. K-step t joins the
+// stage's active chunks 2t and 2t + 1 (row entry a's chunks first); a missing second chunk
+// is zero.
+__global__ void tc_pack16_kernel(const Pack16Args p) {
+  const int N = p.N;
+  for (int e = blockIdx.y; e < p.nstage; e += gridDim.y) {
+    const uint32_t wa = p.wa[e], wb = p.wb[e];
+    const uint32_t ma = wa >> 26, mb = wb >> 26;
+    const int na = __popc(ma), total = na + __popc(mb);
+    const int nks = (total + 1) >> 1;
+    const int units = nks * 2 * N;
+    char* base = p.B + (size_t)p.prefix[e] * 64 * N;
+    for (int u = blockIdx.x * blockDim.x + threadIdx.x; u < units; u += gridDim.x * blockDim.x) {
+      const int t = u / (2 * N), rem = u - t * 2 * N;
+      const int jj = rem / N, n = rem - jj * N;
+      const int idx = 2 * t + jj;
+      const TcCol col = p.cols[n];
+      uint32_t h[4] = {0, 0, 0, 0}, l[4] = {0, 0, 0, 0};
+      if (idx < total && col.src >= 0) {
+        const bool second = idx >= na;
+        const uint32_t w = second ? wb : wa;
+        const int c = second ? nth_bit(mb, idx - na) : nth_bit(ma, idx);
+        const int ky = (int)(w & 1023u), kz = (int)((w >> 10) & 1023u), g = (int)((w >> 20) & 63u);
+        const TcBox bx = p.box[col.box];
+        const int64_t kx0 = (int64_t)TC_GROUP * g + 8 * c;
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+          const int64_t kx = kx0 + q;
+          float v = 0.f;
+          if (kx < p.tx && !in_box(bx, kx, ky, kz))
+            v = p.grid[col.src + kx + p.gx * (ky + p.gy * (int64_t)kz)];
+          uint16_t hh, ll;
+          f16_split(v, p.scale_b, hh, ll);
+          h[q >> 1] |= (uint32_t)hh << (16 * (q & 1));
+          l[q >> 1] |= (uint32_t)ll << (16 * (q & 1));
+        }
+      }
+      uint4* hi = reinterpret_cast<uint4*>(base + (size_t)t * 32 * N + (size_t)rem * 16);
+      uint4* lo = reinterpret_cast<uint4*>(base + (size_t)(nks + t) * 32 * N + (size_t)rem * 16);
+      *hi = make_uint4(h[0], h[1], h[2], h[3]);
+      *lo = make_uint4(l[0], l[1], l[2], l[3]);
+    }
+  }
 }
 
 }  // namespace
@@ -623,23 +835,55 @@ void iq_tc_stages(Dim3 tile, const TcBox* boxes, int nbox, TcStages& out) {
         out.prefix.push_back((uint32_t)out.nsteps);
         out.nsteps += __builtin_popcount(smask);
       }
+  // FP16 form: consecutive row entries in pairs
+  out.w16a.clear();
+  out.w16b.clear();
+  out.pre16.clear();
+  out.nsteps16 = 0;
+  for (size_t i = 0; i < out.word.size(); i += 2) {
+    const uint32_t wa = out.word[i], wb = i + 1 < out.word.size() ? out.word[i + 1] : 0u;
+    out.w16a.push_back(wa);
+    out.w16b.push_back(wb);
+    out.pre16.push_back((uint32_t)out.nsteps16);
+    out.nsteps16 += (__builtin_popcount(wa >> 26) + __builtin_popcount(wb >> 26) + 1) / 2;
+  }
 }
 
-int iq_tf32_exact(iq_ctx* ctx, const float* d, int64_t n, bool& exact) {
-  exact = false;
-  int* flag = (int*)iq_scratch(ctx, S_TCFLAG, sizeof(int));
-  if (!flag) return IQ_ERR_ALLOC;
-  IQ_CUDA_OK(cudaMemsetAsync(flag, 0, sizeof(int), ctx->stream));
+int IqValueStats::maxexp() const { return amax > 0.f ? std::ilogb(amax) : 0; }
+bool IqValueStats::fp16_range() const { return !(amax > 0.f) || minexp >= maxexp() - 17; }
+
+IqValueStats iq_host_stats(const float* v, int64_t n) {
+  IqValueStats s;
+  for (int64_t i = 0; i < n; ++i) {
+    if (!std::isfinite(v[i])) continue;
+    const float a = std::fabs(v[i]);
+    uint32_t b;
+    memcpy(&b, &a, 4);
+    s.amax = std::max(s.amax, a);
+    if (a > 0.f) s.minexp = std::min(s.minexp, std::max(std::ilogb(a), -126));
+    if (b & 0x1FFFu) s.narrow = false;
+  }
+  return s;
+}
+
+int iq_value_stats(iq_ctx* ctx, const float* d, int64_t n, IqValueStats& out) {
+  out = IqValueStats();
+  unsigned* buf = (unsigned*)iq_scratch(ctx, S_TCFLAG, 3 * sizeof(unsigned));
+  if (!buf) return IQ_ERR_ALLOC;
+  const unsigned init[3] = {0u, 0xFFFFFFFFu, 0u};
+  IQ_CUDA_OK(cudaMemcpyAsync(buf, init, sizeof(init), cudaMemcpyHostToDevice, ctx->stream));
   if (n > 0) {
     const int blocks = (int)std::min<int64_t>((n + 255) / 256, 1024);
-    tf32_check_kernel<<<blocks, 256, 0, ctx->stream>>>(d, n, flag);
+    value_stats_kernel<<<blocks, 256, 0, ctx->stream>>>(d, n, buf);
     iq_count(ctx);
     IQ_CUDA_OK(cudaGetLastError());
   }
-  int h = 1;
-  IQ_CUDA_OK(cudaMemcpyAsync(&h, flag, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  unsigned h[3];
+  IQ_CUDA_OK(cudaMemcpyAsync(h, buf, sizeof(h), cudaMemcpyDeviceToHost, ctx->stream));
   IQ_CUDA_OK(cudaStreamSynchronize(ctx->stream));
-  exact = h == 0;
+  memcpy(&out.amax, &h[0], 4);
+  out.minexp = h[1] == 0xFFFFFFFFu ? (1 << 30) : (int)h[1] - 256;
+  out.narrow = h[2] == 0u;
   return IQ_OK;
 }
 
@@ -651,6 +895,13 @@ int iq_launch_corr_tc(iq_ctx* ctx, const TcCorrLaunch& L) {
     return iq_set_error(IQ_ERR_LIMIT, "tensor-core correlation: tile too large");
   const Dim3 od = L.out_dims;
   if (od.vol() <= 0) return IQ_OK;
+  // FP16 halves when both operands' ranges allow them (engine 2), else TF32 halves; one MMA
+  // per K-step when every value has at most 11 significant bits
+  const bool f16 = ctx->corr_engine == 2 && L.stage16 && L.img_stats.fp16_range() &&
+                   L.tmpl_stats.fp16_range();
+  const bool exact = L.img_stats.narrow && L.tmpl_stats.narrow;
+  const int ka = f16 && L.img_stats.amax > 0.f ? L.img_stats.maxexp() - 14 : 0;
+  const int kb = f16 && L.tmpl_stats.amax > 0.f ? L.tmpl_stats.maxexp() - 14 : 0;
   TcArgs a;
   a.img = L.img;
   a.ix = L.img_dims.x;
@@ -665,13 +916,24 @@ int iq_launch_corr_tc(iq_ctx* ctx, const TcCorrLaunch& L) {
   a.nbox = L.nbox;
   for (int b = 0; b < IQ_TC_MAXBOX; ++b) a.box[b] = L.box[b];
   a.disabled = L.disabled;
-  a.word = L.stage_word;
-  a.prefix = L.stage_prefix;
-  a.nstage = L.nstage;
+  const int nstage = f16 ? L.nstage16 : L.nstage;
+  const int64_t nsteps = f16 ? L.nsteps16 : L.nsteps;
+  if (f16) {
+    a.word = L.stage16;
+    a.wordb = L.stage16 + L.nstage16;
+    a.prefix = L.stage16 + 2 * L.nstage16;
+  } else {
+    a.word = L.stage_word;
+    a.wordb = nullptr;
+    a.prefix = L.stage_prefix;
+  }
+  a.nstage = nstage;
   a.B = (const char*)L.B;
   a.cols = L.cols;
   a.N = L.N;
-  a.exact = L.exact ? 1 : 0;
+  a.exact = exact ? 1 : 0;
+  a.scale_a = std::ldexp(1.f, -ka);
+  a.ab2 = std::ldexp(1.f, ka + kb + 1);
   uint32_t tc = 32;
   while (tc < (uint32_t)(TC_MB * L.N)) tc <<= 1;
   a.tmem_cols = tc;
@@ -679,29 +941,40 @@ int iq_launch_corr_tc(iq_ctx* ctx, const TcCorrLaunch& L) {
   a.stats = ctx->prof ? ctx->d_stats : nullptr;
 
   iq_timer_start(ctx, "corr");
-  if (L.nstage > 0) {  // no stages: every column's mask is empty and its products are zero
-    PackArgs p;
-    p.grid = L.grid; p.gx = L.grid_dims.x; p.gy = L.grid_dims.y; p.tx = L.tile.x;
-    p.cols = L.cols; p.N = L.N;
-    p.word = L.stage_word; p.prefix = L.stage_prefix; p.nstage = L.nstage;
-    for (int b = 0; b < IQ_TC_MAXBOX; ++b) p.box[b] = L.box[b];
-    p.B = (char*)L.B;
-    dim3 grid((unsigned)((TC_STEPS * 2 * L.N + 255) / 256), (unsigned)std::min(L.nstage, 65535));
-    tc_pack_kernel<<<grid, 256, 0, ctx->stream>>>(p);
+  if (nstage > 0) {  // no stages: every column's mask is empty and its products are zero
+    const dim3 grid((unsigned)((TC_STEPS * 2 * L.N + 255) / 256), (unsigned)std::min(nstage, 65535));
+    if (f16) {
+      Pack16Args p;
+      p.grid = L.grid; p.gx = L.grid_dims.x; p.gy = L.grid_dims.y; p.tx = L.tile.x;
+      p.cols = L.cols; p.N = L.N;
+      p.wa = a.word; p.wb = a.wordb; p.prefix = a.prefix; p.nstage = nstage;
+      for (int b = 0; b < IQ_TC_MAXBOX; ++b) p.box[b] = L.box[b];
+      p.scale_b = std::ldexp(1.f, -kb);
+      p.B = (char*)L.B;
+      tc_pack16_kernel<<<grid, 256, 0, ctx->stream>>>(p);
+    } else {
+      PackArgs p;
+      p.grid = L.grid; p.gx = L.grid_dims.x; p.gy = L.grid_dims.y; p.tx = L.tile.x;
+      p.cols = L.cols; p.N = L.N;
+      p.word = L.stage_word; p.prefix = L.stage_prefix; p.nstage = nstage;
+      for (int b = 0; b < IQ_TC_MAXBOX; ++b) p.box[b] = L.box[b];
+      p.B = (char*)L.B;
+      tc_pack_kernel<<<grid, 256, 0, ctx->stream>>>(p);
+    }
     iq_count(ctx);
     IQ_CUDA_OK(cudaGetLastError());
   }
-  const size_t smem = tc_smem_bytes(L.N);
-  IQ_CUDA_OK(cudaFuncSetAttribute(corr_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  (int)smem));
+  const size_t smem = f16 ? tc_smem_bytes<true>(L.N) : tc_smem_bytes<false>(L.N);
+  auto kern = f16 ? corr_tc_kernel<true> : corr_tc_kernel<false>;
+  IQ_CUDA_OK(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   const int64_t nblk = od.z * bpp;
   if (ctx->prof) {
-    ctx->prof_mma_flops += 2.0 * (double)nblk * 128 * TC_MB * (double)L.nsteps * 8 * L.N *
-                           (L.exact ? 1 : 3);
+    ctx->prof_mma_flops += 2.0 * (double)nblk * 128 * TC_MB * (double)nsteps * (f16 ? 16 : 8) *
+                           L.N * (exact ? 1 : 3);
     ctx->prof_mma_launches += 1;
     ctx->prof_tc_cols += L.N;
   }
-  corr_tc_kernel<<<(unsigned)nblk, TC_THREADS, smem, ctx->stream>>>(a);
+  kern<<<(unsigned)nblk, TC_THREADS, smem, ctx->stream>>>(a);
   iq_count(ctx);
   iq_timer_stop(ctx, "corr", L.flops);
   IQ_CUDA_OK(cudaGetLastError());

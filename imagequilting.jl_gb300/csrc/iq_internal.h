@@ -15,6 +15,23 @@
 // ---------------------------------------------------------------------------------------
 // Context
 // ---------------------------------------------------------------------------------------
+// Magnitude range and precision of an array of floats (NaN and Inf ignored), which decide how
+// the tensor-core correlation may represent it: TF32 halves, or FP16 halves after a power-of-two
+// scaling (only when the range keeps every half a normal FP16 number).
+struct IqValueStats {
+  float amax = 0.f;       // largest magnitude
+  int minexp = 1 << 30;   // smallest binary exponent of a nonzero magnitude
+  bool narrow = true;     // every value has at most 11 significant bits (a TF32 value)
+  void merge(const IqValueStats& o) {
+    amax = amax > o.amax ? amax : o.amax;
+    minexp = minexp < o.minexp ? minexp : o.minexp;
+    narrow = narrow && o.narrow;
+  }
+  int maxexp() const;      // binary exponent of amax (0 when amax == 0)
+  bool fp16_range() const; // nonzero magnitudes within 2^17 of amax
+};
+IqValueStats iq_host_stats(const float* v, int64_t n);
+
 struct IqTimer {
   std::vector<cudaEvent_t> ev;  // start/stop pairs
   size_t used = 0;              // pairs recorded
@@ -32,7 +49,7 @@ struct iq_ctx {
   double* d_ti2ii = nullptr;   // integral image of TI^2, (x+1)(y+1)(z+1) doubles
   int32_t* d_nanii = nullptr;  // integral image of the NaN indicator
   int64_t ti_nan = 0;          // number of NaN voxels
-  bool ti_tf32 = false;        // every prepared TI value is a TF32 value
+  IqValueStats ti_stats;       // magnitude range and precision of the prepared TI
   int* d_status = nullptr;     // device status word (first kernel error)
   // grow-only scratch buffers, by slot
   std::vector<void*> buf;
@@ -53,7 +70,8 @@ struct iq_ctx {
   int cut_threads = 512;
   int64_t level_chunk = 64;     // most tiles of one dependency level launched together
   int corr_variant = 1;         // launch shape of the 16-template correlation
-  int corr_engine = 1;          // 1: tensor-core (tcgen05) correlation for box masks, 0: SIMT
+  int corr_engine = 2;          // box-mask distances: 2 tensor cores FP16 halves when the data's
+                                // range allows (else TF32), 1 tensor cores TF32, 0 SIMT
   int64_t max_steps = -1;       // tiles simulated per realization (< 0: all)
 };
 enum IqStat { ST_CUT_ROUNDS = 0, ST_CUT_LEVELS, ST_CUT_CTAS, ST_PICK_ITERS, ST_PICK_CAND,
@@ -196,6 +214,10 @@ struct TcCol {
 struct TcStages {
   std::vector<uint32_t> word, prefix;
   int64_t nsteps = 0;  // K-steps of all stages
+  // the FP16 form: consecutive rows in pairs (w16b = 0 when a row has no partner), each K-step
+  // of 16 offsets made of two 8-offset chunks of the pair
+  std::vector<uint32_t> w16a, w16b, pre16;
+  int64_t nsteps16 = 0;
 };
 void iq_tc_stages(Dim3 tile, const TcBox* boxes, int nbox, TcStages& out);
 
@@ -207,20 +229,23 @@ struct TcCorrLaunch {
   int nbox = 1;
   TcBox box[IQ_TC_MAXBOX] = {};
   const uint8_t* disabled = nullptr;
-  const uint32_t* stage_word = nullptr; // device copies of TcStages
+  const uint32_t* stage_word = nullptr; // device copies of TcStages (TF32 form)
   const uint32_t* stage_prefix = nullptr;
   int nstage = 0;
   int64_t nsteps = 0;
+  const uint32_t* stage16 = nullptr;    // FP16 form: w16a, w16b, pre16 of nstage16 each
+  int nstage16 = 0;
+  int64_t nsteps16 = 0;
   const float* grid = nullptr; Dim3 grid_dims{1, 1, 1};  // template source
   const TcCol* cols = nullptr;          // device array of N columns
   int N = 0;                            // multiple of 16, at most 256
-  void* B = nullptr;                    // packed templates, nsteps * 64 * N bytes
-  bool exact = false;                   // img and templates are TF32 values: one MMA per step
+  void* B = nullptr;                    // packed templates, max(nsteps, nsteps16) * 64 * N bytes
+  IqValueStats img_stats, tmpl_stats;   // ranges of the image and of the templates
   double flops = 0;                     // algorithmic FLOPs (profiling)
 };
 int iq_launch_corr_tc(iq_ctx* ctx, const TcCorrLaunch& L);
-// true when every value of the device array is a TF32 value (low 13 mantissa bits zero)
-int iq_tf32_exact(iq_ctx* ctx, const float* d, int64_t n, bool& exact);
+// statistics of a device array of floats
+int iq_value_stats(iq_ctx* ctx, const float* d, int64_t n, IqValueStats& out);
 
 // integral images and disabled windows
 int iq_build_integrals(iq_ctx* ctx, const float* d_img, Dim3 dims, double* d_sqii,

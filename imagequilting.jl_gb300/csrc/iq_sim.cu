@@ -438,7 +438,7 @@ extern "C" int iq_simulate(iq_ctx* ctx, const iq_sim_params* p, const iq_hard_da
           if (in) klist[(size_t)c * T + k++] = kpack(x, y, z);
         }
   }
-  const bool tc = ctx->corr_engine == 1;
+  const bool tc = ctx->corr_engine >= 1;
   // hard lists of data tiles
   std::vector<int64_t> hoff(g.ntot + 1, 0);
   for (int64_t t = 0; t < g.ntot; ++t) hoff[t + 1] = hoff[t] + (int64_t)tile_hard[t].size();
@@ -526,8 +526,9 @@ extern "C" int iq_simulate(iq_ctx* ctx, const iq_sim_params* p, const iq_hard_da
       for (int d = 0; d < 3; ++d) { b.lo[d] = (int32_t)cfgs[c].lo[d]; b.hi[d] = (int32_t)cfgs[c].hi[d]; }
     return b;
   };
-  struct TcStageRef { int64_t off; int nstage; int64_t nsteps; };
-  std::vector<uint32_t> tc_word, tc_pre;
+  // stage lists in both forms: TF32 (one row entry per stage) and FP16 (two per stage)
+  struct TcStageRef { int64_t off; int nstage; int64_t nsteps; int64_t off16; int nstage16; int64_t nsteps16; };
+  std::vector<uint32_t> tc_word, tc_pre, tc_w16;  // tc_w16: per list, w16a then w16b then pre16
   std::map<std::vector<int>, TcStageRef> tc_stage_of;
   auto stages_for = [&](const std::vector<int>& cfgset) -> TcStageRef {
     auto it = tc_stage_of.find(cfgset);
@@ -536,9 +537,13 @@ extern "C" int iq_simulate(iq_ctx* ctx, const iq_sim_params* p, const iq_hard_da
     for (int c : cfgset) bx.push_back(cfg_box(c));
     TcStages st;
     iq_tc_stages(tileD, bx.data(), (int)bx.size(), st);
-    TcStageRef r{(int64_t)tc_word.size(), (int)st.word.size(), st.nsteps};
+    TcStageRef r{(int64_t)tc_word.size(), (int)st.word.size(), st.nsteps,
+                 (int64_t)tc_w16.size(), (int)st.w16a.size(), st.nsteps16};
     tc_word.insert(tc_word.end(), st.word.begin(), st.word.end());
     tc_pre.insert(tc_pre.end(), st.prefix.begin(), st.prefix.end());
+    tc_w16.insert(tc_w16.end(), st.w16a.begin(), st.w16a.end());
+    tc_w16.insert(tc_w16.end(), st.w16b.begin(), st.w16b.end());
+    tc_w16.insert(tc_w16.end(), st.pre16.begin(), st.pre16.end());
     tc_stage_of[cfgset] = r;
     return r;
   };
@@ -597,14 +602,14 @@ extern "C" int iq_simulate(iq_ctx* ctx, const iq_sim_params* p, const iq_hard_da
     }
     tcbeg[c + 1] = (int64_t)tcruns.size();
   }
-  const TcStageRef soft_st = (tc && nsoft > 0 && T > 0) ? stages_for(std::vector<int>{ncfg}) : TcStageRef{0, 0, 0};
-  // exactness: the simulation grid holds TI values and hard data only
-  bool sim_tf32 = ctx->ti_tf32;
-  for (int64_t i = 0; i < nh && sim_tf32; ++i) {
-    const float f = (float)hv[i];
-    uint32_t bits;
-    memcpy(&bits, &f, 4);
-    if (!std::isnan(f) && (bits & 0x1FFFu)) sim_tf32 = false;
+  const TcStageRef soft_st = (tc && nsoft > 0 && T > 0) ? stages_for(std::vector<int>{ncfg})
+                                                         : TcStageRef{0, 0, 0, 0, 0, 0};
+  // the simulation grid holds TI values, hard data and zeros only
+  IqValueStats sim_stats = ctx->ti_stats;
+  {
+    std::vector<float> hvf(nh);
+    for (int64_t i = 0; i < nh; ++i) hvf[i] = (float)hv[i];
+    sim_stats.merge(iq_host_stats(hvf.data(), nh));
   }
   uint32_t* d_tcst = nullptr;  // stage words of every list, then their prefixes
   void* d_tcb = nullptr;        // packed templates of one launch
@@ -614,9 +619,11 @@ extern "C" int iq_simulate(iq_ctx* ctx, const iq_sim_params* p, const iq_hard_da
     const size_t ns = tc_word.size();
     std::vector<uint32_t> both(tc_word);
     both.insert(both.end(), tc_pre.begin(), tc_pre.end());
+    both.insert(both.end(), tc_w16.begin(), tc_w16.end());
     int64_t bmax = 1;
-    for (const TcRun& u : tcruns) bmax = std::max<int64_t>(bmax, u.st.nsteps * 64 * u.N);
-    bmax = std::max<int64_t>(bmax, soft_st.nsteps * 64 * IQ_TC_MAXN);
+    for (const TcRun& u : tcruns)
+      bmax = std::max<int64_t>(bmax, std::max(u.st.nsteps, u.st.nsteps16) * 64 * u.N);
+    bmax = std::max<int64_t>(bmax, std::max(soft_st.nsteps, soft_st.nsteps16) * 64 * IQ_TC_MAXN);
     d_tcst = (uint32_t*)iq_scratch(ctx, S_TCSTAGE, sizeof(uint32_t) * both.size());
     d_tcb = iq_scratch(ctx, S_TCB, (size_t)bmax);
     d_tcb2 = (double*)iq_scratch(ctx, S_TCB2, sizeof(double) * IQ_TC_MAXN);
@@ -635,7 +642,8 @@ extern "C" int iq_simulate(iq_ctx* ctx, const iq_sim_params* p, const iq_hard_da
   // one tensor-core launch over the columns cols[0..N) with the masks of `cfgset`
   auto tc_launch = [&](const std::vector<int>& cfgset, const TcStageRef& sr, const float* img,
                        const double* ii, const float* grid, Dim3 gdims, const TcCol* cols, int N,
-                       bool exact, double flops) -> int {
+                       const IqValueStats& img_stats, const IqValueStats& tmpl_stats,
+                       double flops) -> int {
     TcCorrLaunch L;
     L.img = img; L.img_dims = ctx->ti; L.out_dims = distD; L.tile = tileD; L.ii = ii;
     L.nbox = (int)cfgset.size();
@@ -645,8 +653,11 @@ extern "C" int iq_simulate(iq_ctx* ctx, const iq_sim_params* p, const iq_hard_da
     L.stage_prefix = d_tcst + tc_word.size() + sr.off;
     L.nstage = sr.nstage;
     L.nsteps = sr.nsteps;
+    L.stage16 = d_tcst + 2 * tc_word.size() + sr.off16;
+    L.nstage16 = sr.nstage16;
+    L.nsteps16 = sr.nsteps16;
     L.grid = grid; L.grid_dims = gdims; L.cols = cols; L.N = N; L.B = d_tcb;
-    L.exact = exact; L.flops = flops;
+    L.img_stats = img_stats; L.tmpl_stats = tmpl_stats; L.flops = flops;
     return iq_launch_corr_tc(ctx, L);
   };
 
@@ -687,6 +698,7 @@ extern "C" int iq_simulate(iq_ctx* ctx, const iq_sim_params* p, const iq_hard_da
       d_auxii[s] = a_ii + iivol * s;
       IQ_CUDA_OK(cudaMemcpyAsync(a_raw, soft[s].aux, sizeof(float) * asz.vol(), cudaMemcpyDefault, st));
       RET_IF(iq_launch_pad_symmetric(ctx, a_raw, asz, d_aux[s], psz));
+      RET_IF(iq_launch_prepare(ctx, d_aux[s], psz.vol(), nullptr));  // NaN -> 0 (prepare(aux))
       IQ_CUDA_OK(cudaMemcpyAsync(d_auxti[s], soft[s].auxti, sizeof(float) * tivol, cudaMemcpyDefault, st));
       RET_IF(iq_launch_prepare(ctx, d_auxti[s], tivol, nullptr));
       RET_IF(iq_build_integrals(ctx, d_auxti[s], ctx->ti, d_auxii[s], nullptr, nullptr));
@@ -716,9 +728,9 @@ extern "C" int iq_simulate(iq_ctx* ctx, const iq_sim_params* p, const iq_hard_da
             }
           }
         }
-        bool exact = false, ea = false;
-        RET_IF(iq_tf32_exact(ctx, d_aux[s], psz.vol(), ea));
-        if (ea) RET_IF(iq_tf32_exact(ctx, d_auxti[s], tivol, exact));
+        IqValueStats aux_stats, auxti_stats;
+        RET_IF(iq_value_stats(ctx, d_aux[s], psz.vol(), aux_stats));
+        RET_IF(iq_value_stats(ctx, d_auxti[s], tivol, auxti_stats));
         TcCol* d_cols = (TcCol*)iq_scratch(ctx, S_TCSOFT, sizeof(TcCol) * cols.size());
         if (!d_cols) return IQ_ERR_ALLOC;
         IQ_CUDA_OK(cudaMemcpyAsync(d_cols, cols.data(), sizeof(TcCol) * cols.size(),
@@ -734,7 +746,7 @@ extern "C" int iq_simulate(iq_ctx* ctx, const iq_sim_params* p, const iq_hard_da
                             d_softmm + 2 * slot0};
           RET_IF(iq_launch_gather(ctx, G));
           RET_IF(tc_launch(std::vector<int>{ncfg}, soft_st, d_auxti[s], d_auxii[s], d_aux[s], psz,
-                           d_cols + launches[l].first, launches[l].second, exact,
+                           d_cols + launches[l].first, launches[l].second, auxti_stats, aux_stats,
                            2.0 * (double)P * (double)T * nb));
         }
         IQ_CUDA_OK(cudaStreamSynchronize(st));  // `cols` is a host vector
@@ -856,7 +868,7 @@ extern "C" int iq_simulate(iq_ctx* ctx, const iq_sim_params* p, const iq_hard_da
       for (int64_t l = tcbeg[c]; l < tcbeg[c + 1]; ++l) {
         const TcRun& u = tcruns[l];
         RET_IF(tc_launch(u.cfgset, u.st, ctx->d_ti, ctx->d_ti2ii, d_sim, padD, d_tccols + u.col0, u.N,
-                         sim_tf32, u.flops));
+                         ctx->ti_stats, sim_stats, u.flops));
       }
     } else {
       CorrLaunch C;

@@ -182,8 +182,10 @@ int64_t iq_ctx_launches(iq_ctx* ctx);
  *                         1 processes the tile path one tile at a time)
  *   "sim.max_steps"       simulate only the first n tiles of the path (< 0: all; default -1);
  *                         for bounded samples and for locating the first differing tile
- *   "corr.engine"         1: distance maps of "tile minus box" masks on the tensor cores
- *                         (tcgen05, TF32 split in two halves; default), 0: SIMT FP32 kernel
+ *   "corr.engine"         distance maps of "tile minus box" masks: 2 (default) tensor cores
+ *                         (tcgen05) with FP16 halves after a power-of-two scaling when every
+ *                         nonzero magnitude lies within 2^17 of the largest, else TF32 halves;
+ *                         1 tensor cores with TF32 halves; 0 the SIMT FP32 kernel
  * Returns IQ_ERR_ARG for an unknown name or an out-of-range value.
  */
 int iq_set_option(iq_ctx* ctx, const char* name, int64_t value);

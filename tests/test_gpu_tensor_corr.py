@@ -1,9 +1,10 @@
 """Tensor-core (tcgen05) distance maps against the oracle and against the SIMT kernel.
 
 The tensor-core kernel serves every mask of the form "tile minus a box" (overlap masks, the
-full tile of soft data); `corr.engine` = 0 forces the SIMT kernel. Tolerance of a distance map
-as in test_gpu_parity: 1e-5 * (A^2 + B^2). Integer-valued data are exact in both kernels, so
-the maps and whole realizations must then be identical.
+full tile of soft data). `corr.engine`: 2 (default) FP16 halves with power-of-two scaling when
+the data's range allows, else TF32 halves; 1 TF32 halves; 0 the SIMT kernel. Tolerance of a
+distance map as in test_gpu_parity: 1e-5 * (A^2 + B^2). Integer-valued data are exact in every
+engine, so the maps and whole realizations must then be identical.
 """
 import numpy as np
 import pytest
@@ -26,6 +27,14 @@ def ctx(iq):
 def ctx_simt(iq):
     c = iq.Context(0)
     c.set_option("corr.engine", 0)
+    yield c
+    c.close()
+
+
+@pytest.fixture(scope="module")
+def ctx_tf32(iq):
+    c = iq.Context(0)
+    c.set_option("corr.engine", 1)
     yield c
     c.close()
 
@@ -115,6 +124,49 @@ def test_iqsim_engines_identical_integer_ti(iq, ctx, ctx_simt, path):
         assert np.array_equal(np.asarray(x, float), np.asarray(y, float), equal_nan=True)
 
 
+@pytest.mark.parametrize("scale", [1.0, 1e5, 3e-4])
+def test_fp16_and_tf32_vs_oracle_scaled(iq, ctx, ctx_tf32, scale):
+    # values far from 1 exercise the power-of-two scaling of the FP16 halves
+    rng = np.random.default_rng(35)
+    ti = (scale * np.exp(rng.normal(size=(48, 40, 10)))).astype(np.float32)
+    tm = (scale * np.exp(rng.normal(size=(4, 11, 9, 4)))).astype(np.float32)
+    w = _mask((11, 9, 4), "prev")
+    for c in (ctx, ctx_tf32):
+        got = iq.fastdistance(ti, tm, w, ctx=c)
+        for i in range(4):
+            ref = O.fastdistance(ti, tm[i], w, "direct")
+            err = np.abs(got[i].astype(np.float64) - ref) / _scale(ti, tm[i], w)
+            assert err.max() <= DIST_RTOL, (scale, err.max())
+
+
+def test_wide_range_falls_back_to_tf32(iq, ctx, ctx_tf32):
+    # magnitudes spanning 2^30 are outside the FP16 halves' range: engine 2 must give the
+    # TF32 result
+    rng = np.random.default_rng(36)
+    ti = (np.exp(rng.uniform(-10, 10, size=(40, 30, 8))) * rng.choice([-1, 1], (40, 30, 8))).astype(np.float32)
+    tm = rng.normal(size=(3, 8, 6, 3)).astype(np.float32)
+    w = _mask((8, 6, 3), "inner")
+    a = iq.fastdistance(ti, tm, w, ctx=ctx)
+    b = iq.fastdistance(ti, tm, w, ctx=ctx_tf32)
+    assert np.array_equal(a, b)
+    for i in range(3):
+        ref = O.fastdistance(ti, tm[i], w, "direct")
+        assert (np.abs(a[i].astype(np.float64) - ref) / _scale(ti, tm[i], w)).max() <= DIST_RTOL
+
+
+@pytest.mark.parametrize("path", ["raster", "random"])
+def test_iqsim_fp16_tf32_identical_integer_ti(iq, ctx, ctx_tf32, path):
+    rng = np.random.default_rng(37)
+    ti = rng.integers(0, 5, (28, 26, 12)).astype(np.float32)
+    aux = rng.integers(0, 3, (34, 32, 12)).astype(np.float32)
+    auxti = rng.integers(0, 3, ti.shape).astype(np.float32)
+    kw = dict(overlap=(0.3, 0.3, 0.3), path=path, nreal=2, rng=7, soft=[(aux, auxti)])
+    a = iq.iqsim(ti, (10, 9, 5), (34, 32, 12), ctx=ctx, **kw)
+    b = iq.iqsim(ti, (10, 9, 5), (34, 32, 12), ctx=ctx_tf32, **kw)
+    for x, y in zip(a, b):
+        assert np.array_equal(np.asarray(x, float), np.asarray(y, float))
+
+
 def test_engine_option_validation(iq, ctx):
     with pytest.raises(Exception):
-        ctx.set_option("corr.engine", 2)
+        ctx.set_option("corr.engine", 3)
