@@ -363,6 +363,7 @@ def run_ours(args, W, dist, rank, world):
     clk = clocks.stop()
     prof = {k: ctx.profile_get(k) for k in ("corr", "pick", "graphcut", "paste")}
     mma = ctx.profile_get("corr.mma")
+    mma16 = ctx.profile_get("corr.mma16")
     cols = ctx.profile_get("corr.columns")
     counters = {k: ctx.profile_get(k) for k in ("graphcut.rounds", "graphcut.levels",
                                                  "pick.iterations", "pick.candidates")}
@@ -379,6 +380,8 @@ def run_ours(args, W, dist, rank, world):
     gc = {k: ctx.profile_get("graphcut." + k) for k in ("setup_cycles", "round_cycles",
                                                         "relabel_cycles")}
     counters["graphcut_cycles_per_cta"] = {k: (v[2] / v[1]) if v[1] else None for k, v in gc.items()}
+    pk = {k: ctx.profile_get("pick." + k) for k in ("select_cycles", "weight_cycles", "draw_cycles")}
+    counters["pick_cycles_per_cta"] = {k: (v[2] / v[1]) if v[1] else None for k, v in pk.items()}
     ctx.profile(False)
     ms_max = reduce_max(dist, ms)
     barrier(dist)
@@ -420,14 +423,18 @@ def run_ours(args, W, dist, rank, world):
             "flops_per_launch": corr_flops / corr_n if corr_n else None,
             "traffic": profile_traffic("corr_tc_kernel", W["name"], cols[2] / cols[1] if cols[1] else None),
             "mma_tflops_issued": (mma[2] / (corr_ms / 1e3) / 1e12) if corr_ms and mma[2] else None,
+            "mma_tflops_issued_fp16": (mma16[2] / (corr_ms / 1e3) / 1e12) if corr_ms else None,
             "note": "achieved = algorithmic FLOPs (2 x positions x mask offsets x templates) "
-                    "over the correlation's time; the tensor pipe issues TF32 MMAs (three per "
-                    "K-step for FP32 data: hi*hi + hi*lo + lo*hi) over padded positions and "
-                    "offsets, counted in mma_tflops_issued; TF32 runs at half the bf16 rate"}
+                    "over the correlation's time; the tensor pipe issues FP16 (or TF32) MMAs, "
+                    "three per K-step for FP32 data (hi*hi + hi*lo + lo*hi), over padded "
+                    "positions and offsets, counted in mma_tflops_issued; mma_frac is that work "
+                    "over its peak (FP16 at the bf16 rate, TF32 at half of it)"}
     if roof["achieved"] is not None and roof["peak"]:
         roof["frac"] = roof["achieved"] / roof["peak"]
         if roof["mma_tflops_issued"]:
-            roof["mma_frac_of_tf32_peak"] = roof["mma_tflops_issued"] / (roof["peak"] / 2)
+            f16 = roof["mma_tflops_issued_fp16"] or 0.0
+            tf32 = roof["mma_tflops_issued"] - f16
+            roof["mma_frac"] = f16 / roof["peak"] + tf32 / (roof["peak"] / 2)
     kernel_share = {k: {"ms": round(v[0], 3), "launches": v[1],
                         "share_of_step": round(v[0] / ms, 4) if ms else None}
                     for k, v in prof.items()}
@@ -445,7 +452,7 @@ def run_ours(args, W, dist, rank, world):
                        "options": args.option,
                        "voxels_per_step": voxels * world, "parallelism": "replicas x%d" % world,
                        "l2": "working set > L2 (simulation grids 350 MB, soft maps 1.6 GB)",
-                       "form": "plain (FP32 correlation as TF32x3 on the tensor cores)"},
+                       "form": "plain (FP32-accurate correlation as split FP16/TF32 MMAs on the tensor cores)"},
             "roofline": roof, "dominant_kernel": dom, "kernels": kernel_share,
             "counters": counters,
             "cpu_baseline": cpu,

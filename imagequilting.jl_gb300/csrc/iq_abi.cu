@@ -76,6 +76,7 @@ extern "C" int iq_profile(iq_ctx* ctx, int32_t enable) {
   cudaStreamSynchronize(ctx->stream);
   for (auto& kv : ctx->timers) { kv.second.used = 0; kv.second.work = 0; }
   ctx->prof_mma_flops = 0;
+  ctx->prof_mma_flops16 = 0;
   ctx->prof_mma_launches = 0;
   ctx->prof_tc_cols = 0;
   cudaMemsetAsync(ctx->d_stats, 0, sizeof(unsigned long long) * ST_COUNT, ctx->stream);
@@ -94,22 +95,27 @@ extern "C" int iq_profile_get(iq_ctx* ctx, const char* kernel, double* ms_total,
   // counters: "graphcut.rounds", "graphcut.levels" (work = total, launches = CTAs),
   // "pick.iterations", "pick.candidates" (work = total, launches = CTAs), "corr.mma" (work =
   // tensor-pipe FLOPs issued, with the TF32 split and the padded positions and offsets),
-  // "corr.columns" (work = columns of the tensor-core launches, launches = their count)
-  if (!strcmp(kernel, "corr.mma") || !strcmp(kernel, "corr.columns")) {
+  // "corr.mma16" (the FP16 part of it), "corr.columns" (work = columns of the tensor-core
+  // launches, launches = their count)
+  if (!strcmp(kernel, "corr.mma") || !strcmp(kernel, "corr.mma16") ||
+      !strcmp(kernel, "corr.columns")) {
     if (ms_total) *ms_total = 0;
     if (launches) *launches = ctx->prof_mma_launches;
-    if (work) *work = kernel[5] == 'm' ? ctx->prof_mma_flops : ctx->prof_tc_cols;
+    if (work)
+      *work = !strcmp(kernel, "corr.mma") ? ctx->prof_mma_flops
+              : !strcmp(kernel, "corr.mma16") ? ctx->prof_mma_flops16 : ctx->prof_tc_cols;
     return IQ_OK;
   }
   // "corr.loop", "corr.wait_full", "corr.wait_afull", "corr.wait_done", "corr.producer_wait",
   // "corr.producer_loop", "corr.epilogue" (work = SM cycles summed over CTAs, launches = CTAs)
-  const char* names[18] = {"graphcut.rounds", "graphcut.levels", "pick.iterations",
+  const char* names[21] = {"graphcut.rounds", "graphcut.levels", "pick.iterations",
                            "pick.candidates", "graphcut.max_rounds", "graphcut.max_levels",
                            "corr.loop", "corr.wait_full", "corr.wait_afull", "corr.wait_done",
                            "corr.producer_wait", "corr.producer_loop", "corr.epilogue",
                            "corr.issue", "corr.mma_units", "graphcut.setup_cycles",
-                           "graphcut.round_cycles", "graphcut.relabel_cycles"};
-  const int idx[18][2] = {{ST_CUT_ROUNDS, ST_CUT_CTAS}, {ST_CUT_LEVELS, ST_CUT_CTAS},
+                           "graphcut.round_cycles", "graphcut.relabel_cycles",
+                           "pick.select_cycles", "pick.weight_cycles", "pick.draw_cycles"};
+  const int idx[21][2] = {{ST_CUT_ROUNDS, ST_CUT_CTAS}, {ST_CUT_LEVELS, ST_CUT_CTAS},
                           {ST_PICK_ITERS, ST_PICK_CTAS}, {ST_PICK_CAND, ST_PICK_CTAS},
                           {ST_CUT_MAXROUNDS, ST_CUT_CTAS}, {ST_CUT_MAXLEVELS, ST_CUT_CTAS},
                           {ST_TC_LOOP, ST_TC_CTAS}, {ST_TC_WFULL, ST_TC_CTAS},
@@ -117,8 +123,10 @@ extern "C" int iq_profile_get(iq_ctx* ctx, const char* kernel, double* ms_total,
                           {ST_TC_PWAIT, ST_TC_CTAS}, {ST_TC_PLOOP, ST_TC_CTAS},
                           {ST_TC_EPI, ST_TC_CTAS}, {ST_TC_ISSUE, ST_TC_CTAS},
                           {ST_TC_MMAU, ST_TC_CTAS}, {ST_CUT_TSETUP, ST_CUT_CTAS},
-                          {ST_CUT_TROUNDS, ST_CUT_CTAS}, {ST_CUT_TGR, ST_CUT_CTAS}};
-  for (int i = 0; i < 18; ++i)
+                          {ST_CUT_TROUNDS, ST_CUT_CTAS}, {ST_CUT_TGR, ST_CUT_CTAS},
+                          {ST_PICK_TSEL, ST_PICK_CTAS}, {ST_PICK_TW, ST_PICK_CTAS},
+                          {ST_PICK_TDRAW, ST_PICK_CTAS}};
+  for (int i = 0; i < 21; ++i)
     if (!strcmp(kernel, names[i])) {
       unsigned long long h[ST_COUNT];
       IQ_CUDA_OK(cudaMemcpy(h, ctx->d_stats, sizeof(h), cudaMemcpyDeviceToHost));

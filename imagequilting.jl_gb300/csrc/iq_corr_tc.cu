@@ -969,8 +969,10 @@ int iq_launch_corr_tc(iq_ctx* ctx, const TcCorrLaunch& L) {
   IQ_CUDA_OK(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   const int64_t nblk = od.z * bpp;
   if (ctx->prof) {
-    ctx->prof_mma_flops += 2.0 * (double)nblk * 128 * TC_MB * (double)nsteps * (f16 ? 16 : 8) *
-                           L.N * (exact ? 1 : 3);
+    const double fl = 2.0 * (double)nblk * 128 * TC_MB * (double)nsteps * (f16 ? 16 : 8) * L.N *
+                      (exact ? 1 : 3);
+    ctx->prof_mma_flops += fl;
+    if (f16) ctx->prof_mma_flops16 += fl;
     ctx->prof_mma_launches += 1;
     ctx->prof_tc_cols += L.N;
   }

@@ -63,6 +63,7 @@ struct iq_ctx {
   // [7] max cut BFS levels
   unsigned long long* d_stats = nullptr;
   double prof_mma_flops = 0;    // tensor-pipe FLOPs issued by the correlation while profiling
+  double prof_mma_flops16 = 0;  // the part issued as FP16 MMAs (bf16/fp16 rate; TF32: half)
   int64_t prof_mma_launches = 0;
   double prof_tc_cols = 0;      // columns (templates, with padding) of those launches
   // tuning knobs (iq_set_option)
@@ -84,7 +85,9 @@ enum IqStat { ST_CUT_ROUNDS = 0, ST_CUT_LEVELS, ST_CUT_CTAS, ST_PICK_ITERS, ST_P
               ST_TC_EPI, ST_TC_CTAS, ST_TC_ISSUE, ST_TC_MMAU,
               // graph cut, SM cycles summed over CTAs: set-up (loads, capacities), push and
               // relabel rounds, global relabels
-              ST_CUT_TSETUP, ST_CUT_TROUNDS, ST_CUT_TGR, ST_COUNT };
+              ST_CUT_TSETUP, ST_CUT_TROUNDS, ST_CUT_TGR,
+              // pick, SM cycles summed over CTAs: selection + compaction, tau-model weights, draw
+              ST_PICK_TSEL, ST_PICK_TW, ST_PICK_TDRAW, ST_COUNT };
 
 // scratch slot ids
 enum IqSlot {

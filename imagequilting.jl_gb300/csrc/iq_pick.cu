@@ -269,6 +269,8 @@ __device__ __forceinline__ int bin_shift(uint32_t mn, uint32_t mx) {
   return sh;
 }
 
+constexpr int SEL_BATCH = 8;  // loads in flight per thread and source in the select passes
+
 template <int NS>
 __device__ void hist_select(Smem& s, uint32_t* hist, unsigned long long* sbuf, SelReq* req,
                             int64_t P, Key* out) {
@@ -293,18 +295,18 @@ __device__ void hist_select(Smem& s, uint32_t* hist, unsigned long long* sbuf, S
     for (int j = 0; j < NS; ++j) sh[j] = pend[j] ? bin_shift(lo[j], hi[j]) : 0;
     for (int i = threadIdx.x; i < NS * NBIN; i += PT) hist[i] = 0;
     __syncthreads();
-    for (int64_t it0 = 0; it0 < iters; it0 += 4) {
-      // four independent loads per source before the atomics (memory-level parallelism)
-      uint32_t bv[NS][4];
+    for (int64_t it0 = 0; it0 < iters; it0 += SEL_BATCH) {
+      // SEL_BATCH independent loads per source before the atomics (memory-level parallelism)
+      uint32_t bv[NS][SEL_BATCH];
 #pragma unroll
-      for (int u = 0; u < 4; ++u) {
+      for (int u = 0; u < SEL_BATCH; ++u) {
         const int64_t p = (it0 + u) * PT + threadIdx.x;
 #pragma unroll
         for (int j = 0; j < NS; ++j)
           bv[j][u] = (p < P && pend[j]) ? fbits(req[j].src[p]) : 0xFFFFFFFFu;
       }
 #pragma unroll
-      for (int u = 0; u < 4; ++u)
+      for (int u = 0; u < SEL_BATCH; ++u)
 #pragma unroll
         for (int j = 0; j < NS; ++j) {
           const uint32_t b = bv[j][u];
@@ -364,15 +366,15 @@ __device__ void hist_select(Smem& s, uint32_t* hist, unsigned long long* sbuf, S
         // collect the bin's (value, index) keys and sort them
         if (threadIdx.x == 0) s.ncol = 0;
         __syncthreads();
-        for (int64_t it0 = 0; it0 < iters; it0 += 4) {
-          uint32_t vv[4];
+        for (int64_t it0 = 0; it0 < iters; it0 += SEL_BATCH) {
+          uint32_t vv[SEL_BATCH];
 #pragma unroll
-          for (int u = 0; u < 4; ++u) {
+          for (int u = 0; u < SEL_BATCH; ++u) {
             const int64_t p = (it0 + u) * PT + threadIdx.x;
             vv[u] = p < P ? fbits(req[j].src[p]) : 0xFFFFFFFFu;
           }
 #pragma unroll
-          for (int u = 0; u < 4; ++u) {
+          for (int u = 0; u < SEL_BATCH; ++u) {
             const uint32_t v = vv[u];
             if (v >= blo && v <= bhi) {
               const uint32_t at = atomicAdd(&s.ncol, 1u);
@@ -632,6 +634,8 @@ __global__ void __launch_bounds__(PT) pick_kernel(const PickArgs a) {
     amm[j] = j < naux ? tk.aux_mm[j] + r * tk.aux_mm_rs[j] : nullptr;
   }
 
+  const bool prof = a.stats != nullptr && threadIdx.x == 0;
+  const long long t0 = prof ? clock64() : 0;
   int64_t n;
   if (naux == 0) {
     const float mn = __uint_as_float(mm[0]);
@@ -694,6 +698,8 @@ __global__ void __launch_bounds__(PT) pick_kernel(const PickArgs a) {
     atomicAdd(a.stats + ST_PICK_CAND, (unsigned long long)n);
     atomicAdd(a.stats + ST_PICK_CTAS, 1ull);
   }
+  const long long t1 = prof ? clock64() : 0;
+  if (prof) atomicAdd(a.stats + ST_PICK_TSEL, (unsigned long long)(t1 - t0));
 
   // ---- tau model weights ----
   if (n == 1) {
@@ -721,6 +727,8 @@ __global__ void __launch_bounds__(PT) pick_kernel(const PickArgs a) {
     w[i] = __ddiv_rn(1.0, __dadd_rn(1.0, __dmul_rn(x0, prod[i])));
   __syncthreads();
 
+  const long long t2 = prof ? clock64() : 0;
+  if (prof) atomicAdd(a.stats + ST_PICK_TW, (unsigned long long)(t2 - t1));
   // ---- weighted draw ----
   const int64_t nch = (n + IQ_DRAW_CHUNK - 1) / IQ_DRAW_CHUNK;
   double* csum = prod;  // reuse
@@ -747,6 +755,7 @@ __global__ void __launch_bounds__(PT) pick_kernel(const PickArgs a) {
       if (__dadd_rn(base, part) >= t) { pick = i; break; }
     }
     a.rind[b] = cand[pick];
+    if (prof) atomicAdd(a.stats + ST_PICK_TDRAW, (unsigned long long)(clock64() - t2));
   }
 }
 
