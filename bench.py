@@ -378,7 +378,8 @@ def run_ours(args, W, dist, rank, world):
                                                     "mma_units")}
     counters["corr_cycles_per_cta"] = {k: (v[2] / v[1]) if v[1] else None for k, v in tc.items()}
     gc = {k: ctx.profile_get("graphcut." + k) for k in ("setup_cycles", "round_cycles",
-                                                        "relabel_cycles")}
+                                                        "relabel_cycles", "active_nodes",
+                                                        "nodes")}
     counters["graphcut_cycles_per_cta"] = {k: (v[2] / v[1]) if v[1] else None for k, v in gc.items()}
     pk = {k: ctx.profile_get("pick." + k) for k in ("select_cycles", "weight_cycles", "draw_cycles")}
     counters["pick_cycles_per_cta"] = {k: (v[2] / v[1]) if v[1] else None for k, v in pk.items()}

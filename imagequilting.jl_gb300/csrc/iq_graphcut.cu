@@ -13,11 +13,13 @@
 //   * so residuals and excesses are kept as int64 counts of q (the same values as the exact
 //     Float64 arithmetic, without GB300's narrow FP64 pipe); an arc is open when its residual
 //     is positive (the oracle quantizes and tests the same way);
-//   * each round: every active node pushes along its admissible arcs (h(u) = h(v) + 1) while
-//     it has excess, adding to the receivers' excesses with integer atomics, then every node
-//     with excess and no admissible arc relabels. The flow found depends on the order of the
-//     atomics, the cut does not: integer sums are exact, and the set of nodes that can reach
-//     t is the same for every maximum preflow;
+//   * each round: every node on the active list pushes along its admissible arcs
+//     (h(u) = h(v) + 1) while it has excess, adding to the receivers' excesses with integer
+//     atomics and listing them; then every listed node with excess and no admissible arc
+//     relabels in place, and the nodes still active form the next list (a few percent of the
+//     slab per round). The flow found depends on the order of the atomics, the cut does not:
+//     integer sums are exact, and the set of nodes that can reach t is the same for every
+//     maximum preflow;
 //   * a global relabel (BFS from t over open arcs) runs at the start, every GR rounds and at
 //     the end; nodes that cannot reach t get height NH and stop being active.
 // At the end the nodes that can reach t are the sink side of the canonical minimum cut (the
@@ -281,29 +283,53 @@ __global__ void __launch_bounds__(CUT_MAX_THREADS) cut_kernel(const CutArgs a) {
   }
   __syncthreads();
 
-  int cur = 0;
+  // heights live in h0 (relabels are in place: heights only grow, so a stale neighbour
+  // height read by a concurrent relabel still gives a valid label); between global relabels
+  // the BFS frontier lists hold the work lists and h1 the "listed" flags
+  HT* const hc = h0;
+  HT* const L = fa;     // nodes with excess and height below NH (pushed this round)
+  HT* const Nl = fb;    // nodes to relabel: the pushers left with excess and the receivers
+  HT* const flag = h1;  // 1 while a node is in Nl
+  __shared__ int s_wl[2];  // |L|, |Nl|
   int round = 0, levels = 0;
+  long long nactive = 0;
   const long long t_setup = prof ? clock64() : 0;
   auto relabel_all = [&]() {
     const long long t = prof ? clock64() : 0;
-    levels += global_relabel(g, cur ? h1 : h0, fa, fb, s_cnt);
+    levels += global_relabel(g, hc, fa, fb, s_cnt);
     if (prof) t_gr += clock64() - t;
+  };
+  // the active list from scratch (after a global relabel, which used the lists as frontiers)
+  auto rebuild = [&]() {
+    if (threadIdx.x == 0) s_wl[0] = 0;
+    __syncthreads();
+    for (int u = threadIdx.x; u < n; u += blockDim.x) {
+      flag[u] = 0;
+      if (g.kind(u) == 0 && g.ex[u] > 0 && (int)hc[u] < g.NH) L[atomicAdd(&s_wl[0], 1)] = (HT)u;
+    }
+    __syncthreads();
+  };
+  auto list_once = [&](int v) {  // append v to Nl unless it is there already
+    if (cas_height(&flag[v], 0, 1)) Nl[atomicAdd(&s_wl[1], 1)] = (HT)v;
   };
   if (g.L > 2) {
     relabel_all();
+    rebuild();
     bool capped = false;
     for (;;) {
-      HT* hc = cur ? h1 : h0;
-      HT* hn = cur ? h0 : h1;
-      // push phase: every active node pushes along all its admissible arcs while it has
-      // excess; the receivers' excesses are updated with integer atomics (exact in any
-      // order). Two ends of one edge never push on it in the same round (that would need
+      const int A = s_wl[0];
+      if (A == 0) break;
+      nactive += A;
+      if (threadIdx.x == 0) s_wl[1] = 0;
+      __syncthreads();
+      // push phase: every listed node pushes along its admissible arcs while it has excess;
+      // the receivers' excesses are updated with integer atomics (exact in any order). Two
+      // ends of one edge never push on it in the same round (that would need
       // h(u) = h(v) + 1 and h(v) = h(u) + 1), so each residual has one writer.
-      for (int u = threadIdx.x; u < n; u += blockDim.x) {
-        if (g.kind(u) != 0) continue;
+      for (int i = threadIdx.x; i < A; i += blockDim.x) {
+        const int u = L[i];
         const int hu = hc[u];
         long long e = g.ex[u];
-        if (e <= 0 || hu >= g.NH) continue;
         const long long e0 = e;
 #pragma unroll
         for (int dir = 0; dir < 6; ++dir) {
@@ -319,21 +345,28 @@ __global__ void __launch_bounds__(CUT_MAX_THREADS) cut_kernel(const CutArgs a) {
           *ruv = rr - delta;
           *rvu += delta;
           e -= delta;
-          if (g.kind(v) == 0) atomicAdd(reinterpret_cast<unsigned long long*>(&g.ex[v]),
-                                        (unsigned long long)delta);
+          if (g.kind(v) == 0) {
+            atomicAdd(reinterpret_cast<unsigned long long*>(&g.ex[v]), (unsigned long long)delta);
+            list_once(v);
+          }
         }
         if (e != e0)
           atomicAdd(reinterpret_cast<unsigned long long*>(&g.ex[u]), (unsigned long long)(e - e0));
+        if (e > 0) list_once(u);
       }
       __syncthreads();
-      // relabel phase: a node left with excess and no admissible arc moves to 1 + the lowest
-      // neighbour it still has residual capacity to
-      int active = 0;
-      for (int u = threadIdx.x; u < n; u += blockDim.x) {
-        if (g.kind(u) != 0) continue;
+      // relabel phase over Nl: a node left with excess and no admissible arc moves to 1 + the
+      // lowest neighbour it still has residual capacity to; the nodes that stay active form
+      // the next round's list
+      const int B = s_wl[1];
+      __syncthreads();
+      if (threadIdx.x == 0) s_wl[0] = 0;
+      __syncthreads();
+      for (int i = threadIdx.x; i < B; i += blockDim.x) {
+        const int u = Nl[i];
+        flag[u] = 0;
         const long long e = g.ex[u];
         int hu = hc[u];
-        int hnew = hu;
         if (e > 0 && hu < g.NH) {
           bool adm = false;
           int mh = 0x7fffffff;
@@ -348,19 +381,19 @@ __global__ void __launch_bounds__(CUT_MAX_THREADS) cut_kernel(const CutArgs a) {
             if (hu == hv + 1) { adm = true; break; }
             mh = min(mh, hv);
           }
-          if (!adm) hnew = mh >= g.NH - 1 ? g.NH : mh + 1;
+          if (!adm) {
+            hu = mh >= g.NH - 1 ? g.NH : mh + 1;
+            hc[u] = (HT)hu;
+          }
+          if (hu < g.NH) L[atomicAdd(&s_wl[0], 1)] = (HT)u;
         }
-        hn[u] = (HT)hnew;
-        if (e > 0 && hnew < g.NH) active = 1;
       }
-      active = __syncthreads_or(active);
-      cur ^= 1;
+      __syncthreads();
       ++round;
-      if (!active) break;
-      if (round >= a.round_cap) { capped = true; break; }
+      if (round >= a.round_cap && s_wl[0] > 0) { capped = true; break; }
       if (round % a.gr_period == 0) {
         relabel_all();
-        __syncthreads();
+        rebuild();
       }
     }
     relabel_all();
@@ -374,13 +407,14 @@ __global__ void __launch_bounds__(CUT_MAX_THREADS) cut_kernel(const CutArgs a) {
     atomicAdd(a.stats + ST_CUT_TGR, (unsigned long long)t_gr);
     atomicAdd(a.stats + ST_CUT_TROUNDS, (unsigned long long)(t_end - t_setup - t_gr));
     atomicAdd(a.stats + ST_CUT_ROUNDS, (unsigned long long)round);
+    atomicAdd(a.stats + ST_CUT_NODES, (unsigned long long)n);
+    atomicAdd(a.stats + ST_CUT_ACTIVE, (unsigned long long)nactive);
     atomicAdd(a.stats + ST_CUT_LEVELS, (unsigned long long)levels);
     atomicAdd(a.stats + ST_CUT_CTAS, 1ull);
     atomicMax(a.stats + ST_CUT_MAXROUNDS, (unsigned long long)round);
     atomicMax(a.stats + ST_CUT_MAXLEVELS, (unsigned long long)levels);
   }
   // ---- mask: not sink side ----
-  const HT* hc = cur ? h1 : h0;
   uint8_t* out = a.out + ((int64_t)y * 6 + s_id) * a.slabmax;
   for (int u = threadIdx.x; u < n; u += blockDim.x) {
     const int k = g.kind(u);

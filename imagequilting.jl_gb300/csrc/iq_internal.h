@@ -87,7 +87,9 @@ enum IqStat { ST_CUT_ROUNDS = 0, ST_CUT_LEVELS, ST_CUT_CTAS, ST_PICK_ITERS, ST_P
               // relabel rounds, global relabels
               ST_CUT_TSETUP, ST_CUT_TROUNDS, ST_CUT_TGR,
               // pick, SM cycles summed over CTAs: selection + compaction, tau-model weights, draw
-              ST_PICK_TSEL, ST_PICK_TW, ST_PICK_TDRAW, ST_COUNT };
+              ST_PICK_TSEL, ST_PICK_TW, ST_PICK_TDRAW,
+              // graph cut: active nodes summed over rounds, node count of the slabs
+              ST_CUT_ACTIVE, ST_CUT_NODES, ST_COUNT };
 
 // scratch slot ids
 enum IqSlot {
