@@ -199,6 +199,25 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t (&r)[16]) {
   asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 }
 
+// two 16-column loads (columns taddr0.., taddr1..) and one wait
+__device__ __forceinline__ void tmem_ld16x2(uint32_t taddr0, uint32_t taddr1, uint32_t (&r)[32]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,"
+      "%15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+        "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr0));
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,"
+      "%15}, [%16];"
+      : "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]),
+        "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]),
+        "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+      : "r"(taddr1));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
+
 // v = hi + lo with both halves rounded to TF32 (11 significant bits, ties away from zero).
 __device__ __forceinline__ void tf32_split(float v, uint32_t& hi, uint32_t& lo) {
   hi = (__float_as_uint(v) + 0x1000u) & 0xFFFFE000u;
@@ -663,37 +682,67 @@ __global__ void __launch_bounds__(TC_THREADS, 1) corr_tc_kernel(const TcArgs a) 
       const bool valid = rel < a.Lp && x < a.dx;
       const int64_t pout = valid ? x + a.dx * (y + a.dy * z) : 0;
       const bool dis = valid && a.disabled != nullptr && a.disabled[pout];
+      // this warp's 16-column chunks are c0 = 16 half + 32 k; two are loaded per wait
+      int pbox = -1;
+      float a2v = 0.f;
 #pragma unroll 1
-      for (int c0 = 16 * half; c0 < N; c0 += 32) {
-        uint32_t r[16];
+      for (int c0 = 16 * half; c0 < N; c0 += 64) {
+        const bool two = c0 + 32 < N;
+        uint32_t r[32];
         if (a.nstage > 0) {
-          tmem_ld16(tmem + ((uint32_t)(32 * lq) << 16) + (uint32_t)(mb * N + c0), r);
+          const uint32_t base = tmem + ((uint32_t)(32 * lq) << 16) + (uint32_t)(mb * N);
+          tmem_ld16x2(base + (uint32_t)c0, base + (uint32_t)(two ? c0 + 32 : c0), r);
         } else {
 #pragma unroll
-          for (int j = 0; j < 16; ++j) r[j] = 0u;  // no offsets: AB = 0
+          for (int j = 0; j < 32; ++j) r[j] = 0u;  // no offsets: AB = 0
         }
+        // per column: this lane's value, then a transpose-reduction over the warp (after the
+        // 5 exchange steps lane c holds the min / max of column c of the group)
+        unsigned vmn[32], vmx[32];
 #pragma unroll
-        for (int j = 0; j < 16; ++j) {
-          const int n = c0 + j;
+        for (int j = 0; j < 32; ++j) {
+          vmn[j] = 0x7F800000u;
+          vmx[j] = 0u;
+          if (j >= 16 && !two) continue;
+          const int n = j < 16 ? c0 + j : c0 + 16 + j;  // second load: columns c0 + 32..
           float* o = s_out[n];
-          unsigned mnb = 0x7F800000u, mxb = 0u;
           if (valid && o) {
             float df;
             if (dis) {
               df = __int_as_float(0x7F800000);
             } else {
-              const float s2 = __fadd_rn(s_a2[s_box[n] * 128 * TC_MB + m], s_b2[n]);
+              const int bx = s_box[n];
+              if (bx != pbox) {  // columns are grouped by mask
+                a2v = s_a2[bx * 128 * TC_MB + m];
+                pbox = bx;
+              }
+              const float s2 = __fadd_rn(a2v, s_b2[n]);
               df = fabsf(__fmaf_rn(-a.ab2, __uint_as_float(r[j]), s2));
             }
             o[pout] = df;
-            mnb = __float_as_uint(df);
-            if (mnb < 0x7F800000u) mxb = mnb;
+            vmn[j] = __float_as_uint(df);
+            if (vmn[j] < 0x7F800000u) vmx[j] = vmn[j];
           }
-          const unsigned m1 = __reduce_min_sync(0xffffffffu, mnb);
-          const unsigned m2 = __reduce_max_sync(0xffffffffu, mxb);
-          if (lane == 0 && o) {
-            if (m1 != 0x7F800000u) atomicMin(s_mn + n, m1);
-            if (m2 != 0u) atomicMax(s_mx + n, m2);
+        }
+#pragma unroll
+        for (int d = 16; d >= 1; d >>= 1) {
+#pragma unroll
+          for (int i = 0; i < d; ++i) {
+            const bool up = lane & d;
+            const unsigned smn = up ? vmn[i] : vmn[i + d], kmn = up ? vmn[i + d] : vmn[i];
+            const unsigned smx = up ? vmx[i] : vmx[i + d], kmx = up ? vmx[i + d] : vmx[i];
+            vmn[i] = min(kmn, __shfl_xor_sync(0xffffffffu, smn, d));
+            vmx[i] = max(kmx, __shfl_xor_sync(0xffffffffu, smx, d));
+          }
+        }
+        {
+          const int j = lane;  // the group's column this lane now holds
+          if (j < 16 || two) {
+            const int n = j < 16 ? c0 + j : c0 + 16 + j;
+            if (s_out[n]) {
+              if (vmn[0] != 0x7F800000u) atomicMin(s_mn + n, vmn[0]);
+              if (vmx[0] != 0u) atomicMax(s_mx + n, vmx[0]);
+            }
           }
         }
       }
