@@ -96,7 +96,7 @@ enum IqSlot {
   S_SIM = 0, S_CUT, S_D, S_DHARD, S_SOFT, S_TV, S_B2, S_KLIST, S_MINMAX, S_PICK_CAND,
   S_PICK_K0, S_PICK_V0, S_PICK_K1, S_PICK_V1, S_PICK_W, S_PICK_PROD, S_RIND, S_NCAND,
   S_CUTBUF, S_CUTSCR, S_DIS, S_AUX, S_AUXTI, S_AUXII, S_HARDLIST, S_HARDPTS, S_OUT,
-  S_TMP0, S_TMP1, S_TMP2, S_STARTS, S_SOFTMM, S_TASKS, S_VOX, S_TCB, S_TCCOLS, S_TCSTAGE, S_TCB2, S_TCFLAG, S_TCSOFT,
+  S_TMP0, S_TMP1, S_TMP2, S_STARTS, S_SOFTMM, S_TASKS, S_VOX, S_TCB, S_TCCOLS, S_TCSTAGE, S_TCB2, S_TCFLAG, S_TCSOFT, S_SOFTKEYS,
   S_COUNT
 };
 
@@ -269,6 +269,10 @@ struct PickTask {
   int64_t aux_rs[IQ_MAX_AUX];
   const unsigned* aux_mm[IQ_MAX_AUX];
   int64_t aux_mm_rs[IQ_MAX_AUX];
+  // selection keys of aux j, (value bits << 32 | index), precomputed for the first nkeys steps
+  // of the normal softdbsize sequence (sources shared by all realizations; nullable)
+  const unsigned long long* aux_keys[IQ_MAX_AUX];
+  int nkeys;
   int64_t tile;                             // Philox counter of the draw
 };
 
@@ -299,6 +303,12 @@ struct PickLaunch {
   unsigned long long* stats = nullptr;  // profiling counters (nullable)
 };
 int iq_launch_pick(iq_ctx* ctx, const PickLaunch& L);
+
+// Selection keys of nmaps maps of P floats (map m at maps + m * P, its [min, max finite] bits
+// at mm + 2 m) for the sizes seq[0..nq): keys[m * nq + q] (iq_pick.cu)
+constexpr int IQ_PRE_KEYS = 3;  // softdbsize steps precomputed per shared map
+int iq_launch_select_keys(iq_ctx* ctx, const float* maps, const unsigned* mm, int64_t nmaps,
+                          int64_t P, const int64_t* seq, int nq, unsigned long long* keys);
 
 // ---------------------------------------------------------------------------------------
 // Graph cut (iq_graphcut.cu) and paste (iq_paste.cu)

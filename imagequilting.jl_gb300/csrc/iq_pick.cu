@@ -665,7 +665,8 @@ __global__ void __launch_bounds__(PT) pick_kernel(const PickArgs a) {
       int j0 = 0;
       if (q == 0) {
         req[0] = SelReq{D, mm[0], mm[1], dbsize};
-        if (NAUX > 0 && naux > 0 && sz > 0 && sz < P) {
+        const bool pre0 = !allzero && tk.aux_keys[0] && q < tk.nkeys;
+        if (NAUX > 0 && naux > 0 && sz > 0 && sz < P && !pre0) {
           req[1] = SelReq{aux[0], amm[0][0], amm[0][1], sz};
           hist_select<2>(s, hist, sbuf, req, P, res);
           pr.ka[0] = res[1];
@@ -678,6 +679,11 @@ __global__ void __launch_bounds__(PT) pick_kernel(const PickArgs a) {
 #pragma unroll
       for (int j = 0; j < NAUX; ++j) {
         if (j < j0 || j >= naux) continue;
+        if (!allzero && tk.aux_keys[j] && q < tk.nkeys) {  // shared source: key precomputed
+          const unsigned long long kk = tk.aux_keys[j][q];
+          pr.ka[j] = Key{(uint32_t)(kk >> 32), (uint32_t)kk};
+          continue;
+        }
         if (sz >= P) { pr.ka[j] = Key{0xFFFFFFFFu, 0xFFFFFFFFu}; continue; }
         if (sz <= 0) { pr.ka[j] = Key{0u, 0u}; continue; }
         req[0] = SelReq{aux[j], amm[j][0], amm[j][1], sz};
@@ -759,6 +765,40 @@ __global__ void __launch_bounds__(PT) pick_kernel(const PickArgs a) {
   }
 }
 
+// One CTA per (map, sequence step): the key of the k-th smallest (value, index) of the map, as
+// the relaxation in pick_kernel computes it (k >= P: everything; k <= 0: nothing).
+struct KeyArgs {
+  const float* maps;
+  const unsigned* mm;
+  int64_t P;
+  int nq;
+  int64_t seq[IQ_PRE_KEYS];
+  unsigned long long* keys;
+};
+
+__global__ void __launch_bounds__(PT) select_keys_kernel(const KeyArgs a) {
+  __shared__ Smem s;
+  extern __shared__ __align__(16) unsigned char dyn[];
+  uint32_t* hist = reinterpret_cast<uint32_t*>(dyn);
+  unsigned long long* sbuf = reinterpret_cast<unsigned long long*>(dyn + 2 * NBIN * 4);
+  const int64_t m = blockIdx.x / a.nq;
+  const int q = blockIdx.x % a.nq;
+  const int64_t k = a.seq[q];
+  Key key;
+  if (k >= a.P) {
+    key = Key{0xFFFFFFFFu, 0xFFFFFFFFu};
+  } else if (k <= 0) {
+    key = Key{0u, 0u};
+  } else {
+    SelReq req[1] = {SelReq{a.maps + m * a.P, a.mm[2 * m], a.mm[2 * m + 1], k}};
+    Key res[1];
+    hist_select<1>(s, hist, sbuf, req, a.P, res);
+    key = res[0];
+  }
+  if (threadIdx.x == 0)
+    a.keys[m * a.nq + q] = ((unsigned long long)key.v << 32) | key.i;
+}
+
 template <int NAUX>
 cudaError_t launch_pick_t(const PickArgs& a, int nblocks, cudaStream_t st) {
   static bool attr = false;
@@ -807,5 +847,26 @@ int iq_launch_pick(iq_ctx* ctx, const PickLaunch& L) {
   iq_timer_stop(ctx, "pick", 4.0 * (double)L.P * (double)(1 + naux) * (double)nblocks);
   iq_count(ctx);
   if (e != cudaSuccess) return iq_set_error(IQ_ERR_CUDA, "pick launch: %s", cudaGetErrorString(e));
+  return IQ_OK;
+}
+
+int iq_launch_select_keys(iq_ctx* ctx, const float* maps, const unsigned* mm, int64_t nmaps,
+                          int64_t P, const int64_t* seq, int nq, unsigned long long* keys) {
+  if (nmaps <= 0 || nq <= 0) return IQ_OK;
+  if (nq > IQ_PRE_KEYS) return iq_set_error(IQ_ERR_ARG, "too many precomputed keys");
+  KeyArgs a;
+  a.maps = maps; a.mm = mm; a.P = P; a.nq = nq; a.keys = keys;
+  for (int q = 0; q < IQ_PRE_KEYS; ++q) a.seq[q] = q < nq ? seq[q] : 0;
+  static bool attr = false;
+  if (!attr) {
+    IQ_CUDA_OK(cudaFuncSetAttribute(select_keys_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)DYN_BYTES));
+    attr = true;
+  }
+  iq_timer_start(ctx, "pick");
+  select_keys_kernel<<<(unsigned)(nmaps * nq), PT, DYN_BYTES, ctx->stream>>>(a);
+  iq_timer_stop(ctx, "pick", 0);
+  iq_count(ctx);
+  IQ_CUDA_OK(cudaGetLastError());
   return IQ_OK;
 }

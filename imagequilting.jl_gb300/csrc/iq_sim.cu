@@ -772,6 +772,21 @@ extern "C" int iq_simulate(iq_ctx* ctx, const iq_sim_params* p, const iq_hard_da
     }
   }
 
+  // ---- relaxation sizes; selection keys of the soft maps (shared by all realizations) for
+  // the first steps of the softdbsize sequence, computed once instead of per realization ----
+  int64_t dbn = 0, dbz = 0;
+  int nsn = 0, nsz = 0;
+  int64_t seqn[IQ_MAX_SEQ], seqz[IQ_MAX_SEQ];
+  if (npat > 0) iq_relax_sizes(npat, p->tol, dbn, dbz, nsn, seqn, nsz, seqz);
+  const int nkeys = std::min(nsn, IQ_PRE_KEYS);
+  unsigned long long* d_softkeys = nullptr;
+  if (nsoft > 0 && npat > 0 && nkeys > 0 && nslot > 0) {
+    d_softkeys = (unsigned long long*)iq_scratch(ctx, S_SOFTKEYS,
+                                                 sizeof(unsigned long long) * nslot * nsoft * nkeys);
+    if (!d_softkeys) return IQ_ERR_ALLOC;
+    RET_IF(iq_launch_select_keys(ctx, d_soft, d_softmm, nslot * nsoft, P, seqn, nkeys, d_softkeys));
+  }
+
   // ---- task descriptors of every step, uploaded once ----
   const int64_t nsteps = (int64_t)steps.size();
   std::vector<GatherTask> gt(nsteps), hgt;
@@ -818,6 +833,7 @@ extern "C" int iq_simulate(iq_ctx* ctx, const iq_sim_params* p, const iq_hard_da
         const int64_t slot = (int64_t)sv * nslot + slot_of[s.tile];
         q.aux[na] = d_soft + slot * P; q.aux_rs[na] = 0;
         q.aux_mm[na] = d_softmm + 2 * slot; q.aux_mm_rs[na] = 0;
+        if (d_softkeys) { q.aux_keys[na] = d_softkeys + slot * nkeys; q.nkeys = nkeys; }
         ++na;
       }
       q.naux = na;
@@ -852,10 +868,6 @@ extern "C" int iq_simulate(iq_ctx* ctx, const iq_sim_params* p, const iq_hard_da
   IQ_CUDA_OK(cudaGetLastError());
 
   // ---- the tile loop (src/iqsim.jl:172-285), one dependency level chunk at a time ----
-  int64_t dbn = 0, dbz = 0;
-  int nsn = 0, nsz = 0;
-  int64_t seqn[IQ_MAX_SEQ], seqz[IQ_MAX_SEQ];
-  if (npat > 0) iq_relax_sizes(npat, p->tol, dbn, dbz, nsn, seqn, nsz, seqz);
   for (int64_t c = 0; c < nchunk; ++c) {
     const int64_t k0 = cbeg[c];
     const int m = (int)(cbeg[c + 1] - cbeg[c]);
