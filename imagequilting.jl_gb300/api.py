@@ -102,9 +102,10 @@ class Context:
         return int(load().iq_ctx_launches(self.h))
 
     def set_option(self, name, value):
-        """Set a knob of this context (include/iqgpu.h lists them). Launch shapes and chunk
-        sizes leave results unchanged; `corr.engine` (tensor cores vs SIMT) changes continuous
-        distances within the stated tolerance and integer-data results not at all."""
+        """Set a knob of this context (include/iqgpu.h lists them). Launch shapes, chunk sizes,
+        stream groups and `corr.engine` (tensor cores vs SIMT) change how the distances are
+        summed: continuous distances move within the stated tolerance, integer-data results not
+        at all."""
         check(load().iq_set_option(self.h, name.encode(), int(value)))
 
 

@@ -201,6 +201,12 @@ extern "C" int iq_ctx_destroy(iq_ctx* ctx) {
     for (auto e : kv.second.ev) cudaEventDestroy(e);
   cudaFree(ctx->d_status);
   cudaFree(ctx->d_stats);
+  if (ctx->stream2) {
+    cudaStreamSynchronize(ctx->stream2);
+    cudaStreamDestroy(ctx->stream2);
+  }
+  if (ctx->ev_fork) cudaEventDestroy(ctx->ev_fork);
+  if (ctx->ev_join) cudaEventDestroy(ctx->ev_join);
   cudaStreamDestroy(ctx->stream);
   delete ctx;
   return IQ_OK;
@@ -238,6 +244,11 @@ extern "C" int iq_set_option(iq_ctx* ctx, const char* name, int64_t value) {
   if (!strcmp(name, "sim.level_chunk")) {
     if (value < 1 || value > 4096) return iq_set_error(IQ_ERR_ARG, "level_chunk out of range");
     ctx->level_chunk = value;
+    return IQ_OK;
+  }
+  if (!strcmp(name, "sim.streams")) {
+    if (value < 1 || value > 2) return iq_set_error(IQ_ERR_ARG, "sim.streams must be 1 or 2");
+    ctx->sim_streams = (int)value;
     return IQ_OK;
   }
   return iq_set_error(IQ_ERR_ARG, "unknown option '%s'", name);

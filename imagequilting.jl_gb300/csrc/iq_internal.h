@@ -74,6 +74,9 @@ struct iq_ctx {
   int corr_engine = 2;          // box-mask distances: 2 tensor cores FP16 halves when the data's
                                 // range allows (else TF32), 1 tensor cores TF32, 0 SIMT
   int64_t max_steps = -1;       // tiles simulated per realization (< 0: all)
+  int sim_streams = 1;          // realization groups of iq_simulate, each on its own stream
+  cudaStream_t stream2 = nullptr;  // stream of the second realization group (made on first use)
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
 };
 enum IqStat { ST_CUT_ROUNDS = 0, ST_CUT_LEVELS, ST_CUT_CTAS, ST_PICK_ITERS, ST_PICK_CAND,
               ST_PICK_CTAS, ST_CUT_MAXROUNDS, ST_CUT_MAXLEVELS,

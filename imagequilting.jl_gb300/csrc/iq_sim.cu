@@ -481,16 +481,26 @@ extern "C" int iq_simulate(iq_ctx* ctx, const iq_sim_params* p, const iq_hard_da
   int64_t cmax = 1;
   for (int64_t c = 0; c < nchunk; ++c) cmax = std::max(cmax, cbeg[c + 1] - cbeg[c]);
 
+  // Realization groups: realizations never read one another, so with the tensor-core path two
+  // groups run on two streams, interleaved chunk by chunk. One group's pick and cut then share
+  // the GPU with the other group's correlation, and the tail of each launch is filled by the
+  // other stream's work. Group g holds realizations [gb[g], gb[g+1]).
+  const int ngrp = (tc && T > 0 && R >= 2 && ctx->sim_streams >= 2) ? 2 : 1;
+  const int gb[3] = {0, ngrp == 2 ? (R + 1) / 2 : R, R};
+  // hard-data distance maps depend on the data only: one map per data tile, made up front
+  int64_t nhs = 0;
+  for (const Step& s : steps) nhs += s.hardtile ? 1 : 0;
+
   // ---- device buffers ----
   const bool debug = p->debug != 0 && (cuts || voxs);
   float* d_sim = (float*)iq_scratch(ctx, S_SIM, sizeof(float) * padvol * R);
   float* d_cut = debug ? (float*)iq_scratch(ctx, S_CUT, sizeof(float) * padvol * R) : nullptr;
   float* d_D = (float*)iq_scratch(ctx, S_D, sizeof(float) * P * R * cmax);
-  float* d_Dh = (float*)iq_scratch(ctx, S_DHARD, sizeof(float) * P * cmax);
-  float* d_tv = (float*)iq_scratch(ctx, S_TV, sizeof(float) * T * (std::max(rpad, 16) * cmax + cmax));
-  double* d_b2 = (double*)iq_scratch(ctx, S_B2, sizeof(double) * (std::max(rpad, 16) * cmax + cmax));
+  float* d_Dh = (float*)iq_scratch(ctx, S_DHARD, sizeof(float) * P * std::max<int64_t>(nhs, 1));
+  float* d_tv = (float*)iq_scratch(ctx, S_TV, sizeof(float) * T * (std::max(rpad, 16) * cmax + nhs));
+  double* d_b2 = (double*)iq_scratch(ctx, S_B2, sizeof(double) * (std::max(rpad, 16) * cmax + nhs));
   uint32_t* d_kl = (uint32_t*)iq_scratch(ctx, S_KLIST, sizeof(uint32_t) * klist.size());
-  unsigned* d_mm = (unsigned*)iq_scratch(ctx, S_MINMAX, sizeof(unsigned) * 2 * (R + 1) * cmax);
+  unsigned* d_mm = (unsigned*)iq_scratch(ctx, S_MINMAX, sizeof(unsigned) * 2 * (R * cmax + nhs));
   uint32_t* d_hk = (uint32_t*)iq_scratch(ctx, S_HARDLIST, sizeof(uint32_t) * hk.size());
   float* d_hkv = (float*)iq_scratch(ctx, S_HARDPTS, sizeof(float) * hkv.size());
   const size_t pk = (size_t)P * R * cmax;
@@ -510,6 +520,9 @@ extern "C" int iq_simulate(iq_ctx* ctx, const iq_sim_params* p, const iq_hard_da
       !d_ncand || !d_cutbuf || (cutscr_per && !d_cutscr))
     return IQ_ERR_ALLOC;
   float* d_tvh = d_tv + (size_t)T * std::max(rpad, 16) * cmax;  // hard templates (T x 1 each)
+  // per-step scratch of group g starts at its first realization's share
+  auto grp_pick = [&](int g) { return (size_t)gb[g] * cmax * P; };
+  auto grp_rind = [&](int g) { return (size_t)gb[g] * cmax; };
   double* d_b2h = d_b2 + (size_t)std::max(rpad, 16) * cmax;
   unsigned* d_mmh = d_mm + 2 * R * cmax;
   IQ_CUDA_OK(cudaMemsetAsync(d_sim, 0, sizeof(float) * padvol * R, st));
@@ -552,21 +565,24 @@ extern "C" int iq_simulate(iq_ctx* ctx, const iq_sim_params* p, const iq_hard_da
   };
   std::vector<TcRun> tcruns;
   std::vector<TcCol> tccols;
-  std::vector<int64_t> tcbeg(nchunk + 1, 0);
+  std::vector<int64_t> tcbeg(nchunk * ngrp + 1, 0);  // launches of (chunk c, group g): c * ngrp + g
   std::vector<uint8_t> chunk_tc(nchunk, 0);
   // Every chunk runs its overlap distances on the tensor cores: the (tile, realization)
-  // columns of the chunk, grouped by mask, in launches of at most 256 columns and 8 masks
-  // with balanced widths. A tile without pasted neighbours (mask box = the whole tile) gets
-  // zero templates and A2 = B2 = 0, i.e. D = 0 like the reference's empty overlap.
-  for (int64_t c = 0; c < nchunk && tc; ++c) {
-    const bool ok = T > 0;
+  // columns of the chunk and group, grouped by mask, in launches of at most 256 columns and
+  // 8 masks with balanced widths. A tile without pasted neighbours (mask box = the whole tile)
+  // gets zero templates and A2 = B2 = 0, i.e. D = 0 like the reference's empty overlap.
+  for (int64_t cg = 0; cg < nchunk * ngrp; ++cg) {
+    const int64_t c = cg / ngrp;
+    const int grp = (int)(cg % ngrp);
+    const int Rg = gb[grp + 1] - gb[grp];
+    const bool ok = tc && T > 0;
     chunk_tc[c] = ok;
     if (ok) {
       std::vector<std::pair<int, int64_t>> order;  // (cfg, step index in chunk) sorted by cfg
       for (int64_t k = cbeg[c]; k < cbeg[c + 1]; ++k) order.push_back({steps[k].cfg, k - cbeg[c]});
       std::stable_sort(order.begin(), order.end(),
                        [](const std::pair<int, int64_t>& x, const std::pair<int, int64_t>& y) { return x.first < y.first; });
-      const int64_t ncols = (int64_t)order.size() * R;
+      const int64_t ncols = (int64_t)order.size() * Rg;
       const int64_t nl = (ncols + IQ_TC_MAXN - 1) / IQ_TC_MAXN;
       const int64_t per = std::min<int64_t>(IQ_TC_MAXN, ((ncols + nl - 1) / nl + 15) / 16 * 16);
       int64_t q = 0;
@@ -577,7 +593,7 @@ extern "C" int iq_simulate(iq_ctx* ctx, const iq_sim_params* p, const iq_hard_da
         int64_t cnt = 0;
         double fl = 0;
         while (q < ncols && cnt < per) {
-          const int cf = order[q / R].first;
+          const int cf = order[q / Rg].first;
           int bid = -1;
           for (size_t j = 0; j < run.cfgset.size(); ++j) if (run.cfgset[j] == cf) bid = (int)j;
           if (bid < 0) {
@@ -585,7 +601,7 @@ extern "C" int iq_simulate(iq_ctx* ctx, const iq_sim_params* p, const iq_hard_da
             run.cfgset.push_back(cf);
             bid = (int)run.cfgset.size() - 1;
           }
-          const int64_t i = order[q / R].second, r = q % R;
+          const int64_t i = order[q / Rg].second, r = gb[grp] + q % Rg;
           tccols.push_back(TcCol{r * padvol + steps[cbeg[c] + i].startlin,
                                  d_D + ((size_t)i * R + r) * P, d_b2 + (size_t)i * rpad + r,
                                  d_mm + (size_t)i * R * 2 + 2 * r, bid, 0});
@@ -600,7 +616,7 @@ extern "C" int iq_simulate(iq_ctx* ctx, const iq_sim_params* p, const iq_hard_da
         tcruns.push_back(run);
       }
     }
-    tcbeg[c + 1] = (int64_t)tcruns.size();
+    tcbeg[cg + 1] = (int64_t)tcruns.size();
   }
   const TcStageRef soft_st = (tc && nsoft > 0 && T > 0) ? stages_for(std::vector<int>{ncfg})
                                                          : TcStageRef{0, 0, 0, 0, 0, 0};
@@ -612,11 +628,12 @@ extern "C" int iq_simulate(iq_ctx* ctx, const iq_sim_params* p, const iq_hard_da
     sim_stats.merge(iq_host_stats(hvf.data(), nh));
   }
   uint32_t* d_tcst = nullptr;  // stage words of every list, then their prefixes
-  void* d_tcb = nullptr;        // packed templates of one launch
+  void* d_tcb = nullptr;        // packed templates of one launch, per group
+  size_t tcb_bytes = 0;
   double* d_tcb2 = nullptr;     // squared sums of the soft templates of one launch
   TcCol* d_tccols = nullptr;
-  if (tc && !tc_word.empty()) {
-    const size_t ns = tc_word.size();
+  // (a simulation of one tile has columns but no stages: its launches only write D = 0)
+  if (tc && (!tc_word.empty() || !tccols.empty())) {
     std::vector<uint32_t> both(tc_word);
     both.insert(both.end(), tc_pre.begin(), tc_pre.end());
     both.insert(both.end(), tc_w16.begin(), tc_w16.end());
@@ -624,14 +641,16 @@ extern "C" int iq_simulate(iq_ctx* ctx, const iq_sim_params* p, const iq_hard_da
     for (const TcRun& u : tcruns)
       bmax = std::max<int64_t>(bmax, std::max(u.st.nsteps, u.st.nsteps16) * 64 * u.N);
     bmax = std::max<int64_t>(bmax, std::max(soft_st.nsteps, soft_st.nsteps16) * 64 * IQ_TC_MAXN);
-    d_tcst = (uint32_t*)iq_scratch(ctx, S_TCSTAGE, sizeof(uint32_t) * both.size());
-    d_tcb = iq_scratch(ctx, S_TCB, (size_t)bmax);
+    tcb_bytes = (size_t)(bmax + 255) / 256 * 256;  // one packed-template buffer per group
+    d_tcst = (uint32_t*)iq_scratch(ctx, S_TCSTAGE, sizeof(uint32_t) * std::max<size_t>(both.size(), 1));
+    d_tcb = iq_scratch(ctx, S_TCB, tcb_bytes * ngrp);
     d_tcb2 = (double*)iq_scratch(ctx, S_TCB2, sizeof(double) * IQ_TC_MAXN);
     if (!d_tcst || !d_tcb || !d_tcb2) return IQ_ERR_ALLOC;
-    IQ_CUDA_OK(cudaMemcpyAsync(d_tcst, both.data(), sizeof(uint32_t) * both.size(),
-                               cudaMemcpyHostToDevice, st));
-    IQ_CUDA_OK(cudaStreamSynchronize(st));  // `both` is a host vector
-    (void)ns;
+    if (!both.empty()) {
+      IQ_CUDA_OK(cudaMemcpyAsync(d_tcst, both.data(), sizeof(uint32_t) * both.size(),
+                                 cudaMemcpyHostToDevice, st));
+      IQ_CUDA_OK(cudaStreamSynchronize(st));  // `both` is a host vector
+    }
     if (!tccols.empty()) {
       d_tccols = (TcCol*)iq_scratch(ctx, S_TCCOLS, sizeof(TcCol) * tccols.size());
       if (!d_tccols) return IQ_ERR_ALLOC;
@@ -643,7 +662,7 @@ extern "C" int iq_simulate(iq_ctx* ctx, const iq_sim_params* p, const iq_hard_da
   auto tc_launch = [&](const std::vector<int>& cfgset, const TcStageRef& sr, const float* img,
                        const double* ii, const float* grid, Dim3 gdims, const TcCol* cols, int N,
                        const IqValueStats& img_stats, const IqValueStats& tmpl_stats,
-                       double flops) -> int {
+                       double flops, void* B) -> int {
     TcCorrLaunch L;
     L.img = img; L.img_dims = ctx->ti; L.out_dims = distD; L.tile = tileD; L.ii = ii;
     L.nbox = (int)cfgset.size();
@@ -656,7 +675,7 @@ extern "C" int iq_simulate(iq_ctx* ctx, const iq_sim_params* p, const iq_hard_da
     L.stage16 = d_tcst + 2 * tc_word.size() + sr.off16;
     L.nstage16 = sr.nstage16;
     L.nsteps16 = sr.nsteps16;
-    L.grid = grid; L.grid_dims = gdims; L.cols = cols; L.N = N; L.B = d_tcb;
+    L.grid = grid; L.grid_dims = gdims; L.cols = cols; L.N = N; L.B = B;
     L.img_stats = img_stats; L.tmpl_stats = tmpl_stats; L.flops = flops;
     return iq_launch_corr_tc(ctx, L);
   };
@@ -747,7 +766,7 @@ extern "C" int iq_simulate(iq_ctx* ctx, const iq_sim_params* p, const iq_hard_da
           RET_IF(iq_launch_gather(ctx, G));
           RET_IF(tc_launch(std::vector<int>{ncfg}, soft_st, d_auxti[s], d_auxii[s], d_aux[s], psz,
                            d_cols + launches[l].first, launches[l].second, auxti_stats, aux_stats,
-                           2.0 * (double)P * (double)T * nb));
+                           2.0 * (double)P * (double)T * nb, d_tcb));
         }
         IQ_CUDA_OK(cudaStreamSynchronize(st));  // `cols` is a host vector
       } else {
@@ -788,16 +807,17 @@ extern "C" int iq_simulate(iq_ctx* ctx, const iq_sim_params* p, const iq_hard_da
   }
 
   // ---- task descriptors of every step, uploaded once ----
+  // Gather and pick tasks point at per-realization slots: each group has its own copy, whose
+  // pointers start at the group's first realization. Cut and paste tasks are shared.
   const int64_t nsteps = (int64_t)steps.size();
-  std::vector<GatherTask> gt(nsteps), hgt;
+  std::vector<GatherTask> gt(nsteps * ngrp), hgt;
   std::vector<CorrTask> ct(nsteps), hct;
-  std::vector<PickTask> pt(nsteps);
+  std::vector<PickTask> pt(nsteps * ngrp);
   std::vector<StepTask> stk(nsteps);
-  std::vector<int64_t> hbeg(nchunk + 1, 0);  // hard tasks of chunk c: [hbeg[c], hbeg[c+1])
   std::vector<double> cflops(nchunk, 0.0);
   std::vector<int> cslab(nchunk, 0), chard(nchunk, 0);
+  int64_t hi = 0;  // slot of the next data tile's hard-data map
   for (int64_t c = 0; c < nchunk; ++c) {
-    int hi = 0;
     for (int64_t k = cbeg[c]; k < cbeg[c + 1]; ++k) {
       const Step& s = steps[k];
       const int64_t i = k - cbeg[c];
@@ -806,14 +826,11 @@ extern "C" int iq_simulate(iq_ctx* ctx, const iq_sim_params* p, const iq_hard_da
       double* b2 = d_b2 + (size_t)i * rpad;
       unsigned* mm = d_mm + (size_t)i * R * 2;
       float* D = d_D + (size_t)i * R * P;
-      gt[k] = GatherTask{d_kl + (size_t)s.cfg * T, m.K, s.startlin, nullptr, tv, b2, mm};
       ct[k] = CorrTask{d_kl + (size_t)s.cfg * T, m.K, tv, b2, ctx->d_ti2ii,
                        {m.lo[0], m.lo[1], m.lo[2]}, {m.hi[0], m.hi[1], m.hi[2]}, D, mm};
       cflops[c] += 2.0 * (double)P * (double)m.K * (double)R;
-      PickTask& q = pt[k];
-      memset(&q, 0, sizeof(q));
-      q.tile = s.tile;
-      int na = 0;
+      const float* Dh = nullptr;
+      const unsigned* mmh = nullptr;
       if (s.hardtile) {
         const int64_t h0 = hoff[s.tile], hn = hoff[s.tile + 1] - hoff[s.tile];
         float* tvh = d_tvh + (size_t)hi * T;
@@ -821,35 +838,44 @@ extern "C" int iq_simulate(iq_ctx* ctx, const iq_sim_params* p, const iq_hard_da
         hct.push_back(CorrTask{d_hk + h0, (int)hn, tvh, d_b2h + hi, nullptr, {0, 0, 0}, {0, 0, 0},
                                d_Dh + (size_t)hi * P, d_mmh + 2 * hi});
         cflops[c] += 2.0 * (double)P * (double)hn;
-        q.D0 = d_Dh + (size_t)hi * P; q.D0_rs = 0; q.mm0 = d_mmh + 2 * hi; q.mm0_rs = 0;
-        q.aux[na] = D; q.aux_rs[na] = P; q.aux_mm[na] = mm; q.aux_mm_rs[na] = 2;
-        ++na;
+        Dh = d_Dh + (size_t)hi * P;
+        mmh = d_mmh + 2 * hi;
         ++hi;
         chard[c] = 1;
-      } else {
-        q.D0 = D; q.D0_rs = P; q.mm0 = mm; q.mm0_rs = 2;
       }
-      for (int sv = 0; sv < nsoft; ++sv) {
-        const int64_t slot = (int64_t)sv * nslot + slot_of[s.tile];
-        q.aux[na] = d_soft + slot * P; q.aux_rs[na] = 0;
-        q.aux_mm[na] = d_softmm + 2 * slot; q.aux_mm_rs[na] = 0;
-        if (d_softkeys) { q.aux_keys[na] = d_softkeys + slot * nkeys; q.nkeys = nkeys; }
-        ++na;
+      for (int grp = 0; grp < ngrp; ++grp) {
+        const int64_t r0 = gb[grp];
+        gt[grp * nsteps + k] = GatherTask{d_kl + (size_t)s.cfg * T, m.K, s.startlin, nullptr,
+                                          chunk_tc[c] ? nullptr : tv, b2 + r0, mm + 2 * r0};
+        PickTask& q = pt[grp * nsteps + k];
+        memset(&q, 0, sizeof(q));
+        q.tile = s.tile;
+        int na = 0;
+        if (s.hardtile) {
+          q.D0 = Dh; q.D0_rs = 0; q.mm0 = mmh; q.mm0_rs = 0;
+          q.aux[na] = D + r0 * P; q.aux_rs[na] = P; q.aux_mm[na] = mm + 2 * r0; q.aux_mm_rs[na] = 2;
+          ++na;
+        } else {
+          q.D0 = D + r0 * P; q.D0_rs = P; q.mm0 = mm + 2 * r0; q.mm0_rs = 2;
+        }
+        for (int sv = 0; sv < nsoft; ++sv) {
+          const int64_t slot = (int64_t)sv * nslot + slot_of[s.tile];
+          q.aux[na] = d_soft + slot * P; q.aux_rs[na] = 0;
+          q.aux_mm[na] = d_softmm + 2 * slot; q.aux_mm_rs[na] = 0;
+          if (d_softkeys) { q.aux_keys[na] = d_softkeys + slot * nkeys; q.nkeys = nkeys; }
+          ++na;
+        }
+        q.naux = na;
       }
-      q.naux = na;
       StepTask& sk = stk[k];
       sk.start = s.startlin;
       sk.nslab = s.nslab;
       for (int j = 0; j < 6; ++j) sk.slab[j] = s.slab[j];
       cslab[c] = std::max(cslab[c], s.nslab);
     }
-    hbeg[c + 1] = hbeg[c] + hi;
   }
-  for (int64_t c = 0; c < nchunk; ++c)
-    if (chunk_tc[c])
-      for (int64_t k = cbeg[c]; k < cbeg[c + 1]; ++k) gt[k].tv = nullptr;  // only B2 and min/max
-  const size_t tbytes = sizeof(GatherTask) * (nsteps + hgt.size()) + sizeof(CorrTask) * (nsteps + hct.size()) +
-                        sizeof(PickTask) * nsteps + sizeof(StepTask) * nsteps + 6 * 256;
+  const size_t tbytes = sizeof(GatherTask) * (gt.size() + hgt.size()) + sizeof(CorrTask) * (nsteps + hct.size()) +
+                        sizeof(PickTask) * pt.size() + sizeof(StepTask) * nsteps + 6 * 256;
   char* d_tasks = (char*)iq_scratch(ctx, S_TASKS, tbytes);
   if (!d_tasks) return IQ_ERR_ALLOC;
   size_t toff = 0;
@@ -859,79 +885,114 @@ extern "C" int iq_simulate(iq_ctx* ctx, const iq_sim_params* p, const iq_hard_da
     toff += (bytes + 255) & ~(size_t)255;
     return dst;
   };
-  const GatherTask* d_gt = (const GatherTask*)put(gt.data(), sizeof(GatherTask) * nsteps);
+  const GatherTask* d_gt = (const GatherTask*)put(gt.data(), sizeof(GatherTask) * gt.size());
   const CorrTask* d_ct = (const CorrTask*)put(ct.data(), sizeof(CorrTask) * nsteps);
   const GatherTask* d_hgt = (const GatherTask*)put(hgt.data(), sizeof(GatherTask) * hgt.size());
   const CorrTask* d_hct = (const CorrTask*)put(hct.data(), sizeof(CorrTask) * hct.size());
-  const PickTask* d_pt = (const PickTask*)put(pt.data(), sizeof(PickTask) * nsteps);
+  const PickTask* d_pt = (const PickTask*)put(pt.data(), sizeof(PickTask) * pt.size());
   const StepTask* d_st = (const StepTask*)put(stk.data(), sizeof(StepTask) * nsteps);
   IQ_CUDA_OK(cudaGetLastError());
 
+  // ---- hard-data distance of every data tile: data values against the TI ----
+  for (int64_t h = 0; h < (int64_t)hgt.size(); h += 32768) {
+    const int nb = (int)std::min<int64_t>(32768, (int64_t)hgt.size() - h);
+    GatherLaunch H;
+    H.ntmpl = 1; H.rpad = 1; H.ntask = nb; H.tasks = d_hgt + h;
+    RET_IF(iq_launch_gather(ctx, H));
+    CorrLaunch Ch;
+    Ch.img = ctx->d_ti; Ch.img_dims = ctx->ti; Ch.out_dims = distD; Ch.tile = tileD;
+    Ch.rpad = 1; Ch.ntmpl = 1; Ch.out_stride = P; Ch.disabled = d_dis;
+    Ch.ntask = nb; Ch.tasks = d_hct + h; Ch.flops = 1;
+    RET_IF(iq_launch_corr(ctx, Ch));
+  }
+
   // ---- the tile loop (src/iqsim.jl:172-285), one dependency level chunk at a time ----
-  for (int64_t c = 0; c < nchunk; ++c) {
-    const int64_t k0 = cbeg[c];
-    const int m = (int)(cbeg[c + 1] - cbeg[c]);
-    // overlap distance of every realization of every tile of the chunk
-    GatherLaunch G;
-    G.grid = d_sim; G.grid_dims = padD; G.grid_stride = padvol; G.ntmpl = R; G.rpad = rpad;
-    G.ntask = m; G.tasks = d_gt + k0;
-    RET_IF(iq_launch_gather(ctx, G));
-    if (chunk_tc[c]) {
-      for (int64_t l = tcbeg[c]; l < tcbeg[c + 1]; ++l) {
-        const TcRun& u = tcruns[l];
-        RET_IF(tc_launch(u.cfgset, u.st, ctx->d_ti, ctx->d_ti2ii, d_sim, padD, d_tccols + u.col0, u.N,
-                         ctx->ti_stats, sim_stats, u.flops));
+  cudaStream_t gstream[2] = {st, st};
+  if (ngrp == 2) {
+    if (!ctx->stream2) IQ_CUDA_OK(cudaStreamCreateWithFlags(&ctx->stream2, cudaStreamNonBlocking));
+    if (!ctx->ev_fork) IQ_CUDA_OK(cudaEventCreateWithFlags(&ctx->ev_fork, cudaEventDisableTiming));
+    if (!ctx->ev_join) IQ_CUDA_OK(cudaEventCreateWithFlags(&ctx->ev_join, cudaEventDisableTiming));
+    gstream[1] = ctx->stream2;
+    IQ_CUDA_OK(cudaEventRecord(ctx->ev_fork, st));  // the second group follows the set-up
+    IQ_CUDA_OK(cudaStreamWaitEvent(ctx->stream2, ctx->ev_fork, 0));
+  }
+  {
+    // Launchers use the context stream, which is switched per group. On every way out of this
+    // block it is restored and made to wait for the second group's stream.
+    struct GroupJoin {
+      iq_ctx* ctx;
+      cudaStream_t main;
+      bool on;
+      ~GroupJoin() {
+        ctx->stream = main;
+        if (on && cudaEventRecord(ctx->ev_join, ctx->stream2) == cudaSuccess)
+          cudaStreamWaitEvent(main, ctx->ev_join, 0);
       }
-    } else {
-      CorrLaunch C;
-      C.img = ctx->d_ti; C.img_dims = ctx->ti; C.out_dims = distD; C.tile = tileD;
-      C.rpad = rpad; C.ntmpl = R; C.out_stride = P; C.disabled = d_dis;
-      C.ntask = m; C.tasks = d_ct + k0; C.flops = cflops[c];
-      RET_IF(iq_launch_corr(ctx, C));
-    }
-    // hard distance of the data tiles of the chunk
-    const int nh_c = (int)(hbeg[c + 1] - hbeg[c]);
-    if (nh_c > 0) {
-      GatherLaunch H;
-      H.ntmpl = 1; H.rpad = 1; H.ntask = nh_c; H.tasks = d_hgt + hbeg[c];
-      RET_IF(iq_launch_gather(ctx, H));
-      CorrLaunch Ch;
-      Ch.img = ctx->d_ti; Ch.img_dims = ctx->ti; Ch.out_dims = distD; Ch.tile = tileD;
-      Ch.rpad = 1; Ch.ntmpl = 1; Ch.out_stride = P; Ch.disabled = d_dis;
-      Ch.ntask = nh_c; Ch.tasks = d_hct + hbeg[c]; Ch.flops = 1;
-      RET_IF(iq_launch_corr(ctx, Ch));
-    }
-    // pick
-    PickLaunch L;
-    L.P = P; L.npat = npat; L.tol = p->tol; L.seed = p->seed; L.real0 = 0; L.nreal = R;
-    L.ntask = m; L.tasks = d_pt + k0; L.naux_max = nsoft + chard[c];
-    L.dbsize_norm = dbn; L.dbsize_zero = dbz; L.nseq_norm = nsn; L.nseq_zero = nsz;
-    for (int q = 0; q < IQ_MAX_SEQ; ++q) { L.seq_norm[q] = q < nsn ? seqn[q] : 0; L.seq_zero[q] = q < nsz ? seqz[q] : 0; }
-    L.cand = d_cand; L.k0 = d_k0; L.v0 = d_v0; L.k1 = d_k1; L.v1 = d_v1; L.w = d_w; L.prod = d_prod;
-    L.rind = d_rind; L.ncand = d_ncand; L.status = ctx->d_status;
-    L.stats = ctx->prof ? ctx->d_stats : nullptr;
-    RET_IF(iq_launch_pick(ctx, L));
-    // boundary cuts
-    if (cslab[c] > 0) {
-      CutLaunch K;
-      K.nreal = R; K.ntask = m; K.nslab_max = cslab[c]; K.tasks = d_st + k0;
-      K.sim = d_sim; K.sim_dims = padD; K.sim_rstride = padvol;
-      K.ti = ctx->d_ti; K.ti_dims = ctx->ti; K.dist_dims = distD; K.rind = d_rind;
-      K.out = d_cutbuf; K.slabmax = slabmax;
-      K.scratch = d_cutscr; K.scratch_per_cta = cutscr_per;
-      K.status = ctx->d_status;
-      K.stats = ctx->prof ? ctx->d_stats : nullptr;
-      K.gr_period = ctx->cut_gr_period;
-      K.threads = ctx->cut_threads;
-      RET_IF(iq_launch_cut(ctx, K));
-    }
-    // paste
-    PasteLaunch Pl;
-    Pl.nreal = R; Pl.ntask = m; Pl.tasks = d_st + k0;
-    Pl.sim = d_sim; Pl.sim_dims = padD; Pl.sim_rstride = padvol; Pl.cut = d_cut;
-    Pl.tile = tileD; Pl.ti = ctx->d_ti; Pl.ti_dims = ctx->ti; Pl.dist_dims = distD;
-    Pl.rind = d_rind; Pl.cutbuf = d_cutbuf; Pl.slabmax = slabmax;
-    RET_IF(iq_launch_paste(ctx, Pl));
+    } join{ctx, st, ngrp == 2};
+    for (int64_t c = 0; c < nchunk; ++c)
+      for (int grp = 0; grp < ngrp; ++grp) {
+        ctx->stream = gstream[grp];
+        const int64_t k0 = cbeg[c];
+        const int m = (int)(cbeg[c + 1] - cbeg[c]);
+        const int r0 = gb[grp], Rg = gb[grp + 1] - gb[grp];
+        float* sim = d_sim + (size_t)r0 * padvol;
+        int64_t* rind = d_rind + grp_rind(grp);
+        uint8_t* cutbuf = d_cutbuf + grp_rind(grp) * 6 * slabmax;
+        // overlap distance of every realization of the group for every tile of the chunk
+        GatherLaunch G;
+        G.grid = sim; G.grid_dims = padD; G.grid_stride = padvol; G.ntmpl = Rg;
+        G.rpad = ngrp == 1 ? rpad : Rg;
+        G.ntask = m; G.tasks = d_gt + grp * nsteps + k0;
+        RET_IF(iq_launch_gather(ctx, G));
+        if (chunk_tc[c]) {
+          for (int64_t l = tcbeg[c * ngrp + grp]; l < tcbeg[c * ngrp + grp + 1]; ++l) {
+            const TcRun& u = tcruns[l];
+            RET_IF(tc_launch(u.cfgset, u.st, ctx->d_ti, ctx->d_ti2ii, d_sim, padD, d_tccols + u.col0,
+                             u.N, ctx->ti_stats, sim_stats, u.flops, (char*)d_tcb + grp * tcb_bytes));
+          }
+        } else {  // one group
+          CorrLaunch C;
+          C.img = ctx->d_ti; C.img_dims = ctx->ti; C.out_dims = distD; C.tile = tileD;
+          C.rpad = rpad; C.ntmpl = R; C.out_stride = P; C.disabled = d_dis;
+          C.ntask = m; C.tasks = d_ct + k0; C.flops = cflops[c];
+          RET_IF(iq_launch_corr(ctx, C));
+        }
+        // pick
+        PickLaunch L;
+        L.P = P; L.npat = npat; L.tol = p->tol; L.seed = p->seed; L.real0 = r0; L.nreal = Rg;
+        L.ntask = m; L.tasks = d_pt + grp * nsteps + k0; L.naux_max = nsoft + chard[c];
+        L.dbsize_norm = dbn; L.dbsize_zero = dbz; L.nseq_norm = nsn; L.nseq_zero = nsz;
+        for (int q = 0; q < IQ_MAX_SEQ; ++q) { L.seq_norm[q] = q < nsn ? seqn[q] : 0; L.seq_zero[q] = q < nsz ? seqz[q] : 0; }
+        const size_t po = grp_pick(grp);
+        L.cand = d_cand + po; L.k0 = d_k0 + po; L.v0 = d_v0 + po; L.k1 = d_k1 + po; L.v1 = d_v1 + po;
+        L.w = d_w + po; L.prod = d_prod + po;
+        L.rind = rind; L.ncand = d_ncand + grp_rind(grp); L.status = ctx->d_status;
+        L.stats = ctx->prof ? ctx->d_stats : nullptr;
+        RET_IF(iq_launch_pick(ctx, L));
+        // boundary cuts
+        if (cslab[c] > 0) {
+          CutLaunch K;
+          K.nreal = Rg; K.ntask = m; K.nslab_max = cslab[c]; K.tasks = d_st + k0;
+          K.sim = sim; K.sim_dims = padD; K.sim_rstride = padvol;
+          K.ti = ctx->d_ti; K.ti_dims = ctx->ti; K.dist_dims = distD; K.rind = rind;
+          K.out = cutbuf; K.slabmax = slabmax;
+          K.scratch = d_cutscr ? (char*)d_cutscr + grp_rind(grp) * 6 * cutscr_per : nullptr;
+          K.scratch_per_cta = cutscr_per;
+          K.status = ctx->d_status;
+          K.stats = ctx->prof ? ctx->d_stats : nullptr;
+          K.gr_period = ctx->cut_gr_period;
+          K.threads = ctx->cut_threads;
+          RET_IF(iq_launch_cut(ctx, K));
+        }
+        // paste
+        PasteLaunch Pl;
+        Pl.nreal = Rg; Pl.ntask = m; Pl.tasks = d_st + k0;
+        Pl.sim = sim; Pl.sim_dims = padD; Pl.sim_rstride = padvol;
+        Pl.cut = d_cut ? d_cut + (size_t)r0 * padvol : nullptr;
+        Pl.tile = tileD; Pl.ti = ctx->d_ti; Pl.ti_dims = ctx->ti; Pl.dist_dims = distD;
+        Pl.rind = rind; Pl.cutbuf = cutbuf; Pl.slabmax = slabmax;
+        RET_IF(iq_launch_paste(ctx, Pl));
+      }
   }
 
   // ---- voxel reuse, hard overwrite, crop (src/iqsim.jl:287-307) ----

@@ -186,6 +186,11 @@ int64_t iq_ctx_launches(iq_ctx* ctx);
  *                         (tcgen05) with FP16 halves after a power-of-two scaling when every
  *                         nonzero magnitude lies within 2^17 of the largest, else TF32 halves;
  *                         1 tensor cores with TF32 halves; 0 the SIMT FP32 kernel
+ *   "sim.streams"         1 (default) or 2: with 2, the tensor-core engine and nreal >= 2,
+ *                         iq_simulate runs two groups of realizations on two streams so that
+ *                         one group's pick and cut overlap the other's correlation (each
+ *                         correlation launch then holds half the columns, which costs more
+ *                         than the overlap gains at 16 realizations)
  * Returns IQ_ERR_ARG for an unknown name or an out-of-range value.
  */
 int iq_set_option(iq_ctx* ctx, const char* name, int64_t value);

@@ -170,3 +170,52 @@ def test_iqsim_fp16_tf32_identical_integer_ti(iq, ctx, ctx_tf32, path):
 def test_engine_option_validation(iq, ctx):
     with pytest.raises(Exception):
         ctx.set_option("corr.engine", 3)
+
+
+@pytest.fixture(scope="module")
+def ctx_2streams(iq):
+    c = iq.Context(0)
+    c.set_option("sim.streams", 2)
+    yield c
+    c.close()
+
+
+@pytest.mark.parametrize("path,nreal", [("raster", 3), ("random", 2), ("dilation", 5)])
+def test_iqsim_one_and_two_streams_identical(iq, ctx, ctx_2streams, path, nreal):
+    # two realization groups on two streams (uneven when nreal is odd) against one stream,
+    # with hard and soft data; integer data make every distance exact, so realizations,
+    # cuts and voxel reuse must be identical, and equal the oracle's
+    rng = np.random.default_rng(38)
+    ti = rng.integers(0, 4, (30, 26, 12)).astype(np.float32)
+    simsize = (38, 34, 12)
+    hard = {(int(rng.integers(0, 38)), int(rng.integers(0, 34)), int(rng.integers(0, 12))):
+            float(rng.integers(0, 4)) for _ in range(12)}
+    aux = rng.integers(0, 5, simsize).astype(np.float32)
+    auxti = rng.integers(0, 5, ti.shape).astype(np.float32)
+    kw = dict(overlap=(0.25, 0.25, 0.3), path=path, nreal=nreal, rng=5, hard=hard,
+              soft=[(aux, auxti)], debug=True)
+    a = iq.iqsim(ti, (9, 8, 5), simsize, ctx=ctx, **kw)
+    b = iq.iqsim(ti, (9, 8, 5), simsize, ctx=ctx_2streams, **kw)
+    for x, y in zip(a, b):
+        assert np.array_equal(np.asarray(x, float), np.asarray(y, float), equal_nan=True)
+    r = O.iqsim(ti, (9, 8, 5), simsize, overlap=(0.25, 0.25, 0.3), path=path, nreal=nreal,
+                seed=5, hard=hard, soft=[(aux, auxti)])
+    for x, y in zip(a[0] if isinstance(a, tuple) else a, r):
+        assert np.array_equal(np.asarray(x, float), np.asarray(y, float), equal_nan=True)
+
+
+def test_streams_option_validation(iq, ctx):
+    for bad in (0, 3):
+        with pytest.raises(Exception):
+            ctx.set_option("sim.streams", bad)
+
+
+@pytest.mark.parametrize("nreal", [1, 4])
+def test_iqsim_single_tile(iq, ctx, nreal):
+    # one tile: no overlap anywhere, so the tensor-core launches have columns but no stages
+    rng = np.random.default_rng(39)
+    ti = rng.integers(0, 3, (20, 18, 9)).astype(np.float32)
+    a = iq.iqsim(ti, (8, 7, 4), (8, 7, 4), overlap=(0.25, 0.25, 0.25), nreal=nreal, rng=3, ctx=ctx)
+    r = O.iqsim(ti, (8, 7, 4), (8, 7, 4), overlap=(0.25, 0.25, 0.25), nreal=nreal, seed=3)
+    for x, y in zip(a, r):
+        assert np.array_equal(np.asarray(x, float), np.asarray(y, float))
