@@ -103,7 +103,7 @@ __device__ __forceinline__ bool cas_height(int* p, int expect, int val) {
 }
 
 template <typename HT>
-__device__ int global_relabel(const Graph& g, HT* hc, HT* fa, HT* fb, int* cnt) {
+__device__ __forceinline__ int global_relabel(const Graph& g, HT* hc, HT* fa, HT* fb, int* cnt) {
   if (threadIdx.x == 0) { cnt[0] = 0; cnt[1] = 0; }
   __syncthreads();
   const int dsink = 2 * g.d + 1;  // direction towards the sink slice
@@ -149,8 +149,11 @@ __device__ int global_relabel(const Graph& g, HT* hc, HT* fa, HT* fb, int* cnt) 
   return level;
 }
 
-template <typename HT>
-__global__ void __launch_bounds__(CUT_MAX_THREADS) cut_kernel(const CutArgs a) {
+// GS: the slab lives in global scratch (too large for shared memory). The shared-memory form
+// derives every array from the shared window itself, so its loads, stores and atomics are
+// shared-memory instructions rather than generic ones.
+template <typename HT, bool GS>
+__global__ void __launch_bounds__(CUT_MAX_THREADS, 1) cut_kernel(const CutArgs a) {
   extern __shared__ __align__(16) char smem[];
   const int s_id = blockIdx.x;
   const int y = blockIdx.y;
@@ -171,9 +174,8 @@ __global__ void __launch_bounds__(CUT_MAX_THREADS) cut_kernel(const CutArgs a) {
   g.NH = g.n / g.L * (g.L > 2 ? g.L - 2 : 0) + 2;
   const int n = g.n;
 
-  char* base = a.scratch ? a.scratch + (int64_t)(blockIdx.y * gridDim.x + blockIdx.x) *
-                                           a.scratch_per_cta
-                         : smem;
+  char* base = smem;
+  if constexpr (GS) base = a.scratch + (int64_t)(blockIdx.y * gridDim.x + blockIdx.x) * a.scratch_per_cta;
   long long* dp = reinterpret_cast<long long*>(base);
   g.R = dp;
   g.ex = dp + 6 * n;
@@ -459,7 +461,7 @@ int iq_launch_cut(iq_ctx* ctx, const CutLaunch& L) {
   const int64_t nmax = L.slabmax;
   const size_t need = iq_cut_scratch_bytes(nmax);
   const bool narrow = nmax <= CUT_SHORT_MAX;
-  auto kern = narrow ? cut_kernel<short> : cut_kernel<int>;
+  auto kern = narrow ? cut_kernel<short, false> : cut_kernel<int, false>;
   int smem_limit = 0;
   {
     // dynamic shared memory may use the opt-in maximum minus the kernel's static part
@@ -482,6 +484,7 @@ int iq_launch_cut(iq_ctx* ctx, const CutLaunch& L) {
                           (long long)nmax);
     a.scratch = (char*)L.scratch;
     a.scratch_per_cta = L.scratch_per_cta;
+    kern = narrow ? cut_kernel<short, true> : cut_kernel<int, true>;
   }
   const int threads = (L.threads == 256 || L.threads == 1024) ? L.threads : 512;
   dim3 grid((unsigned)nslab_max, (unsigned)(L.ntask * L.nreal));
