@@ -62,6 +62,16 @@ def workload(name):
                     soft=[(aux, auxti)], path="raster",
                     desc="3-D continuous: TI 100x100x50 f32 lognormal, tile 24x24x12, "
                          "overlap 1/4, tol 0.1, out 200x200x100, nreal 16, 500 hard, 1 soft")
+    if name in ("cfg3", "cfg4"):
+        # four facies: argmax over four independent fields, codes 0..3
+        f = np.stack([gaussian_field((256, 256, 128), (10, 10, 3), 10 + i) for i in range(4)])
+        ti = np.argmax(f, axis=0).astype(np.float32)
+        nreal = 32 if name == "cfg3" else 64
+        return dict(name=name, ti=ti, tilesize=(32, 32, 16), simsize=(512, 512, 128),
+                    overlap=(0.25, 0.25, 0.25), tol=0.05, nreal=nreal, hard={}, soft=[],
+                    path="raster",
+                    desc="3-D categorical: TI 256x256x128 (4 facies, codes 0..3), tile 32x32x16, "
+                         "overlap 1/4, tol 0.05, out 512x512x128, nreal %d" % nreal)
     if name == "cfg1":
         f = gaussian_field((128, 128), 8, 1)
         ti = (f > np.quantile(f, 0.6)).astype(np.float64)
@@ -445,6 +455,12 @@ def run_ours(args, W, dist, rank, world):
         cpu = {"value": vps, "unit": "voxels/s", "cores": cores, "kind": "port",
                "sample": "realization 0, first %d of %d tiles (%.1f s), scaled by the tile "
                          "fraction" % (steps, ntiles, dt)}
+    # working set: simulation grids (padded) and the soft maps (one per tile and variable)
+    ovl = [math.ceil(o * t) for o, t in zip(W["overlap"], W["tilesize"])]
+    ntl = [math.ceil(s / (t - o)) for s, t, o in zip(W["simsize"], W["tilesize"], ovl)]
+    padvol = int(np.prod([n * (t - o) + o for n, t, o in zip(ntl, W["tilesize"], ovl)]))
+    npos = int(np.prod([a - t + 1 for a, t in zip(W["ti"].shape, W["tilesize"])]))
+    soft_bytes = len(W["soft"]) * int(np.prod(ntl)) * npos * 4
     line = {"metric": METRIC, "value": value, "unit": "voxels/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_max / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
@@ -452,7 +468,9 @@ def run_ours(args, W, dist, rank, world):
             "config": {"workload": W["desc"], "global_batch": nreal * world,
                        "options": args.option,
                        "voxels_per_step": voxels * world, "parallelism": "replicas x%d" % world,
-                       "l2": "working set > L2 (simulation grids 350 MB, soft maps 1.6 GB)",
+                       "l2": "working set > L2 (simulation grids %.0f MB%s)" % (
+                           padvol * nreal * 4 / 1e6,
+                           ", soft maps %.1f GB" % (soft_bytes / 1e9) if soft_bytes else ""),
                        "form": "plain (FP32-accurate correlation as split FP16/TF32 MMAs on the tensor cores)"},
             "roofline": roof, "dominant_kernel": dom, "kernels": kernel_share,
             "counters": counters,
@@ -471,7 +489,7 @@ def main():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="cfg2", choices=["cfg2", "cfg1"])
+    ap.add_argument("--workload", default="cfg2", choices=["cfg2", "cfg1", "cfg3", "cfg4"])
     ap.add_argument("--cpu-budget", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer arm")

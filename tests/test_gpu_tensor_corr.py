@@ -219,3 +219,30 @@ def test_iqsim_single_tile(iq, ctx, nreal):
     r = O.iqsim(ti, (8, 7, 4), (8, 7, 4), overlap=(0.25, 0.25, 0.25), nreal=nreal, seed=3)
     for x, y in zip(a, r):
         assert np.array_equal(np.asarray(x, float), np.asarray(y, float))
+
+
+def test_iqsim_slabs_in_global_scratch(iq, ctx):
+    # tile 32x32x16 with overlap 1/4: cut slabs of 8x32x16 = 4096 nodes need more than the
+    # shared memory of a CTA, so the cut works on global scratch (the large-tile workload's case)
+    rng = np.random.default_rng(40)
+    ti = rng.integers(0, 4, (40, 40, 20)).astype(np.float32)
+    kw = dict(overlap=(0.25, 0.25, 0.25), nreal=2)
+    a = iq.iqsim(ti, (32, 32, 16), (56, 56, 16), rng=11, ctx=ctx, **kw)
+    r = O.iqsim(ti, (32, 32, 16), (56, 56, 16), seed=11, **kw)
+    for x, y in zip(a, r):
+        assert np.array_equal(np.asarray(x, float), np.asarray(y, float))
+
+
+def test_tensor_large_ti_streaming_stores(iq, ctx, ctx_simt):
+    # a TI of 9 MB (4.1 M voxels, 1.9 M positions): many CTAs per z-plane and maps far larger
+    # than the small cases
+    rng = np.random.default_rng(41)
+    ti = rng.integers(0, 5, (160, 160, 90)).astype(np.float32)
+    assert ti.nbytes > 8 << 20
+    tm = rng.integers(0, 5, (3, 8, 8, 4)).astype(np.float32)
+    w = _mask((8, 8, 4), "prev")
+    got = iq.fastdistance(ti, tm, w, ctx=ctx)
+    simt = iq.fastdistance(ti, tm, w, ctx=ctx_simt)
+    assert np.array_equal(got, simt)
+    ref = O.fastdistance(ti, tm[1], w, "direct")
+    assert np.array_equal(got[1], ref.astype(np.float32))
