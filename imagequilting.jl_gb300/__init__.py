@@ -10,7 +10,8 @@ this package is the Python host side. Load it under any module name, e.g.
 from ._lib import IQError, load  # noqa: F401
 from .api import (Context, default_context, fastdistance, finddisabled, genpath,  # noqa: F401
                   graphcut, iqsim, pick, voxelreuse)
+from .autotune import autotune  # noqa: F401
 from .build import build  # noqa: F401
 
 __all__ = ["iqsim", "voxelreuse", "Context", "fastdistance", "pick", "graphcut",
-           "finddisabled", "genpath", "build", "load", "IQError"]
+           "finddisabled", "genpath", "autotune", "build", "load", "IQError"]
