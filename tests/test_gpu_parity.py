@@ -8,6 +8,8 @@ Tolerances (stated by the specification of this path):
   * whole realizations: bit-exact on integer-valued training images, where every distance
     is an exact integer in FP32 and FP64.
 """
+import os
+
 import numpy as np
 import pytest
 
@@ -313,3 +315,24 @@ def test_errors_are_reported(iq, ctx):
         iq.iqsim(TI, (10, 10), tol=0, ctx=ctx)
     with pytest.raises(iq.IQError):
         iq.graphcut(np.ones((4, 4)), np.ones((4, 4)), 5, ctx=ctx)
+
+
+# ---- the committed golden fixtures (tests/golden/make_golden.py) ------------------------
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def test_golden_fixtures(iq, ctx):
+    f = np.load(os.path.join(GOLDEN, "iqsim_int3d.npz"))
+    hard = {tuple(int(v) for v in c): float(x) for c, x in zip(f["hard_coords"], f["hard_values"])}
+    reals = iq.iqsim(f["ti"], tuple(int(t) for t in f["tilesize"]),
+                     tuple(int(t) for t in f["simsize"]), overlap=tuple(float(o) for o in f["overlap"]),
+                     path="raster", nreal=int(f["nreal"]), rng=int(f["seed"]), hard=hard,
+                     soft=[(f["aux"], f["auxti"])], ctx=ctx)
+    assert len(reals) == len(f["reals"])
+    for x, y in zip(reals, f["reals"]):
+        assert np.array_equal(np.asarray(x, np.float32), y)
+    g = np.load(os.path.join(GOLDEN, "graphcut_cont3d.npz"))
+    assert np.array_equal(iq.graphcut(g["A"], g["B"], int(g["dim"]), ctx=ctx), g["mask"])
+    d = np.load(os.path.join(GOLDEN, "fastdistance_int3d.npz"))
+    got = iq.fastdistance(d["ti"], d["tmpl"], d["weights"], ctx=ctx)
+    assert np.array_equal(got, d["maps"])

@@ -3,7 +3,9 @@
 These run without a GPU. They pin the oracle before it is trusted as the checker of the CUDA
 path: every invariant and known answer of test/runtests.jl:9-162 is restated here.
 """
+import json
 import math
+import os
 
 import numpy as np
 import pytest
@@ -320,3 +322,36 @@ def test_capacities_are_quantized():
     q = 2.0 ** (math.frexp(c.max())[1] - 1 - 47)
     assert c.max() > 2.0 ** 50  # some eps-denominator edges
     assert np.all(np.mod(c, q) == 0)
+
+
+# ---- golden fixtures (tests/golden/make_golden.py) -------------------------------------
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def test_golden_philox_vectors():
+    for e in json.load(open(os.path.join(GOLDEN, "philox_kat.json"))):
+        ctr = tuple(int(x, 16) for x in e["counter"])
+        key = tuple(int(x, 16) for x in e["key"])
+        assert philox.philox4x32_10(ctr, key) == tuple(int(x, 16) for x in e["output"])
+
+
+def test_golden_oracle_reproduces_iqsim():
+    f = np.load(os.path.join(GOLDEN, "iqsim_int3d.npz"))
+    hard = {tuple(int(v) for v in c): float(x) for c, x in zip(f["hard_coords"], f["hard_values"])}
+    reals = O.iqsim(f["ti"], tuple(int(t) for t in f["tilesize"]),
+                    tuple(int(t) for t in f["simsize"]), overlap=tuple(f["overlap"]),
+                    path="raster", nreal=int(f["nreal"]), seed=int(f["seed"]), hard=hard,
+                    soft=[(f["aux"], f["auxti"])])
+    for x, y in zip(reals, f["reals"]):
+        assert np.array_equal(np.asarray(x, np.float32), y)
+
+
+def test_golden_oracle_reproduces_cut_and_distances():
+    g = np.load(os.path.join(GOLDEN, "graphcut_cont3d.npz"))
+    assert np.array_equal(O.graphcut(g["A"], g["B"], int(g["dim"])), g["mask"])
+    d = np.load(os.path.join(GOLDEN, "fastdistance_int3d.npz"))
+    dis = O.finddisabled(d["ti"], d["tmpl"].shape[1:])
+    for t, m in zip(d["tmpl"], d["maps"]):
+        ref = O.fastdistance(np.nan_to_num(d["ti"]), t, d["weights"], "direct")
+        ref[dis] = np.inf
+        assert np.array_equal(ref.astype(np.float32), m)
