@@ -53,6 +53,10 @@ mutable struct Context
   end
 end
 
+# Tuning knob of a context (iq_set_option; include/iqgpu.h lists the names and ranges)
+setoption!(c::Context, name::AbstractString, value::Integer) =
+  check(ccall((:iq_set_option, LIB[]), Cint, (Ptr{Cvoid}, Cstring, Int64), c.h, name, value))
+
 const DEFAULT = Ref{Union{Nothing,Context}}(nothing)
 context() = (DEFAULT[] === nothing && (DEFAULT[] = Context(0)); DEFAULT[])
 
