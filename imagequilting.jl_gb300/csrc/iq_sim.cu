@@ -467,8 +467,15 @@ extern "C" int iq_simulate(iq_ctx* ctx, const iq_sim_params* p, const iq_hard_da
                            (int64_t)R * 6 * (slabmax + cutscr_per) + 4096;
   size_t freeb = 0, totalb = 0;
   cudaMemGetInfo(&freeb, &totalb);
-  int64_t chunk_max = std::max<int64_t>(1, std::min<int64_t>(ctx->level_chunk,
-                                                              (int64_t)(freeb / 2) / per_step));
+  // hard-data distance maps depend on the data only: one map per data tile, all held at once
+  int64_t nhs = 0;
+  for (const Step& s : steps) nhs += s.hardtile ? 1 : 0;
+  const int64_t hard_bytes = nhs * (P + T) * 4;
+  if ((size_t)hard_bytes > freeb / 2)
+    return iq_set_error(IQ_ERR_LIMIT, "hard-data maps of %lld data tiles need %lld bytes",
+                        (long long)nhs, (long long)hard_bytes);
+  int64_t chunk_max = std::max<int64_t>(
+      1, std::min<int64_t>(ctx->level_chunk, (int64_t)(freeb / 2 - hard_bytes) / per_step));
   std::vector<int64_t> cbeg;  // chunk boundaries into `steps`
   for (size_t i = 0; i < steps.size();) {
     size_t j = i + 1;
@@ -481,15 +488,13 @@ extern "C" int iq_simulate(iq_ctx* ctx, const iq_sim_params* p, const iq_hard_da
   int64_t cmax = 1;
   for (int64_t c = 0; c < nchunk; ++c) cmax = std::max(cmax, cbeg[c + 1] - cbeg[c]);
 
-  // Realization groups: realizations never read one another, so with the tensor-core path two
-  // groups run on two streams, interleaved chunk by chunk. One group's pick and cut then share
-  // the GPU with the other group's correlation, and the tail of each launch is filled by the
-  // other stream's work. Group g holds realizations [gb[g], gb[g+1]).
+  // Realization groups: realizations never read one another, so with `sim.streams` = 2 and
+  // the tensor-core path two groups run on two streams, interleaved chunk by chunk. One
+  // group's pick and cut then share the GPU with the other group's correlation, and the tail
+  // of each launch is filled by the other stream's work. Group g holds realizations
+  // [gb[g], gb[g+1]).
   const int ngrp = (tc && T > 0 && R >= 2 && ctx->sim_streams >= 2) ? 2 : 1;
   const int gb[3] = {0, ngrp == 2 ? (R + 1) / 2 : R, R};
-  // hard-data distance maps depend on the data only: one map per data tile, made up front
-  int64_t nhs = 0;
-  for (const Step& s : steps) nhs += s.hardtile ? 1 : 0;
 
   // ---- device buffers ----
   const bool debug = p->debug != 0 && (cuts || voxs);
