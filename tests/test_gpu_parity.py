@@ -336,3 +336,18 @@ def test_golden_fixtures(iq, ctx):
     d = np.load(os.path.join(GOLDEN, "fastdistance_int3d.npz"))
     got = iq.fastdistance(d["ti"], d["tmpl"], d["weights"], ctx=ctx)
     assert np.array_equal(got, d["maps"])
+
+
+# ---- the benchmark workload at full size: size-independent properties (tests/props.py) ---
+def test_full_size_properties(iq, ctx):
+    import bench
+    from props import check_realizations
+    W = bench.workload("cfg2")  # 16 realizations of 200x200x100, 500 hard data, 1 soft pair
+    kw = dict(overlap=W["overlap"], soft=W["soft"], hard=W["hard"], tol=W["tol"],
+              path=W["path"], nreal=W["nreal"], rng=7, ctx=ctx)
+    a = iq.iqsim(W["ti"], W["tilesize"], W["simsize"], **kw)
+    assert len(a) == W["nreal"] and a[0].shape == W["simsize"]
+    check_realizations(a, W["ti"], W["hard"])
+    b = iq.iqsim(W["ti"], W["tilesize"], W["simsize"], **kw)
+    for x, y in zip(a, b):
+        assert np.array_equal(x, y)

@@ -355,3 +355,18 @@ def test_golden_oracle_reproduces_cut_and_distances():
         ref = O.fastdistance(np.nan_to_num(d["ti"]), t, d["weights"], "direct")
         ref[dis] = np.inf
         assert np.array_equal(ref.astype(np.float32), m)
+
+
+# ---- the full-size property checks (tests/props.py) hold on the oracle's output ---------------
+def test_properties_hold_on_oracle_output():
+    from props import check_realizations
+    rng = np.random.default_rng(60)
+    ti = np.exp(rng.normal(size=(20, 18, 8))).astype(np.float32)
+    hard = {(2, 3, 1): 0.5, (17, 20, 5): 7.25}
+    reals = O.iqsim(ti, (8, 8, 4), (24, 26, 8), overlap=(0.25,) * 3, hard=hard, nreal=2, seed=5)
+    check_realizations(reals, ti, hard)
+    # a planted mistake is caught: a value that is neither a TI value nor a hard datum
+    bad = [r.copy() for r in reals]
+    bad[1][5, 5, 5] = -1.0
+    with pytest.raises(AssertionError):
+        check_realizations(bad, ti, hard)
