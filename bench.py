@@ -14,7 +14,10 @@ complete iqsim call (16 realizations, 64M voxels).
   cpu_baseline / --impl reference : the CPU oracle (Float64, FFT correlation with scipy.fft
           on all host cores, C Boykov-Kolmogorov cut) on a bounded sample of the same
           workload: realization 0, the first tiles of the path, scaled to voxels/s
-N>1 (torchrun): every rank runs its own replica (weak scaling, no data-path collective).
+N>1 (torchrun): the ranks are shards of one call (weak scaling, no data-path collective):
+every rank runs nreal realizations with the same seed and real0 = rank * nreal, so N ranks
+together produce realizations [0, N * nreal) of one call, each drawing the Philox streams of
+its global realization index.
 """
 import argparse
 import json
@@ -200,10 +203,15 @@ def barrier(dist):
         dist.barrier()
 
 
-def step_seed(step, rank):
-    """Seed of one simulation call: ranks shard the realizations (each rank's calls draw their
-    own Philox streams), so no data moves between ranks."""
-    return 1000 + 7919 * step + 104729 * rank
+def step_seed(step):
+    """Seed of one simulation call, the same on every rank."""
+    return 1000 + 7919 * step
+
+
+def step_real0(rank, nreal):
+    """First global realization of `rank`'s shard: the ranks' blocks of nreal realizations
+    are consecutive, so together they are the realizations of one call (no data moves)."""
+    return rank * nreal
 
 
 def aggregate_rate(units_per_rank_step, steps, world, ms_max):
@@ -338,13 +346,15 @@ def run_ours(args, W, dist, rank, world):
     hd_host, sd_host = make_io(False)
     size = _lib.i64arr(ti_h.shape)
 
+    p.real0 = step_real0(rank, nreal)
+
     def step_resident(i):
-        p.seed = step_seed(i, rank)
+        p.seed = step_seed(i)
         _lib.check(lib.iq_simulate(ctx.h, ctypes.byref(p), ctypes.byref(hd_dev), len(soft_d),
                                    sd_dev if soft_d else None, out_d.data_ptr(), None, None))
 
     def step_e2e(i):
-        p.seed = step_seed(i, rank)
+        p.seed = step_seed(i)
         _lib.check(lib.iq_set_ti(ctx.h, ti_h.ctypes.data, ti_dt, N, size))
         _lib.check(lib.iq_simulate(ctx.h, ctypes.byref(p), ctypes.byref(hd_host), len(soft_h),
                                    sd_host if soft_h else None, out_h.ctypes.data, None, None))
@@ -467,7 +477,8 @@ def run_ours(args, W, dist, rank, world):
             "data": "synthetic (seeded Gaussian fields)",
             "config": {"workload": W["desc"], "global_batch": nreal * world,
                        "options": args.option,
-                       "voxels_per_step": voxels * world, "parallelism": "replicas x%d" % world,
+                       "voxels_per_step": voxels * world,
+                       "parallelism": "realization shards x%d" % world,
                        "l2": "working set > L2 (simulation grids %.0f MB%s)" % (
                            padvol * nreal * 4 / 1e6,
                            ", soft maps %.1f GB" % (soft_bytes / 1e9) if soft_bytes else ""),

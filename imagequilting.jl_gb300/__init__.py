@@ -12,6 +12,8 @@ from .api import (Context, default_context, fastdistance, finddisabled, genpath,
                   graphcut, iqsim, pick, voxelreuse)
 from .autotune import autotune  # noqa: F401
 from .build import build  # noqa: F401
+from .shard import gather_realizations, iqsim_shard, shard_range  # noqa: F401
 
 __all__ = ["iqsim", "voxelreuse", "Context", "fastdistance", "pick", "graphcut",
-           "finddisabled", "genpath", "autotune", "build", "load", "IQError"]
+           "finddisabled", "genpath", "autotune", "build", "load", "IQError", "shard_range",
+           "iqsim_shard", "gather_realizations"]

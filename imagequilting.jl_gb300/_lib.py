@@ -34,7 +34,8 @@ class SimParams(ctypes.Structure):
     _fields_ = [("ndim", ctypes.c_int32), ("tilesize", ctypes.c_int64 * 3),
                 ("simsize", ctypes.c_int64 * 3), ("overlap", ctypes.c_double * 3),
                 ("tol", ctypes.c_double), ("path", ctypes.c_int32), ("nreal", ctypes.c_int32),
-                ("debug", ctypes.c_int32), ("seed", ctypes.c_uint64)]
+                ("debug", ctypes.c_int32), ("seed", ctypes.c_uint64),
+                ("real0", ctypes.c_int64)]
 
 
 class HardData(ctypes.Structure):

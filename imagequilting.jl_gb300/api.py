@@ -118,8 +118,13 @@ def default_context():
 
 
 def iqsim(trainimg, tilesize, simsize=None, *, overlap=None, soft=(), hard=None, tol=0.1,
-          path="raster", nreal=1, debug=False, showprogress=False, rng=None, ctx=None):
+          path="raster", nreal=1, debug=False, showprogress=False, rng=None, ctx=None,
+          real0=0):
     """Image quilting simulation (src/iqsim.jl:5-49 documents the arguments).
+
+    `real0` (not in the reference) is the global index of the first realization: calls with
+    the same `rng` seed and disjoint ranges [real0, real0 + nreal) are shards of one call, on
+    one device or several, and their realizations equal those of the whole call.
 
     Returns a list of `nreal` arrays of shape `simsize` ("reals"), or (reals, cuts, voxs)
     with debug=True. Float training images give arrays of their float type; other types give
@@ -168,6 +173,7 @@ def iqsim(trainimg, tilesize, simsize=None, *, overlap=None, soft=(), hard=None,
     p.nreal = int(nreal)
     p.debug = 1 if debug else 0
     p.seed = _seed(rng)
+    p.real0 = int(real0)
     coords = np.ascontiguousarray(coords)
     hd = _lib.HardData(len(values), coords.ctypes.data if len(values) else None,
                        values.ctypes.data if len(values) else None)

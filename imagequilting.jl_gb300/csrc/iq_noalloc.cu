@@ -168,17 +168,20 @@ extern "C" int iq_pick_noalloc(const float* D, int64_t P, int32_t naux, const fl
   const int64_t n = hr[1];
   if (out_ncand) *out_ncand = n;
   const int64_t m = std::min(n, cap);
-  if (out_cands && m > 0) {
-    // widen the int32 candidate list in place of nothing: copy in chunks through the stack
-    const int32_t* dc = L.cand;
-    int32_t buf[1024];
-    for (int64_t i = 0; i < m; i += 1024) {
-      const int64_t c = std::min<int64_t>(1024, m - i);
-      IQ_CUDA_OK(cudaMemcpy(buf, dc + i, sizeof(int32_t) * c, cudaMemcpyDeviceToHost));
-      for (int64_t j = 0; j < c; ++j) out_cands[i + j] = buf[j];
+  if (m > 0 && (out_cands || out_weights)) {
+    // Both read-backs run on the caller's stream, followed by one synchronization. The int32
+    // candidate list lands in the front half of out_cands and is widened in place from the
+    // last entry down: int32 entry i lies below int64 entry i, so every entry is read before
+    // a wider write reaches it.
+    if (out_cands)
+      IQ_CUDA_OK(cudaMemcpyAsync(out_cands, L.cand, sizeof(int32_t) * m, cudaMemcpyDefault, st));
+    if (out_weights)
+      IQ_CUDA_OK(cudaMemcpyAsync(out_weights, L.w, sizeof(double) * m, cudaMemcpyDefault, st));
+    IQ_CUDA_OK(cudaStreamSynchronize(st));
+    if (out_cands) {
+      const int32_t* narrow = reinterpret_cast<const int32_t*>(out_cands);
+      for (int64_t i = m - 1; i >= 0; --i) out_cands[i] = (int64_t)narrow[i];
     }
   }
-  if (out_weights && m > 0)
-    IQ_CUDA_OK(cudaMemcpy(out_weights, L.w, sizeof(double) * m, cudaMemcpyDefault));
   return IQ_OK;
 }

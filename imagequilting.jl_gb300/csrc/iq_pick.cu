@@ -799,16 +799,14 @@ __global__ void __launch_bounds__(PT) select_keys_kernel(const KeyArgs a) {
     a.keys[m * a.nq + q] = ((unsigned long long)key.v << 32) | key.i;
 }
 
+// The shared-memory attribute belongs to the current device, so it is set on every launch
+// (a host call of a few microseconds) rather than once per process.
 template <int NAUX>
 cudaError_t launch_pick_t(const PickArgs& a, int nblocks, cudaStream_t st) {
-  static bool attr = false;
-  if (!attr) {
-    cudaError_t e = cudaFuncSetAttribute(pick_kernel<NAUX>,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)DYN_BYTES);
-    if (e != cudaSuccess) return e;
-    attr = true;
-  }
+  cudaError_t e = cudaFuncSetAttribute(pick_kernel<NAUX>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)DYN_BYTES);
+  if (e != cudaSuccess) return e;
   pick_kernel<NAUX><<<nblocks, PT, DYN_BYTES, st>>>(a);
   return cudaGetLastError();
 }
@@ -857,12 +855,8 @@ int iq_launch_select_keys(iq_ctx* ctx, const float* maps, const unsigned* mm, in
   KeyArgs a;
   a.maps = maps; a.mm = mm; a.P = P; a.nq = nq; a.keys = keys;
   for (int q = 0; q < IQ_PRE_KEYS; ++q) a.seq[q] = q < nq ? seq[q] : 0;
-  static bool attr = false;
-  if (!attr) {
-    IQ_CUDA_OK(cudaFuncSetAttribute(select_keys_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                    (int)DYN_BYTES));
-    attr = true;
-  }
+  IQ_CUDA_OK(cudaFuncSetAttribute(select_keys_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)DYN_BYTES));
   iq_timer_start(ctx, "pick");
   select_keys_kernel<<<(unsigned)(nmaps * nq), PT, DYN_BYTES, ctx->stream>>>(a);
   iq_timer_stop(ctx, "pick", 0);

@@ -196,6 +196,8 @@ extern "C" int iq_simulate(iq_ctx* ctx, const iq_sim_params* p, const iq_hard_da
   if (!(p->tol > 0 && p->tol <= 1)) return iq_set_error(IQ_ERR_ARG, "tolerance must be in range (0,1]");
   if (p->path < 0 || p->path > 2) return iq_set_error(IQ_ERR_ARG, "invalid simulation path");
   if (p->nreal <= 0) return iq_set_error(IQ_ERR_ARG, "invalid number of realizations");
+  if (p->real0 < 0 || p->real0 + p->nreal > ((int64_t)1 << 32))
+    return iq_set_error(IQ_ERR_ARG, "realization range outside [0, 2^32)");
   if (nsoft < 0 || (nsoft > 0 && !soft)) return iq_set_error(IQ_ERR_ARG, "invalid soft data");
   if (nsoft + 1 > IQ_MAX_AUX) return iq_set_error(IQ_ERR_LIMIT, "at most %d soft variables", IQ_MAX_AUX - 1);
   for (int s = 0; s < nsoft; ++s) {
@@ -474,6 +476,18 @@ extern "C" int iq_simulate(iq_ctx* ctx, const iq_sim_params* p, const iq_hard_da
   if ((size_t)hard_bytes > freeb / 2)
     return iq_set_error(IQ_ERR_LIMIT, "hard-data maps of %lld data tiles need %lld bytes",
                         (long long)nhs, (long long)hard_bytes);
+  // soft-data maps: one map of P floats per (non-skipped tile, soft variable), all held for the
+  // whole call (about 122 GB for a 5.7 M-position map over 5,324 tiles)
+  if (nsoft > 0) {
+    int64_t nlive = 0;
+    for (int64_t t = 0; t < g.ntot; ++t) nlive += skipped[t] ? 0 : 1;
+    const double soft_bytes = (double)nlive * nsoft * (double)P * 4.0;
+    if (soft_bytes + (double)hard_bytes > (double)freeb * 0.75)
+      return iq_set_error(IQ_ERR_LIMIT,
+                          "soft-data maps of %lld tiles x %d variables need %.0f bytes, more than "
+                          "three quarters of the %zu free bytes of the device",
+                          (long long)nlive, nsoft, soft_bytes, freeb);
+  }
   int64_t chunk_max = std::max<int64_t>(
       1, std::min<int64_t>(ctx->level_chunk, (int64_t)(freeb / 2 - hard_bytes) / per_step));
   std::vector<int64_t> cbeg;  // chunk boundaries into `steps`
@@ -964,7 +978,7 @@ extern "C" int iq_simulate(iq_ctx* ctx, const iq_sim_params* p, const iq_hard_da
         }
         // pick
         PickLaunch L;
-        L.P = P; L.npat = npat; L.tol = p->tol; L.seed = p->seed; L.real0 = r0; L.nreal = Rg;
+        L.P = P; L.npat = npat; L.tol = p->tol; L.seed = p->seed; L.real0 = p->real0 + r0; L.nreal = Rg;
         L.ntask = m; L.tasks = d_pt + grp * nsteps + k0; L.naux_max = nsoft + chard[c];
         L.dbsize_norm = dbn; L.dbsize_zero = dbz; L.nseq_norm = nsn; L.nseq_zero = nsz;
         for (int q = 0; q < IQ_MAX_SEQ; ++q) { L.seq_norm[q] = q < nsn ? seqn[q] : 0; L.seq_zero[q] = q < nsz ? seqz[q] : 0; }

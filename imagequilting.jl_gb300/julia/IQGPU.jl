@@ -23,6 +23,7 @@ struct SimParams
   nreal::Int32
   debug::Int32
   seed::UInt64
+  real0::Int64
 end
 
 struct HardData
@@ -105,7 +106,7 @@ function iqsim(trainimg::AbstractArray{T,N}, tilesize::Dims{N}, simsize::Dims{N}
 
   seed = rand(rng, UInt64)
   p = Ref(SimParams(N, pad3(tilesize, 1), pad3(simsize, 1), pad3(Float64.(overlap), 0.5),
-                    tol, PATHS[path], nreal, debug, seed))
+                    tol, PATHS[path], nreal, debug, seed, 0))
   nvox = prod(simsize)
   out = Vector{Float32}(undef, nvox * nreal)
   cuts = debug ? Vector{Float32}(undef, nvox * nreal) : Float32[]

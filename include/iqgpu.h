@@ -54,6 +54,10 @@ typedef struct iq_sim_params {
   int32_t nreal;       /* number of realizations */
   int32_t debug;       /* nonzero: also write boundary cuts and voxel reuse */
   uint64_t seed;       /* key of the Philox4x32-10 streams (path and draws) */
+  int64_t real0;       /* global index of the first realization: realization r of this call
+                          draws with counter (tile, real0 + r), so calls on several devices
+                          with the same seed and disjoint [real0, real0 + nreal) ranges are
+                          shards of one call (0 for a whole call) */
 } iq_sim_params;
 
 /* Hard data: the reference's Dict{CartesianIndex,Real} as a list of unique coordinates. */

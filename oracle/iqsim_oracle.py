@@ -574,13 +574,14 @@ def cut_cost(A, B, mask):
 # --------------------------------------------------------------------------------------
 def iqsim(trainimg, tilesize, simsize=None, overlap=None, soft=(), hard=None, tol=0.1,
           path="raster", nreal=1, debug=False, seed=0, method="direct", workers=None,
-          trace=None, max_steps=None):
+          trace=None, max_steps=None, real0=0):
     """Image quilting simulation, the reference's loop in Float64.
 
     `seed` keys the Philox streams (path and draws). `method` picks the distance form
     ("direct" exact SSD or "fft" as the reference). `trace`, when a list, receives one tuple
     (real, tile, rind, ncand) per simulated tile. `max_steps` stops each realization after
-    that many tiles (used to time a bounded sample)."""
+    that many tiles (used to time a bounded sample). `real0` is the global index of the first
+    realization (its Philox draws use counter (tile, real0 + r))."""
     tisize = tuple(np.shape(trainimg))
     N = len(tisize)
     tilesize = tuple(int(t) for t in tilesize)
@@ -652,7 +653,7 @@ def iqsim(trainimg, tilesize, simsize=None, overlap=None, soft=(), hard=None, to
             else:
                 D, Ds = ovldist, softdists
 
-            rind, cands, _ = pick(D, Ds, tol, seed, ind, real)
+            rind, cands, _ = pick(D, Ds, tol, seed, ind, real0 + real)
             if trace is not None:
                 trace.append((real, ind, rind, len(cands)))
             rstart = lin2cart(geo.distsize, rind)

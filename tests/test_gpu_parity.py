@@ -212,6 +212,30 @@ def test_iqsim_bit_exact_integer_ti(iq, ctx, case):
     assert np.allclose(g[2], r[2], rtol=0, atol=0)
 
 
+@pytest.mark.parametrize("data", ["int", "hard_soft"])
+def test_iqsim_shards_equal_whole_call(iq, ctx, data):
+    """Two shards of one call (real0 = 0 and 3), run one after the other on this GPU, equal
+    the whole 5-realization call bit for bit; the oracle agrees with the shards."""
+    rng = np.random.default_rng(24)
+    ti = rng.integers(0, 4, (22, 20, 12)).astype(np.float32)
+    simsize = (26, 24, 12)
+    kw = dict(overlap=(0.25, 0.25, 0.25))
+    if data == "hard_soft":
+        kw["hard"] = {(3, 4, 5): 1.0, (20, 11, 2): 3.0}
+        kw["soft"] = [(rng.integers(0, 5, simsize).astype(np.float32),
+                       rng.integers(0, 5, ti.shape).astype(np.float32))]
+    whole = iq.iqsim(ti, (8, 8, 6), simsize, nreal=5, rng=13, ctx=ctx, **kw)
+    parts = []
+    for rank in range(2):
+        r0, local = iq.iqsim_shard(iq.iqsim, ti, (8, 8, 6), simsize, nreal=5, rank=rank, world=2,
+                                   rng=13, ctx=ctx, **kw)
+        parts.append((r0, local))
+    assert [r0 for r0, _ in parts] == [0, 3]
+    _same_reals(parts[0][1] + parts[1][1], whole)
+    r = O.iqsim(ti, (8, 8, 6), simsize, nreal=2, real0=3, seed=13, **kw)
+    _same_reals(parts[1][1], r)
+
+
 def test_iqsim_bit_exact_hard_and_soft(iq, ctx):
     rng = np.random.default_rng(22)
     ti = rng.integers(0, 4, (22, 20, 12)).astype(np.float32)
@@ -304,6 +328,20 @@ def test_runtests_cut_and_voxelreuse(iq, ctx):
     assert 0 <= voxs[0] <= 1
     mu, _ = iq.voxelreuse(np.random.default_rng(3).random((20, 20, 20)), (10, 10, 10), nreal=1,
                           ctx=ctx)
+    assert 0 <= mu <= 1
+
+
+@pytest.mark.parametrize("shape,tile,overlap", [((30, 28, 14), (8, 8, 6), (0.25, 0.25, 0.34)),
+                                                ((40, 36), (12, 10), None)])
+def test_voxelreuse_vs_oracle(iq, ctx, shape, tile, overlap):
+    """voxelreuse (src/voxelreuse.jl:18-41): a 2-tile grid per dimension, nreal debug runs,
+    mean and standard deviation of the reuse. Integer data, so equal to the oracle's bits."""
+    ti = np.random.default_rng(19).integers(0, 3, shape).astype(np.float32)
+    kw = dict(nreal=5, rng=41) if overlap is None else dict(overlap=overlap, nreal=5, rng=41)
+    mu, sd = iq.voxelreuse(ti, tile, ctx=ctx, **kw)
+    kw_o = {k: v for k, v in kw.items() if k != "rng"}
+    mu_o, sd_o = O.voxelreuse(ti, tile, seed=41, **kw_o)
+    assert mu == mu_o and sd == sd_o
     assert 0 <= mu <= 1
 
 

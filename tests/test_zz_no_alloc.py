@@ -14,7 +14,7 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 
-def _noalloc(lib, D, Ds, tol, seed, tile, real):
+def _noalloc(lib, D, Ds, tol, seed, tile, real, stream=None):
     d = np.ascontiguousarray(D, np.float32)
     aux = [np.ascontiguousarray(x, np.float32) for x in Ds]
     P = d.size
@@ -26,7 +26,7 @@ def _noalloc(lib, D, Ds, tol, seed, tile, real):
     rc = lib.iq_pick_noalloc(d.ctypes.data, P, len(aux), arr if aux else None, tol, seed, tile,
                              real, ctypes.byref(idx), ctypes.byref(nc),
                              cands.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)),
-                             w.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), P, None)
+                             w.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), P, stream)
     return rc, idx.value, cands[:nc.value].copy(), w[:nc.value].copy()
 
 
@@ -48,6 +48,31 @@ def test_noalloc_pick_matches_iq_pick(iq):
             assert i == ref[0]
             assert np.array_equal(c, ref[1])
             assert np.array_equal(w, ref[2])  # bit-exact, like iq_pick against the oracle
+    ctx.close()
+
+
+def test_noalloc_pick_at_its_limits_on_a_caller_stream(iq):
+    """P = 2^18 and three auxiliary maps fill every region of the scratch array; the calls run
+    on the context's (non-default) stream."""
+    lib = iq.load()
+    ctx = iq.Context(0)
+    rng = np.random.default_rng(47)
+    P = 1 << 18
+    D = (rng.random(P) * 25).astype(np.float32)
+    D[rng.random(P) < 0.05] = np.inf
+    Ds = []
+    for scale in (7.0, 3.0, 11.0):
+        S = np.floor(rng.random(P) * scale).astype(np.float32)  # ties inside every aux map
+        S[np.isinf(D)] = np.inf
+        Ds.append(S)
+    ref = iq.pick(D, Ds, 0.1, 9, 40, 3, ctx=ctx)
+    stream = ctx.stream
+    for _ in range(2):
+        rc, i, c, w = _noalloc(lib, D, Ds, 0.1, 9, 40, 3, stream=stream)
+        assert rc == 0, lib.iq_last_error()
+        assert i == ref[0]
+        assert np.array_equal(c, ref[1])
+        assert np.array_equal(w, ref[2])
     ctx.close()
 
 
