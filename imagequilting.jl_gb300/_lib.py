@@ -54,6 +54,7 @@ SIGNATURES = {
     "iq_ctx_create": (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(ctypes.c_void_p)]),
     "iq_ctx_destroy": (ctypes.c_int, [ctypes.c_void_p]),
     "iq_ctx_stream": (ctypes.c_void_p, [ctypes.c_void_p]),
+    "iq_ties": (ctypes.c_int, [ctypes.c_void_p, c_i64p]),
     "iq_set_ti": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32,
                                  c_i64p]),
     "iq_simulate": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(SimParams),

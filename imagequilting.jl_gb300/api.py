@@ -98,6 +98,13 @@ class Context:
         return ms.value, n.value, w.value
 
     @property
+    def ties(self):
+        """Near-ties (|D - t| <= 1e-6 t at a decision value t) of the last iqsim or pick."""
+        v = ctypes.c_int64()
+        check(load().iq_ties(self.h, ctypes.byref(v)))
+        return int(v.value)
+
+    @property
     def launches(self):
         return int(load().iq_ctx_launches(self.h))
 

@@ -177,6 +177,14 @@ extern "C" int iq_ctx_create(int device, iq_ctx** out) {
     return iq_set_error(IQ_ERR_ALLOC, "counter allocation failed");
   }
   cudaMemset(c->d_stats, 0, sizeof(unsigned long long) * ST_COUNT);
+  if (cudaMalloc(&c->d_ties, sizeof(unsigned long long)) != cudaSuccess) {
+    cudaFree(c->d_stats);
+    cudaFree(c->d_status);
+    cudaStreamDestroy(c->stream);
+    delete c;
+    return iq_set_error(IQ_ERR_ALLOC, "counter allocation failed");
+  }
+  cudaMemset(c->d_ties, 0, sizeof(unsigned long long));
   *out = c;
   return IQ_OK;
 }
@@ -201,6 +209,7 @@ extern "C" int iq_ctx_destroy(iq_ctx* ctx) {
     for (auto e : kv.second.ev) cudaEventDestroy(e);
   cudaFree(ctx->d_status);
   cudaFree(ctx->d_stats);
+  cudaFree(ctx->d_ties);
   if (ctx->stream2) {
     cudaStreamSynchronize(ctx->stream2);
     cudaStreamDestroy(ctx->stream2);
@@ -213,6 +222,16 @@ extern "C" int iq_ctx_destroy(iq_ctx* ctx) {
 }
 
 extern "C" void* iq_ctx_stream(iq_ctx* ctx) { return ctx ? (void*)ctx->stream : nullptr; }
+
+extern "C" int iq_ties(iq_ctx* ctx, int64_t* out) {
+  if (!ctx || !out) return iq_set_error(IQ_ERR_ARG, "null argument");
+  IQ_CUDA_OK(cudaSetDevice(ctx->device));
+  unsigned long long v = 0;
+  IQ_CUDA_OK(cudaMemcpyAsync(&v, ctx->d_ties, sizeof(v), cudaMemcpyDeviceToHost, ctx->stream));
+  IQ_CUDA_OK(cudaStreamSynchronize(ctx->stream));
+  *out = (int64_t)v;
+  return IQ_OK;
+}
 
 extern "C" int iq_set_option(iq_ctx* ctx, const char* name, int64_t value) {
   if (!ctx || !name) return iq_set_error(IQ_ERR_ARG, "null argument");
@@ -519,6 +538,8 @@ extern "C" int iq_pick(iq_ctx* ctx, const float* D, int64_t P, int32_t naux,
                    L.seq_zero);
   L.cand = cand; L.k0 = k0; L.v0 = v0; L.k1 = k1; L.v1 = v1; L.w = w; L.prod = prod;
   L.rind = rind; L.ncand = rind + 1; L.status = ctx->d_status;
+  IQ_CUDA_OK(cudaMemsetAsync(ctx->d_ties, 0, sizeof(unsigned long long), ctx->stream));
+  L.ties = ctx->d_ties;
   int rc = iq_launch_pick(ctx, L);
   if (rc) return rc;
   int64_t hr[2];

@@ -761,9 +761,10 @@ size_t tc_smem_bytes(int N) {
 }
 
 // [largest magnitude bits, smallest exponent + 256 of a nonzero magnitude, OR of the low 13
-// mantissa bits] over the finite values
+// mantissa bits, smallest exponent + 256 of the lowest set bit of a nonzero value] over the
+// finite values
 __global__ void value_stats_kernel(const float* __restrict__ d, int64_t n, unsigned* out) {
-  unsigned amax = 0, minx = 0xFFFFFFFFu, low = 0;
+  unsigned amax = 0, minx = 0xFFFFFFFFu, low = 0, lsb = 0xFFFFFFFFu;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x) {
     const unsigned b = __float_as_uint(d[i]) & 0x7FFFFFFFu;
@@ -772,16 +773,20 @@ __global__ void value_stats_kernel(const float* __restrict__ d, int64_t n, unsig
     if (b) {
       const unsigned ex = b >> 23;  // biased exponent; 0 for subnormals
       minx = min(minx, (ex ? ex : 1u) - 127u + 256u);
+      const unsigned sig = ex ? ((b & 0x7FFFFFu) | 0x800000u) : (b & 0x7FFFFFu);
+      lsb = min(lsb, (ex ? ex : 1u) + (unsigned)(__ffs(sig) - 1) - 150u + 256u);
     }
     low |= b & 0x1FFFu;
   }
   amax = __reduce_max_sync(0xffffffffu, amax);
   minx = __reduce_min_sync(0xffffffffu, minx);
   low = __reduce_or_sync(0xffffffffu, low);
+  lsb = __reduce_min_sync(0xffffffffu, lsb);
   if ((threadIdx.x & 31) == 0) {
     atomicMax(out, amax);
     atomicMin(out + 1, minx);
     atomicOr(out + 2, low);
+    atomicMin(out + 3, lsb);
   }
 }
 
@@ -898,17 +903,54 @@ IqValueStats iq_host_stats(const float* v, int64_t n) {
     uint32_t b;
     memcpy(&b, &a, 4);
     s.amax = std::max(s.amax, a);
-    if (a > 0.f) s.minexp = std::min(s.minexp, std::max(std::ilogb(a), -126));
+    if (a > 0.f) {
+      s.minexp = std::min(s.minexp, std::max(std::ilogb(a), -126));
+      const uint32_t ex = b >> 23;
+      const uint32_t sig = ex ? ((b & 0x7FFFFFu) | 0x800000u) : (b & 0x7FFFFFu);
+      s.lsbexp = std::min(s.lsbexp, (int)(ex ? ex : 1u) + __builtin_ctz(sig) - 150);
+    }
     if (b & 0x1FFFu) s.narrow = false;
   }
   return s;
 }
 
+double iq_map_kappa(const IqValueStats& A, const IqValueStats& B, int64_t K, int form) {
+  if (K <= 0) return 0.0;  // empty mask: every term is an exact zero
+  const double u = std::ldexp(1.0, -24);
+  if (!(A.amax > 0.f) || !(B.amax > 0.f)) {
+    // one operand is all zeros: AB = 0 and D = A2 + B2, exact when the squares are
+    const IqValueStats& Z = A.amax > 0.f ? A : B;
+    if (!(Z.amax > 0.f)) return 0.0;
+    const double m = (double)K * (double)Z.amax * (double)Z.amax;
+    if (Z.narrow && m < std::ldexp(1.0, 24 + 2 * Z.lsbexp)) return 0.0;
+  } else if (A.narrow && B.narrow) {
+    // products exact (11-bit factors), all sums on the grid 2^g and below 2^(24 + g)
+    const int g = 2 * std::min(A.lsbexp, B.lsbexp);
+    const double m = (double)K * ((double)A.amax * A.amax + (double)B.amax * B.amax) * 1.001;
+    if (m < std::ldexp(1.0, 24 + g)) return 0.0;
+  }
+  // one MMA adds its products to the FP32 accumulator with a relative error of at most 4u of
+  // (|accumulator| + sum |products|); three MMAs per K-step (hi*hi + hi*lo + lo*hi) of 16
+  // (FP16) or 8 (TF32) offsets; the SIMT kernel rounds once per fused multiply-add; the split
+  // drops 12u |a||b|, the epilogue rounds A2, B2, their sum and the result (4u); and
+  // sum |a||b| <= (A2 + B2) / 2
+  const double nsteps = form == 1 ? std::ceil(K / 16.0) : form == 2 ? std::ceil(K / 8.0) : 0.0;
+  const double acc = form == 0 ? (double)K : 3.0 * nsteps * 4.0;
+  return (acc + 12.0 + 4.0 + 8.0) * u * 1.01;
+}
+
+double iq_map_eabs(const IqValueStats& A, int64_t n_img) {
+  // A2 from a Float64 integral image: each prefix sum of at most n_img squares rounds n_img
+  // times, and a box sum combines 8 of them
+  const double total = (double)n_img * (double)A.amax * (double)A.amax;
+  return 8.0 * (double)n_img * std::ldexp(1.0, -53) * total * 1.01;
+}
+
 int iq_value_stats(iq_ctx* ctx, const float* d, int64_t n, IqValueStats& out) {
   out = IqValueStats();
-  unsigned* buf = (unsigned*)iq_scratch(ctx, S_TCFLAG, 3 * sizeof(unsigned));
+  unsigned* buf = (unsigned*)iq_scratch(ctx, S_TCFLAG, 4 * sizeof(unsigned));
   if (!buf) return IQ_ERR_ALLOC;
-  const unsigned init[3] = {0u, 0xFFFFFFFFu, 0u};
+  const unsigned init[4] = {0u, 0xFFFFFFFFu, 0u, 0xFFFFFFFFu};
   IQ_CUDA_OK(cudaMemcpyAsync(buf, init, sizeof(init), cudaMemcpyHostToDevice, ctx->stream));
   if (n > 0) {
     const int blocks = (int)std::min<int64_t>((n + 255) / 256, 1024);
@@ -916,12 +958,13 @@ int iq_value_stats(iq_ctx* ctx, const float* d, int64_t n, IqValueStats& out) {
     iq_count(ctx);
     IQ_CUDA_OK(cudaGetLastError());
   }
-  unsigned h[3];
+  unsigned h[4];
   IQ_CUDA_OK(cudaMemcpyAsync(h, buf, sizeof(h), cudaMemcpyDeviceToHost, ctx->stream));
   IQ_CUDA_OK(cudaStreamSynchronize(ctx->stream));
   memcpy(&out.amax, &h[0], 4);
   out.minexp = h[1] == 0xFFFFFFFFu ? (1 << 30) : (int)h[1] - 256;
   out.narrow = h[2] == 0u;
+  out.lsbexp = h[3] == 0xFFFFFFFFu ? (1 << 30) : (int)h[3] - 256;
   return IQ_OK;
 }
 

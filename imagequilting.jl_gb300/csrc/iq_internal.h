@@ -22,15 +22,25 @@ struct IqValueStats {
   float amax = 0.f;       // largest magnitude
   int minexp = 1 << 30;   // smallest binary exponent of a nonzero magnitude
   bool narrow = true;     // every value has at most 11 significant bits (a TF32 value)
+  int lsbexp = 1 << 30;   // smallest binary exponent of the lowest set bit of a nonzero value
+                          // (every value is a multiple of 2^lsbexp)
   void merge(const IqValueStats& o) {
     amax = amax > o.amax ? amax : o.amax;
     minexp = minexp < o.minexp ? minexp : o.minexp;
     narrow = narrow && o.narrow;
+    lsbexp = lsbexp < o.lsbexp ? lsbexp : o.lsbexp;
   }
   int maxexp() const;      // binary exponent of amax (0 when amax == 0)
   bool fp16_range() const; // nonzero magnitudes within 2^17 of amax
 };
 IqValueStats iq_host_stats(const float* v, int64_t n);
+// Error coefficient of a distance map of image values A against templates B over K offsets,
+// |D32 - D| <= kappa (A2 + B2) + eabs: 0 when every product, partial sum and square is exact
+// in FP32 (values on a common binary grid, sums below 2^24 of its step), else the bound of the
+// form that computed it (form 1: tensor cores, FP16 halves; 2: tensor cores, TF32 halves;
+// 0: SIMT FP32). n_img: image voxels, for the Float64 integral image behind A2.
+double iq_map_kappa(const IqValueStats& A, const IqValueStats& B, int64_t K, int form);
+double iq_map_eabs(const IqValueStats& A, int64_t n_img);
 
 struct IqTimer {
   std::vector<cudaEvent_t> ev;  // start/stop pairs
@@ -51,6 +61,7 @@ struct iq_ctx {
   int64_t ti_nan = 0;          // number of NaN voxels
   IqValueStats ti_stats;       // magnitude range and precision of the prepared TI
   int* d_status = nullptr;     // device status word (first kernel error)
+  unsigned long long* d_ties = nullptr;  // near-tie count of the last pick or simulation
   // grow-only scratch buffers, by slot
   std::vector<void*> buf;
   std::vector<size_t> buf_bytes;
@@ -100,6 +111,7 @@ enum IqSlot {
   S_PICK_K0, S_PICK_V0, S_PICK_K1, S_PICK_V1, S_PICK_W, S_PICK_PROD, S_RIND, S_NCAND,
   S_CUTBUF, S_CUTSCR, S_DIS, S_AUX, S_AUXTI, S_AUXII, S_HARDLIST, S_HARDPTS, S_OUT,
   S_TMP0, S_TMP1, S_TMP2, S_STARTS, S_SOFTMM, S_TASKS, S_VOX, S_TCB, S_TCCOLS, S_TCSTAGE, S_TCB2, S_TCFLAG, S_TCSOFT, S_SOFTKEYS,
+  S_PICK_RV, S_PICK_RR, S_PICK_RL, S_SOFTB2,
   S_COUNT
 };
 
@@ -263,6 +275,25 @@ int iq_launch_disabled(iq_ctx* ctx, const int32_t* d_nanii, Dim3 dims, Dim3 tile
 // ---------------------------------------------------------------------------------------
 // Pick (iq_pick.cu)
 // ---------------------------------------------------------------------------------------
+// How the pick re-evaluates one distance map directly at chosen positions (the exact re-rank):
+// D[p] = sum over the mask offsets k (klist order, column-major) of (img[p + k] - tmpl[k])^2.
+// The map itself (FP32, from the tensor cores or the SIMT kernel) satisfies
+// |D32[p] - D[p]| <= kappa * (A2[p] + B2) + eabs; kappa == 0 marks a map whose values are
+// exact, which the pick then uses as they are.
+struct ExactSrc {
+  const float* img;       // image (TI or auxiliary TI, prepared: NaN -> 0)
+  int64_t isx, isxy;      // image strides: x extent, x * y extents
+  const uint32_t* klist;  // packed mask offsets, column-major order
+  int K;
+  const float* tmpl;      // template grid at the tile origin (realization 0), or nullptr
+  int64_t tgx, tgxy;      // grid strides
+  int64_t tmpl_rs;        // floats between consecutive realizations' grids (0: shared)
+  const float* kval;      // per-offset template values instead of a grid (hard data)
+  const double* b2;       // sum of squared template values (realization 0)
+  int64_t b2_rs;
+  double kappa, eabs;
+};
+
 // Sources of one tile; realization r of the tile reads D0 + r * D0_rs etc.
 struct PickTask {
   const float* D0; int64_t D0_rs;           // primary distance
@@ -277,6 +308,10 @@ struct PickTask {
   const unsigned long long* aux_keys[IQ_MAX_AUX];
   int nkeys;
   int64_t tile;                             // Philox counter of the draw
+  // direct re-evaluation of D0 and of each auxiliary map (kappa == 0, or img == nullptr:
+  // the map's values are taken as exact)
+  ExactSrc x0;
+  ExactSrc xa[IQ_MAX_AUX];
 };
 
 struct PickLaunch {
@@ -299,13 +334,24 @@ struct PickLaunch {
   uint32_t *k0 = nullptr, *v0 = nullptr, *k1 = nullptr, *v1 = nullptr;
   double* w = nullptr;
   double* prod = nullptr;
+  // exact re-rank scratch, P entries per CTA (needed when a task has a map with kappa > 0)
+  double* rv = nullptr;       // refined values
+  double* rr = nullptr;       // their error radii
+  uint8_t* rl = nullptr;      // their levels
+  int64_t dx = 0, dxy = 0;    // distance-map strides (x extent, x * y extents)
   // outputs, one per CTA
   int64_t* rind = nullptr;
   int64_t* ncand = nullptr;  // nullable
   int* status = nullptr;
+  unsigned long long* ties = nullptr;   // near-tie counter (nullable)
   unsigned long long* stats = nullptr;  // profiling counters (nullable)
 };
 int iq_launch_pick(iq_ctx* ctx, const PickLaunch& L);
+// an ExactSrc that marks a map as exact (no re-rank)
+inline ExactSrc iq_exact_none() {
+  ExactSrc s{};
+  return s;
+}
 
 // Selection keys of nmaps maps of P floats (map m at maps + m * P, its [min, max finite] bits
 // at mm + 2 m) for the sizes seq[0..nq): keys[m * nq + q] (iq_pick.cu)

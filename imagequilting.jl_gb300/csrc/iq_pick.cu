@@ -44,9 +44,14 @@ struct PickArgs {
   uint32_t *k0, *v0, *k1, *v1;
   double* w;
   double* prod;
+  double* rv;
+  double* rr;
+  uint8_t* rl;
+  int64_t dx, dxy;
   int64_t* rind;
   int64_t* ncand;
   int* status;
+  unsigned long long* ties;
   unsigned long long* stats;
 };
 
@@ -187,7 +192,7 @@ __device__ __forceinline__ bool key_le(uint32_t b, uint32_t p, Key k) {
 
 // Radix select (MSD, 8-bit digits) of the kk-th smallest (value, index) key: the general
 // fallback. With `fixed_value` set it only selects among the indices holding that value.
-__device__ Key radix_select(Smem& s, uint32_t* wcnt, const float* __restrict__ src, int64_t P,
+__device__ __noinline__ Key radix_select(Smem& s, uint32_t* wcnt, const float* __restrict__ src, int64_t P,
                             int64_t kk, bool fixed_value, uint32_t value) {
   uint32_t prefix = 0, mask = 0;
   const int64_t iters = (P + PT - 1) / PT;
@@ -272,7 +277,7 @@ __device__ __forceinline__ int bin_shift(uint32_t mn, uint32_t mx) {
 constexpr int SEL_BATCH = 8;  // loads in flight per thread and source in the select passes
 
 template <int NS>
-__device__ void hist_select(Smem& s, uint32_t* hist, unsigned long long* sbuf, SelReq* req,
+__device__ __noinline__ void hist_select(Smem& s, uint32_t* hist, unsigned long long* sbuf, SelReq* req,
                             int64_t P, Key* out) {
   uint32_t lo[NS], hi[NS];
   int sh[NS];
@@ -425,6 +430,8 @@ __device__ int64_t compact(Smem& s, const Pred& pred, int64_t P, int32_t* out) {
 
 struct ThrPred {
   const float* D; double thr;
+  double tiew;                        // near-tie window 1e-6 thr (0: none)
+  mutable unsigned long long nt = 0;  // this thread's near-ties |D - thr| <= tiew
   // bit i set when D[p0 + i] <= thr (positions past P excluded)
   __device__ uint32_t eval8(int64_t p0, int64_t P) const {
     float v[CITEMS];
@@ -432,18 +439,45 @@ struct ThrPred {
     for (int i = 0; i < CITEMS; ++i) v[i] = p0 + i < P ? D[p0 + i] : __int_as_float(0x7F800000);
     uint32_t bits = 0;
 #pragma unroll
-    for (int i = 0; i < CITEMS; ++i)
+    for (int i = 0; i < CITEMS; ++i) {
       if (p0 + i < P && (double)v[i] <= thr) bits |= 1u << i;
+      if (tiew > 0.0 && p0 + i < P && fabs(__dsub_rn((double)v[i], thr)) <= tiew) nt++;
+    }
     return bits;
   }
 };
 
+// Band of one refined top-k selection: D < lo is in, D > hi is out, positions in between are
+// listed (ascending, bit 31 set when in).
+struct Band {
+  double lo, hi;
+  int32_t* list;
+  int64_t n;
+};
+
+__device__ __forceinline__ bool band_member(const Band& b, int64_t p, float d) {
+  const double dv = (double)d;
+  if (dv < b.lo) return true;
+  if (dv > b.hi) return false;
+  int64_t lo = 0, hi = b.n - 1;
+  while (lo <= hi) {
+    const int64_t mid = (lo + hi) >> 1;
+    const int32_t e = b.list[mid];
+    const int64_t q = e & 0x7FFFFFFF;
+    if (q == p) return (e & (int32_t)0x80000000) != 0;
+    if (q < p) lo = mid + 1; else hi = mid - 1;
+  }
+  return false;  // not reached for a position inside the band
+}
+
 template <int NAUX>
 struct RelaxPred {
   const float* D; Key kD;
+  const Band* bD;  // refined selection of D (nullable: the key decides)
   int naux;  // <= NAUX
   const float* aux[NAUX > 0 ? NAUX : 1];
   Key ka[NAUX > 0 ? NAUX : 1];
+  const Band* ba[NAUX > 0 ? NAUX : 1];
   // bit i set when position p0 + i is in the top set of D and of every auxiliary source
   __device__ uint32_t eval8(int64_t p0, int64_t P) const {
     uint32_t b[CITEMS];
@@ -451,8 +485,12 @@ struct RelaxPred {
     for (int i = 0; i < CITEMS; ++i) b[i] = p0 + i < P ? fbits(D[p0 + i]) : 0xFFFFFFFFu;
     uint32_t bits = 0;
 #pragma unroll
-    for (int i = 0; i < CITEMS; ++i)
-      if (p0 + i < P && key_le(b[i], (uint32_t)(p0 + i), kD)) bits |= 1u << i;
+    for (int i = 0; i < CITEMS; ++i) {
+      if (p0 + i >= P) continue;
+      const bool in = bD ? band_member(*bD, p0 + i, __uint_as_float(b[i]))
+                         : key_le(b[i], (uint32_t)(p0 + i), kD);
+      if (in) bits |= 1u << i;
+    }
 #pragma unroll
     for (int a = 0; a < NAUX; ++a) {
       if (a >= naux || !bits) continue;
@@ -460,8 +498,12 @@ struct RelaxPred {
 #pragma unroll
       for (int i = 0; i < CITEMS; ++i) c[i] = (bits >> i & 1u) ? fbits(aux[a][p0 + i]) : 0u;
 #pragma unroll
-      for (int i = 0; i < CITEMS; ++i)
-        if ((bits >> i & 1u) && !key_le(c[i], (uint32_t)(p0 + i), ka[a])) bits &= ~(1u << i);
+      for (int i = 0; i < CITEMS; ++i) {
+        if (!(bits >> i & 1u)) continue;
+        const bool in = ba[a] ? band_member(*ba[a], p0 + i, __uint_as_float(c[i]))
+                              : key_le(c[i], (uint32_t)(p0 + i), ka[a]);
+        if (!in) bits &= ~(1u << i);
+      }
     }
     return bits;
   }
@@ -469,7 +511,7 @@ struct RelaxPred {
 
 // Stable LSD radix sort of (keys, vals)[0..n) between the buffer pairs (global memory);
 // returns 0 if the result is in (ka, va), 1 if in (kb, vb).
-__device__ int radix_sort(Smem& s, uint32_t* wcnt, uint32_t* ka, uint32_t* va, uint32_t* kb,
+__device__ __noinline__ int radix_sort(Smem& s, uint32_t* wcnt, uint32_t* ka, uint32_t* va, uint32_t* kb,
                           uint32_t* vb, int64_t n) {
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   int cur = 0;
@@ -528,7 +570,7 @@ __device__ int radix_sort(Smem& s, uint32_t* wcnt, uint32_t* ka, uint32_t* va, u
 
 // Dense ranks (1-based) of src[cand[i]], i < n, written to rank[i]; returns the sum of
 // (n - rank + 1) over i. `rank` must not alias k0/v0/k1/v1.
-__device__ unsigned long long dense_ranks(Smem& s, unsigned long long* sbuf,
+__device__ __noinline__ unsigned long long dense_ranks(Smem& s, unsigned long long* sbuf,
                                           const float* __restrict__ src,
                                           const int32_t* __restrict__ cand, int64_t n,
                                           uint32_t* k0, uint32_t* v0, uint32_t* k1, uint32_t* v1,
@@ -603,6 +645,540 @@ __device__ unsigned long long dense_ranks(Smem& s, unsigned long long* sbuf,
   return block_sum_u64(s, acc);
 }
 
+// =============================================================================================
+// Exact re-rank (continuous data)
+//
+// The FP32 maps of the correlation kernels carry an error |D32 - D| <= kappa (A2 + B2) + eabs
+// (cancellation in A2 - 2AB + B2). Decisions of the pick depend only on a few positions near
+// their decision value (the threshold, a top-k boundary, the order of candidates for the tau
+// model), so those positions are re-evaluated directly, D[p] = sum_k (img[p + k] - tmpl_k)^2 --
+// a sum of non-negative terms without cancellation -- at increasing precision until every
+// decision is certain:
+//   level 1  FP32, 32 lanes each summing every 32nd offset, then a 5-step butterfly:
+//            relative error <= (ceil(K/32) + 8) 2^-24
+//   level 2  the same in double-float (pairs of FP32 numbers, error-free sums and products):
+//            relative error <= 4.1 (ceil(K/32) + 8) 2^-48
+//   level 3  the Float64 sequence of the oracle (oracle/direct.c): offsets in column-major
+//            order, d = a - b, D = D + d * d, every operation rounded separately
+// Each level gives an interval [v - r, v + r] that holds the level-3 value (the radius also
+// covers the (K + 2) 2^-53 difference between the level-3 value and the exact sum), so a
+// decision taken on disjoint intervals is the decision the Float64 distance would give.
+// =============================================================================================
+constexpr double RU32 = 5.9604644775390625e-08;  // 2^-24
+constexpr double RU64 = 1.1102230246251565e-16;  // 2^-53
+constexpr double TIE_RTOL = 1e-6;                 // relative window of a reported near-tie
+constexpr double TINY32 = 1.401298464324817e-45;  // smallest FP32 subnormal
+
+// One map of one realization, as the re-rank reads it.
+struct Ref {
+  const float* img;
+  int64_t isx, isxy;
+  const uint32_t* kl;
+  int K;
+  const float* tm;
+  int64_t tgx, tgxy;
+  const float* kv;
+  double b2, kappa, eabs;
+  int64_t dx, dxy;
+};
+
+__device__ __forceinline__ bool ref_on(const ExactSrc& s) {
+  return s.img != nullptr && s.kappa > 0.0;
+}
+
+__device__ Ref make_ref(const ExactSrc& s, int r, int64_t dx, int64_t dxy) {
+  Ref f;
+  f.img = s.img; f.isx = s.isx; f.isxy = s.isxy;
+  f.kl = s.klist; f.K = s.K;
+  f.tm = s.tmpl ? s.tmpl + r * s.tmpl_rs : nullptr;
+  f.tgx = s.tgx; f.tgxy = s.tgxy;
+  f.kv = s.kval;
+  f.b2 = s.b2 ? s.b2[r * s.b2_rs] : 0.0;
+  f.kappa = s.kappa; f.eabs = s.eabs;
+  f.dx = dx; f.dxy = dxy;
+  return f;
+}
+
+// image index of the window origin of map position p
+__device__ __forceinline__ int64_t ref_base(const Ref& f, int64_t p) {
+  const int64_t z = p / f.dxy, rem = p - z * f.dxy, y = rem / f.dx, x = rem - y * f.dx;
+  return x + f.isx * y + f.isxy * z;
+}
+
+__device__ __forceinline__ void ref_term(const Ref& f, int64_t base, int j, float& a, float& b) {
+  const uint32_t k = __ldg(f.kl + j);
+  const int kx = kx_of(k), ky = ky_of(k), kz = kz_of(k);
+  a = __ldg(f.img + base + kx + f.isx * ky + f.isxy * kz);
+  b = f.kv ? __ldg(f.kv + j) : __ldg(f.tm + kx + f.tgx * ky + f.tgxy * kz);
+}
+
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+  s = __fadd_rn(a, b);
+  const float bb = __fsub_rn(s, a);
+  e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+
+// (h, l) += (x, y) in double-float arithmetic; symmetric in its two operands
+__device__ __forceinline__ void df_add(float& h, float& l, float x, float y) {
+  float s, e;
+  two_sum(h, x, s, e);
+  e = __fadd_rn(e, __fadd_rn(l, y));
+  h = __fadd_rn(s, e);
+  l = __fsub_rn(e, __fsub_rn(h, s));
+}
+
+// Warp-collective: value and radius of D[p] at `level` (every lane gets the same result).
+__device__ __noinline__ void ref_eval(const Ref& f, int64_t p, int level, double& v, double& r) {
+  const int lane = threadIdx.x & 31;
+  const int64_t base = ref_base(f, p);
+  const int nl = (f.K + 31) / 32;
+  const double tail = (double)(f.K + 2) * RU64 * 1.02;   // level 3 vs the exact sum
+  if (level <= 1) {
+    float acc = 0.f;
+    for (int j = lane; j < f.K; j += 32) {
+      float a, b;
+      ref_term(f, base, j, a, b);
+      const float d = __fsub_rn(a, b);
+      acc = __fmaf_rn(d, d, acc);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) acc = __fadd_rn(acc, __shfl_xor_sync(0xffffffffu, acc, o));
+    v = (double)acc;
+    r = v * ((double)(nl + 8) * RU32 * 1.02 + tail) + (double)(f.K + 8) * TINY32 * 4.0;
+  } else if (level == 2) {
+    float h = 0.f, l = 0.f;
+    for (int j = lane; j < f.K; j += 32) {
+      float a, b;
+      ref_term(f, base, j, a, b);
+      float dh, dl;
+      two_sum(a, -b, dh, dl);                               // a - b = dh + dl exactly
+      const float p2 = __fmul_rn(dh, dh);
+      const float pe = __fmaf_rn(dh, dh, -p2);              // dh^2 = p2 + pe exactly
+      const float q = __fmaf_rn(__fadd_rn(dh, dh), dl, pe);  // + 2 dh dl (dl^2 dropped)
+      df_add(h, l, p2, q);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const float h2 = __shfl_xor_sync(0xffffffffu, h, o);
+      const float l2 = __shfl_xor_sync(0xffffffffu, l, o);
+      df_add(h, l, h2, l2);
+    }
+    v = (double)h + (double)l;
+    r = v * ((double)(nl + 8) * 4.1 * RU32 * RU32 * 1.02 + tail + RU64) +
+        (double)(f.K + 8) * TINY32 * 8.0;
+  } else {
+    // the oracle's sequence: lanes load and square 32 terms at a time, lane 0 adds them in
+    // offset order
+    double acc = 0.0;
+    for (int j0 = 0; j0 < f.K; j0 += 32) {
+      double t = 0.0;
+      const int j = j0 + lane;
+      if (j < f.K) {
+        float a, b;
+        ref_term(f, base, j, a, b);
+        const double d = __dsub_rn((double)a, (double)b);
+        t = __dmul_rn(d, d);
+      }
+      const int m = min(32, f.K - j0);
+      for (int i = 0; i < m; ++i) {
+        const double ti = __shfl_sync(0xffffffffu, t, i);
+        acc = __dadd_rn(acc, ti);
+      }
+    }
+    v = acc;
+    r = 0.0;
+  }
+}
+
+// Error bound of the map at positions whose distance is at most Dc:
+// kappa (A2 + B2) + eabs with A2 <= (|b| + sqrt(Dc))^2 (triangle inequality).
+__device__ __forceinline__ double tier0_bound(const Ref& f, double Dc) {
+  const double sb = sqrt(fmax(f.b2, 0.0)), sd = sqrt(fmax(Dc, 0.0));
+  return (f.kappa * ((sb + sd) * (sb + sd) + f.b2) + f.eabs) * 1.001 + 1e-300;
+}
+
+// Per-entry state of a refinement list, P entries per CTA.
+struct RefArr {
+  double* v;
+  double* r;
+  uint8_t* l;     // level (low 7 bits), 0x80 = to be raised
+  uint8_t* link;  // 1 where sorted positions t and t + 1 were re-evaluated together
+};
+
+// Level 1 for entries [0, n) of pos (warp per entry).
+__device__ __noinline__ void ref_init(const Ref& f, const int32_t* pos, int64_t n, RefArr a) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  for (int64_t i = warp; i < n; i += NW) {
+    double v, r;
+    ref_eval(f, pos[i] & 0x7FFFFFFF, 1, v, r);
+    if (lane == 0) { a.v[i] = v; a.r[i] = r; a.l[i] = 1; }
+  }
+  __syncthreads();
+}
+
+// Raise every marked entry by one level, or to level 3 when `to3`.
+__device__ __noinline__ void ref_raise(const Ref& f, const int32_t* pos, int64_t n, RefArr a, bool to3) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  for (int64_t i = warp; i < n; i += NW) {
+    const uint8_t l = a.l[i];
+    if (!(l & 0x80)) continue;
+    const int nl = to3 ? 3 : min((l & 0x7F) + 1, 3);
+    double v, r;
+    ref_eval(f, pos[i] & 0x7FFFFFFF, nl, v, r);
+    if (lane == 0) { a.v[i] = v; a.r[i] = r; a.l[i] = (uint8_t)nl; }
+  }
+  __syncthreads();
+}
+
+__device__ __forceinline__ bool ref_exact(const RefArr& a, uint32_t i) { return (a.l[i] & 0x7F) == 3; }
+__device__ __forceinline__ void ref_mark(RefArr& a, uint32_t i) {
+  if ((a.l[i] & 0x7F) < 3) a.l[i] = (uint8_t)(a.l[i] | 0x80);  // racing writers store one value
+}
+
+// (value, position) order of entries i and j
+__device__ __forceinline__ bool ref_less(const RefArr& a, const int32_t* pos, uint32_t i, uint32_t j) {
+  const double vi = a.v[i], vj = a.v[j];
+  return vi < vj || (vi == vj && (pos[i] & 0x7FFFFFFF) < (pos[j] & 0x7FFFFFFF));
+}
+
+// Sort entries [0, n) by (level-1 value, ordinal) into ord[0, n) (ordinals; ordinal order is
+// position order): a bitonic sort in shared memory up to SORT_CAP, else the radix sort.
+__device__ const uint32_t* ref_sort(Smem& s, unsigned long long* sbuf, int64_t n, RefArr a,
+                                    uint32_t* k0, uint32_t* v0, uint32_t* k1, uint32_t* v1) {
+  if (n <= SORT_CAP) {
+    for (int64_t i = threadIdx.x; i < n; i += PT)
+      sbuf[i] = ((unsigned long long)__float_as_uint((float)a.v[i]) << 32) | (uint32_t)i;
+    __syncthreads();
+    bitonic_sort(sbuf, (int)n);
+    for (int64_t i = threadIdx.x; i < n; i += PT) v0[i] = (uint32_t)sbuf[i];
+    __syncthreads();
+    return v0;
+  }
+  for (int64_t i = threadIdx.x; i < n; i += PT) {
+    k0[i] = __float_as_uint((float)a.v[i]);
+    v0[i] = (uint32_t)i;
+  }
+  __syncthreads();
+  const int where = radix_sort(s, reinterpret_cast<uint32_t*>(sbuf), k0, v0, k1, v1, n);
+  return where ? v1 : v0;
+}
+
+// Make the order ord[0, n) exact: while two neighbours' intervals overlap (and are not both
+// exact), raise both and re-sort the runs of raised neighbours by (value, position). At the
+// end every adjacent pair is disjoint or both exact, so the order is the order of the Float64
+// distances with ties broken by position.
+__device__ __noinline__ void ref_resolve(Smem& s, const Ref& f, const int32_t* pos, int64_t n, uint32_t* ord,
+                            RefArr a) {
+  for (int round = 0; round < 64; ++round) {
+    int any = 0;
+    for (int64_t t = threadIdx.x; t < n; t += PT) a.link[t] = 0;
+    __syncthreads();
+    for (int64_t t = threadIdx.x; t + 1 < n; t += PT) {
+      const uint32_t i = ord[t], j = ord[t + 1];
+      if (ref_exact(a, i) && ref_exact(a, j)) continue;
+      if (a.v[i] + a.r[i] >= a.v[j] - a.r[j]) {
+        a.link[t] = 1;
+        any = 1;
+      }
+    }
+    if (!__syncthreads_or(any)) break;
+    for (int64_t t = threadIdx.x; t + 1 < n; t += PT)
+      if (a.link[t]) { ref_mark(a, ord[t]); ref_mark(a, ord[t + 1]); }
+    __syncthreads();
+    ref_raise(f, pos, n, a, round >= 3);
+    // runs of linked neighbours [t, e]: insertion sort by (value, position)
+    for (int64_t t = threadIdx.x; t + 1 < n; t += PT) {
+      if (!a.link[t] || (t > 0 && a.link[t - 1])) continue;
+      int64_t e = t + 1;
+      while (e + 1 < n && a.link[e]) ++e;
+      for (int64_t x = t + 1; x <= e; ++x) {
+        const uint32_t key = ord[x];
+        int64_t y = x - 1;
+        while (y >= t && ref_less(a, pos, key, ord[y])) {
+          ord[y + 1] = ord[y];
+          --y;
+        }
+        ord[y + 1] = key;
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// Near-tie test |D - t| <= 1e-6 t (evaluated as the oracle does, in Float64) of entry i against
+// the value t of entry b: 1 yes, 0 no, -1 undecided on the current intervals.
+__device__ __forceinline__ int ref_tie(const RefArr& a, uint32_t i, double tv, double tr, bool texact) {
+  const double vi = a.v[i], ri = a.r[i];
+  if (ref_exact(a, i) && texact)
+    return fabs(__dsub_rn(vi, tv)) <= __dmul_rn(TIE_RTOL, tv) ? 1 : 0;
+  const double far = fmax(fabs(vi + ri - (tv - tr)), fabs(vi - ri - (tv + tr)));
+  const double near = fmax(0.0, fmax((vi - ri) - (tv + tr), (tv - tr) - (vi + ri)));
+  const double wlo = TIE_RTOL * (tv - tr), whi = TIE_RTOL * (tv + tr);
+  if (far <= wlo * (1.0 - 1e-9)) return 1;
+  if (near > whi * (1.0 + 1e-9)) return 0;
+  return -1;
+}
+
+// Near-ties among entries [0, n) against the value of entry b (b itself excluded when
+// skip_b): raises undecided entries (and b) until every test is decided.
+__device__ __noinline__ unsigned long long ref_count_ties(Smem& s, const Ref& f, const int32_t* pos, int64_t n,
+                                             RefArr a, int64_t b, bool skip_b, double tfix) {
+  for (int round = 0; round < 8; ++round) {
+    double tv, tr;
+    bool tex;
+    if (b >= 0) { tv = a.v[b]; tr = a.r[b]; tex = ref_exact(a, (uint32_t)b); }
+    else { tv = tfix; tr = 0.0; tex = true; }
+    unsigned long long cnt = 0;
+    int und = 0;
+    for (int64_t i = threadIdx.x; i < n; i += PT) {
+      if (skip_b && i == b) continue;
+      const int t = ref_tie(a, (uint32_t)i, tv, tr, tex);
+      if (t > 0) cnt++;
+      if (t < 0) { und = 1; ref_mark(a, (uint32_t)i); }
+    }
+    if (und && b >= 0 && threadIdx.x == 0) ref_mark(a, (uint32_t)b);
+    if (!__syncthreads_or(und)) return block_sum_u64(s, cnt);
+    ref_raise(f, pos, n, a, round >= 2);
+  }
+  return 0;  // not reached: level-3 tests always decide
+}
+
+// Ordered compaction of the positions of `src` with lo <= D <= hi into out; `below` receives
+// the count of positions with D < lo (Inf and NaN are neither).
+__device__ __noinline__ int64_t band_collect(Smem& s, const float* __restrict__ src, int64_t P, double lo,
+                                double hi, int32_t* out, int64_t& below) {
+  int64_t base = 0;
+  unsigned long long nb = 0;
+  const int64_t tile = (int64_t)PT * CITEMS;
+  for (int64_t t0 = 0; t0 < P; t0 += tile) {
+    const int64_t p0 = t0 + (int64_t)threadIdx.x * CITEMS;
+    uint32_t bits = 0;
+#pragma unroll
+    for (int i = 0; i < CITEMS; ++i) {
+      if (p0 + i >= P) continue;
+      const double d = (double)src[p0 + i];
+      if (d < lo) nb++;
+      else if (d <= hi) bits |= 1u << i;
+    }
+    uint32_t total;
+    const uint32_t off = block_excl_sum(s, (uint32_t)__popc(bits), total);
+    int64_t o = base + off;
+#pragma unroll
+    for (int i = 0; i < CITEMS; ++i)
+      if (bits >> i & 1u) out[o++] = (int32_t)(p0 + i);
+    base += total;
+  }
+  below = (int64_t)block_sum_u64(s, nb);
+  return base;
+}
+
+// The exact top-k set of a refined map, given the k-th (value, index) key of its FP32 values:
+// fills `b` (list at `list`) and returns the near-ties at the boundary, or -1 when the bound
+// failed (the FP32 k-th value lies outside the band: then the key is kept as it is).
+__device__ __noinline__ long long band_topk(Smem& s, unsigned long long* sbuf, const Ref& f,
+                               const float* __restrict__ src, int64_t P, int64_t k, Key kv,
+                               int32_t* list, RefArr a, uint32_t* k0, uint32_t* v0, uint32_t* k1,
+                               uint32_t* v1, Band& b) {
+  const double v = (double)__uint_as_float(kv.v);
+  if (!(v < 1e300)) return -1;  // Inf boundary: the key is exact
+  // E0 valid up to Dc = v + 4E, E = E0 plus half the near-tie window
+  double E0 = tier0_bound(f, v * 1.001), E = 0.0;
+  for (int it = 0; it < 200; ++it) {
+    E = E0 + 0.51 * TIE_RTOL * (v + E0);
+    const double need = tier0_bound(f, v + 4.0 * E);
+    if (need <= E0) break;
+    E0 = fmax(need, 1.5 * E0);
+  }
+  b.lo = v - 2.0 * E;
+  b.hi = v + 2.0 * E;
+  b.list = list;
+  int64_t below = 0;
+  b.n = band_collect(s, src, P, b.lo, b.hi, list, below);
+  const int64_t kk = k - below;
+  if (kk < 1 || kk > b.n) { b.n = 0; return -1; }
+  ref_init(f, list, b.n, a);
+  uint32_t* ord = const_cast<uint32_t*>(ref_sort(s, sbuf, b.n, a, k0, v0, k1, v1));
+  ref_resolve(s, f, list, b.n, ord, a);
+  for (int64_t t = threadIdx.x; t < kk; t += PT) list[ord[t]] |= (int32_t)0x80000000;
+  __syncthreads();
+  const int64_t bi = ord[kk - 1];
+  __syncthreads();
+  return (long long)ref_count_ties(s, f, list, b.n, a, bi, true, 0.0);
+}
+
+// Near-ties of an exact map against t (Float64 test of the oracle), counted over all positions.
+__device__ __noinline__ unsigned long long count_near(Smem& s, const float* __restrict__ src, int64_t P,
+                                         double t) {
+  unsigned long long c = 0;
+  if (t > 0.0 && t < 1e300) {
+    const double w = __dmul_rn(TIE_RTOL, t);
+    for (int64_t p = threadIdx.x; p < P; p += PT) {
+      const double d = (double)src[p];
+      if (d < 1e300 && fabs(__dsub_rn(d, t)) <= w) c++;
+    }
+  }
+  return block_sum_u64(s, c);
+}
+
+// Dense ranks (1-based) of a refined source over the candidates cand[0, n), written to rank[i];
+// returns the sum of (n - rank + 1). Ties of the Float64 distance share a rank.
+// `have`: the intervals of the candidates are in `a` already (the refined threshold pick).
+__device__ __noinline__ unsigned long long dense_ranks_refined(Smem& s, unsigned long long* sbuf, const Ref& f,
+                                                  const int32_t* cand, int64_t n, RefArr a,
+                                                  bool have, uint32_t* k0, uint32_t* v0,
+                                                  uint32_t* k1, uint32_t* v1, uint32_t* rank) {
+  if (!have) ref_init(f, cand, n, a);
+  uint32_t* ord = const_cast<uint32_t*>(ref_sort(s, sbuf, n, a, k0, v0, k1, v1));
+  ref_resolve(s, f, cand, n, ord, a);
+  uint32_t carry = 0;
+  unsigned long long acc = 0;
+  for (int64_t t0 = 0; t0 < n; t0 += PT) {
+    const int64_t t = t0 + threadIdx.x;
+    uint32_t fl = 0, idx = 0;
+    if (t < n) {
+      idx = ord[t];
+      if (t == 0) {
+        fl = 1;
+      } else {
+        const uint32_t j = ord[t - 1];
+        fl = (ref_exact(a, idx) && ref_exact(a, j) && a.v[idx] == a.v[j]) ? 0u : 1u;
+      }
+    }
+    uint32_t total;
+    const uint32_t ex = block_excl_sum(s, fl, total);
+    if (t < n) {
+      const uint32_t r = carry + ex + fl;
+      rank[idx] = r;
+      acc += (unsigned long long)(n - r + 1);
+    }
+    carry += total;
+  }
+  __syncthreads();
+  return block_sum_u64(s, acc);
+}
+
+// Keep the entries i of (pos, a) with a.link[i] != 0, in order (in place); returns the count.
+__device__ __noinline__ int64_t ref_filter(Smem& s, int32_t* pos, int64_t n, RefArr a) {
+  int64_t base = 0;
+  for (int64_t t0 = 0; t0 < n; t0 += PT) {
+    const int64_t i = t0 + threadIdx.x;
+    bool keep = false;
+    int32_t pp = 0;
+    double v = 0.0, r = 0.0;
+    uint8_t l = 0;
+    if (i < n && a.link[i]) {
+      keep = true;
+      pp = pos[i]; v = a.v[i]; r = a.r[i]; l = a.l[i];
+    }
+    uint32_t total;
+    const uint32_t off = block_excl_sum(s, keep ? 1u : 0u, total);
+    if (keep) {
+      const int64_t o = base + off;
+      pos[o] = pp; a.v[o] = v; a.r[o] = r; a.l[o] = l;
+    }
+    base += total;
+    __syncthreads();
+  }
+  return base;
+}
+
+__device__ double block_min_f64(Smem& s, double v) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = fmin(v, __shfl_xor_sync(0xffffffffu, v, o));
+  double* red = reinterpret_cast<double*>(s.wred);
+  if (lane == 0) red[wid] = v;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double m = red[0];
+    for (int i = 1; i < NW; ++i) m = fmin(m, red[i]);
+    red[0] = m;
+  }
+  __syncthreads();
+  const double m = red[0];
+  __syncthreads();
+  return m;
+}
+
+// Threshold pick of a refined map (src/iqsim.jl:237): the candidates D <= (1 + tol) min D of the
+// Float64 distance, ascending in cand[0, n), with their intervals in `a`; `ties` receives the
+// positions within 1e-6 of the threshold. m32 is the smallest FP32 value (finite).
+__device__ __noinline__ int64_t thr_refined(Smem& s, const Ref& f, const float* __restrict__ D, int64_t P,
+                               double m32, double tol, int32_t* cand, RefArr a,
+                               unsigned long long& ties) {
+  // every candidate, the minimum and every near-tie have D32 <= cut
+  double E0 = tier0_bound(f, (1.0 + tol) * m32 * 1.01), cut = 0.0;
+  for (int it = 0; it < 200; ++it) {
+    cut = (1.0 + tol) * (m32 + E0) * (1.0 + 1.01 * TIE_RTOL) + E0;
+    const double need = tier0_bound(f, cut + 2.0 * E0);
+    if (need <= E0) break;
+    E0 = fmax(need, 1.5 * E0);
+  }
+  int64_t below = 0;
+  const int64_t n0 = band_collect(s, D, P, -1.0, cut, cand, below);
+  ref_init(f, cand, n0, a);
+  // the exact minimum: raise every entry whose interval reaches below the smallest upper bound
+  double mhi = 0.0;
+  for (int round = 0; round < 8; ++round) {
+    double up = 1e308;
+    for (int64_t i = threadIdx.x; i < n0; i += PT) up = fmin(up, a.v[i] + a.r[i]);
+    mhi = block_min_f64(s, up);
+    int any = 0;
+    for (int64_t i = threadIdx.x; i < n0; i += PT)
+      if (a.v[i] - a.r[i] <= mhi && !ref_exact(a, (uint32_t)i)) { ref_mark(a, (uint32_t)i); any = 1; }
+    if (!__syncthreads_or(any)) break;
+    ref_raise(f, cand, n0, a, round >= 1);
+  }
+  double mloc = 1e308;
+  for (int64_t i = threadIdx.x; i < n0; i += PT)
+    if (a.v[i] - a.r[i] <= mhi) mloc = fmin(mloc, a.v[i]);
+  const double mstar = block_min_f64(s, mloc);
+  const double thr = __dmul_rn(__dadd_rn(1.0, tol), mstar);
+  ties += ref_count_ties(s, f, cand, n0, a, -1, false, thr);
+  // membership D <= thr, raising undecided entries
+  for (int round = 0; round < 8; ++round) {
+    int und = 0;
+    for (int64_t i = threadIdx.x; i < n0; i += PT) {
+      const double v = a.v[i], r = a.r[i];
+      uint8_t in = 0;
+      if (ref_exact(a, (uint32_t)i)) in = v <= thr;
+      else if (v + r <= thr) in = 1;
+      else if (v - r > thr) in = 0;
+      else { ref_mark(a, (uint32_t)i); und = 1; }
+      a.link[i] = in;
+    }
+    if (!__syncthreads_or(und)) break;
+    ref_raise(f, cand, n0, a, round >= 1);
+  }
+  return ref_filter(s, cand, n0, a);
+}
+
+// Whether every enabled position of a refined map has distance exactly 0 (the relaxation's
+// all-zero case, src/relaxation.jl:11): impossible once the largest FP32 value exceeds the
+// map's error bound at 0; otherwise every mask value is compared with its window.
+__device__ __noinline__ bool all_zero_refined(const Ref& f, const float* __restrict__ D, int64_t P,
+                                 unsigned mxbits) {
+  if ((double)__uint_as_float(mxbits) > tier0_bound(f, 0.0)) return false;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t step = (int64_t)NW * 8;
+  for (int64_t p0 = 0; p0 < P; p0 += step) {
+    int bad = 0;
+    for (int64_t p = p0 + warp; p < P && p < p0 + step; p += NW) {
+      if (!(D[p] < __int_as_float(0x7F800000))) continue;
+      const int64_t base = ref_base(f, p);
+      int mis = 0;
+      for (int j = lane; j < f.K; j += 32) {
+        float x, y;
+        ref_term(f, base, j, x, y);
+        mis |= x != y;
+      }
+      if (__any_sync(0xffffffffu, mis)) bad = 1;
+    }
+    if (__syncthreads_or(bad)) return false;
+  }
+  return true;
+}
+
 // One CTA per (task, realization): CTA b picks for realization b % nreal of task b / nreal.
 // NAUX is the largest number of auxiliary sources of the launch's tasks.
 template <int NAUX>
@@ -634,27 +1210,59 @@ __global__ void __launch_bounds__(PT) pick_kernel(const PickArgs a) {
     amm[j] = j < naux ? tk.aux_mm[j] + r * tk.aux_mm_rs[j] : nullptr;
   }
 
+  // exact re-rank state (used only for maps with kappa > 0)
+  RefArr ra;
+  ra.v = a.rv ? a.rv + b * P : nullptr;
+  ra.r = a.rr ? a.rr + b * P : nullptr;
+  ra.l = a.rl ? a.rl + 2 * b * P : nullptr;
+  ra.link = a.rl ? a.rl + 2 * b * P + P : nullptr;
+  const bool can_ref = a.rv != nullptr;
+  __shared__ Band sband[1 + (NAUX > 0 ? NAUX : 1)];
+  unsigned long long ties = 0;
+
   const bool prof = a.stats != nullptr && threadIdx.x == 0;
   const long long t0 = prof ? clock64() : 0;
   int64_t n;
+  bool have0 = false;  // D's candidate intervals are in ra (refined threshold pick)
   if (naux == 0) {
     const float mn = __uint_as_float(mm[0]);
-    const double thr = __dmul_rn(__dadd_rn(1.0, a.tol), (double)mn);
-    ThrPred pr{D, thr};
-    n = compact(s, pr, P, cand);
+    if (can_ref && ref_on(tk.x0) && mn < __int_as_float(0x7F800000)) {
+      const Ref f0 = make_ref(tk.x0, r, a.dx, a.dxy);
+      n = thr_refined(s, f0, D, P, (double)mn, a.tol, cand, ra, ties);
+      have0 = true;
+    } else {
+      const double thr = __dmul_rn(__dadd_rn(1.0, a.tol), (double)mn);
+      ThrPred pr{D, thr, (thr > 0.0 && thr < 1e300) ? __dmul_rn(TIE_RTOL, thr) : 0.0};
+      n = compact(s, pr, P, cand);
+      ties += block_sum_u64(s, pr.nt);
+    }
   } else {
     if (a.npat <= 0) {
       if (threadIdx.x == 0) { iq_dev_fail(a.status, IQ_ERR_NOPATTERN); a.rind[b] = -1; }
       return;
     }
-    const bool allzero = mm[1] == 0u;
+    const bool ref0 = can_ref && ref_on(tk.x0);
+    Ref f0;
+    if (ref0) f0 = make_ref(tk.x0, r, a.dx, a.dxy);
+    const bool allzero = ref0 ? all_zero_refined(f0, D, P, mm[1]) : mm[1] == 0u;
     const int64_t dbsize = allzero ? a.dbsize_zero : a.dbsize_norm;
     const int nseq = allzero ? a.nseq_zero : a.nseq_norm;
     RelaxPred<NAUX> pr;
     pr.D = D;
+    pr.bD = nullptr;
     pr.naux = naux;
 #pragma unroll
-    for (int j = 0; j < NAUX; ++j) { pr.aux[j] = aux[j]; pr.ka[j] = Key{0xFFFFFFFFu, 0xFFFFFFFFu}; }
+    for (int j = 0; j < NAUX; ++j) {
+      pr.aux[j] = aux[j];
+      pr.ka[j] = Key{0xFFFFFFFFu, 0xFFFFFFFFu};
+      pr.ba[j] = nullptr;
+    }
+    // band lists of the refined selections live in `prod` (2P int32 entries), free until the
+    // tau model
+    int32_t* blist = reinterpret_cast<int32_t*>(prod);
+    int64_t boff = 0;
+    long long tiesD = -1;        // near-ties at D's boundary (refined), -1: count on the map
+    long long tiesA[NAUX > 0 ? NAUX : 1];
     n = 0;
     int q = 0;
     for (; q < nseq && n == 0; ++q) {
@@ -675,26 +1283,78 @@ __global__ void __launch_bounds__(PT) pick_kernel(const PickArgs a) {
           hist_select<1>(s, hist, sbuf, req, P, res);
         }
         pr.kD = res[0];
+        if (ref0 && !allzero && dbsize < P) {
+          const long long t = band_topk(s, sbuf, f0, D, P, dbsize, pr.kD, blist, ra, k0, v0, k1,
+                                        v1, sband[0]);
+          if (t >= 0) {
+            pr.bD = &sband[0];
+            boff = sband[0].n;
+            tiesD = t;
+          }
+        }
       }
+      int64_t aoff = boff;  // auxiliary bands of this round follow D's band
 #pragma unroll
       for (int j = 0; j < NAUX; ++j) {
-        if (j < j0 || j >= naux) continue;
-        if (!allzero && tk.aux_keys[j] && q < tk.nkeys) {  // shared source: key precomputed
-          const unsigned long long kk = tk.aux_keys[j][q];
-          pr.ka[j] = Key{(uint32_t)(kk >> 32), (uint32_t)kk};
-          continue;
+        if (j >= naux) continue;
+        tiesA[j] = -1;
+        pr.ba[j] = nullptr;
+        if (j >= j0) {
+          if (!allzero && tk.aux_keys[j] && q < tk.nkeys) {  // shared source: key precomputed
+            const unsigned long long kk = tk.aux_keys[j][q];
+            pr.ka[j] = Key{(uint32_t)(kk >> 32), (uint32_t)kk};
+          } else if (sz >= P) {
+            pr.ka[j] = Key{0xFFFFFFFFu, 0xFFFFFFFFu};
+          } else if (sz <= 0) {
+            pr.ka[j] = Key{0u, 0u};
+          } else {
+            req[0] = SelReq{aux[j], amm[j][0], amm[j][1], sz};
+            hist_select<1>(s, hist, sbuf, req, P, res);
+            pr.ka[j] = res[0];
+          }
         }
-        if (sz >= P) { pr.ka[j] = Key{0xFFFFFFFFu, 0xFFFFFFFFu}; continue; }
-        if (sz <= 0) { pr.ka[j] = Key{0u, 0u}; continue; }
-        req[0] = SelReq{aux[j], amm[j][0], amm[j][1], sz};
-        hist_select<1>(s, hist, sbuf, req, P, res);
-        pr.ka[j] = res[0];
+        if (can_ref && ref_on(tk.xa[j]) && sz > 0 && sz < P) {
+          if (aoff + P > 2 * P) {  // no room for another band: the result would not be exact
+            if (threadIdx.x == 0) iq_dev_fail(a.status, IQ_ERR_LIMIT);
+            continue;
+          }
+          const Ref fa = make_ref(tk.xa[j], r, a.dx, a.dxy);
+          const long long t = band_topk(s, sbuf, fa, aux[j], P, sz, pr.ka[j], blist + aoff, ra,
+                                        k0, v0, k1, v1, sband[1 + j]);
+          if (t >= 0) {
+            pr.ba[j] = &sband[1 + j];
+            aoff += sband[1 + j].n;
+            tiesA[j] = t;
+          }
+        }
       }
       // the compaction counts: an empty intersection moves on to the next softdbsize
       n = compact(s, pr, P, cand);
     }
     if (a.stats && threadIdx.x == 0) atomicAdd(a.stats + ST_PICK_ITERS, (unsigned long long)q);
+    // near-ties at D's boundary and at each auxiliary boundary of the final round; exact maps
+    // are counted on the map (the boundary position itself excluded)
+    if (a.ties) {
+      if (tiesD >= 0) {
+        ties += (unsigned long long)tiesD;
+      } else if (!allzero && dbsize < P) {
+        const unsigned long long c = count_near(s, D, P, (double)__uint_as_float(pr.kD.v));
+        ties += c > 0 ? c - 1 : 0;
+      }
+      const int64_t szf = q > 0 ? (allzero ? a.seq_zero[q - 1] : a.seq_norm[q - 1]) : 0;
+#pragma unroll
+      for (int j = 0; j < NAUX; ++j) {
+        if (j >= naux || !(szf > 0 && szf < P)) continue;
+        if (tiesA[j] >= 0) {
+          ties += (unsigned long long)tiesA[j];
+        } else {
+          const unsigned long long c = count_near(s, aux[j], P, (double)__uint_as_float(pr.ka[j].v));
+          ties += c > 0 ? c - 1 : 0;
+        }
+      }
+    }
   }
+  if (a.ties && threadIdx.x == 0 && ties) atomicAdd(a.ties, ties);
   if (n <= 0) {
     if (threadIdx.x == 0) { iq_dev_fail(a.status, IQ_ERR_NOPATTERN); a.rind[b] = -1; }
     return;
@@ -719,8 +1379,15 @@ __global__ void __launch_bounds__(PT) pick_kernel(const PickArgs a) {
 #pragma unroll 1
   for (int j = 0; j <= naux; ++j) {
     const float* src = j == 0 ? D : aux[j > 0 ? j - 1 : 0];
+    const ExactSrc& xs = j == 0 ? tk.x0 : tk.xa[j > 0 ? j - 1 : 0];
     __syncthreads();
-    const unsigned long long S = dense_ranks(s, sbuf, src, cand, n, k0, v0, k1, v1, rankbuf);
+    unsigned long long S;
+    if (can_ref && ref_on(xs)) {
+      const Ref f = make_ref(xs, r, a.dx, a.dxy);
+      S = dense_ranks_refined(s, sbuf, f, cand, n, ra, j == 0 && have0, k0, v0, k1, v1, rankbuf);
+    } else {
+      S = dense_ranks(s, sbuf, src, cand, n, k0, v0, k1, v1, rankbuf);
+    }
     const double dS = (double)S;
     for (int64_t i = threadIdx.x; i < n; i += PT) {
       const double Pi = __ddiv_rn((double)(n - (int64_t)rankbuf[i] + 1), dS);
@@ -827,6 +1494,8 @@ int iq_launch_pick(iq_ctx* ctx, const PickLaunch& L) {
   for (int q = 0; q < IQ_MAX_SEQ; ++q) { a.seq_norm[q] = L.seq_norm[q]; a.seq_zero[q] = L.seq_zero[q]; }
   a.cand = L.cand; a.k0 = L.k0; a.v0 = L.v0; a.k1 = L.k1; a.v1 = L.v1;
   a.w = L.w; a.prod = L.prod; a.rind = L.rind; a.ncand = L.ncand; a.status = L.status;
+  a.rv = L.rv; a.rr = L.rr; a.rl = L.rl; a.dx = L.dx; a.dxy = L.dxy;
+  a.ties = L.ties;
   a.stats = L.stats;
   const int naux = L.tasks ? L.naux_max : L.t0.naux;
   const int nblocks = L.ntask * L.nreal;

@@ -441,6 +441,29 @@ extern "C" int iq_simulate(iq_ctx* ctx, const iq_sim_params* p, const iq_hard_da
         }
   }
   const bool tc = ctx->corr_engine >= 1;
+  // ---- exact re-rank: error coefficients of the maps (iq_map_kappa) ----
+  // The simulation grid holds TI values, hard data and zeros only. The overlap maps come from
+  // the tensor cores (FP16 halves when both ranges allow, else TF32 halves) or the SIMT kernel;
+  // the hard maps from the SIMT kernel with A2 summed directly; the soft maps like the overlap
+  // maps, from the auxiliary images (their statistics are known after the upload below).
+  IqValueStats hard_stats;
+  {
+    std::vector<float> hvf(nh);
+    for (int64_t i = 0; i < nh; ++i) hvf[i] = std::isnan(hv[i]) ? 0.f : (float)hv[i];
+    hard_stats = iq_host_stats(hvf.data(), nh);
+  }
+  IqValueStats sim_stats = ctx->ti_stats;
+  sim_stats.merge(hard_stats);
+  const int ovl_form = !tc ? 0 : (ctx->corr_engine == 2 && ctx->ti_stats.fp16_range() &&
+                                  sim_stats.fp16_range()) ? 1 : 2;
+  const int64_t tivol_all = ctx->ti.vol();
+  std::vector<double> cfg_kappa(ncfg);
+  bool need_ref = nsoft > 0;
+  for (int c = 0; c < ncfg; ++c) {
+    cfg_kappa[c] = iq_map_kappa(ctx->ti_stats, sim_stats, cfgs[c].K, ovl_form);
+    need_ref = need_ref || cfg_kappa[c] > 0.0;
+  }
+  const double ovl_eabs = iq_map_eabs(ctx->ti_stats, tivol_all);
   // hard lists of data tiles
   std::vector<int64_t> hoff(g.ntot + 1, 0);
   for (int64_t t = 0; t < g.ntot; ++t) hoff[t + 1] = hoff[t] + (int64_t)tile_hard[t].size();
@@ -465,8 +488,11 @@ extern "C" int iq_simulate(iq_ctx* ctx, const iq_sim_params* p, const iq_hard_da
     lim -= 1024;  // the cut kernel's static shared memory
     if ((int64_t)iq_cut_scratch_bytes(slabmax) > lim) cutscr_per = (int64_t)iq_cut_scratch_bytes(slabmax);
   }
-  const int64_t per_step = (int64_t)R * P * (4 + 4 + 16 + 16) + P * 4 + T * (rpad + 1) * 4 +
-                           (int64_t)R * 6 * (slabmax + cutscr_per) + 4096;
+  for (int64_t t = 0; t < g.ntot && !need_ref; ++t)
+    if (!tile_hard[t].empty())
+      need_ref = iq_map_kappa(ctx->ti_stats, hard_stats, (int64_t)tile_hard[t].size(), 0) > 0.0;
+  const int64_t per_step = (int64_t)R * P * (4 + 4 + 16 + 16 + (need_ref ? 18 : 0)) + P * 4 +
+                           T * (rpad + 1) * 4 + (int64_t)R * 6 * (slabmax + cutscr_per) + 4096;
   size_t freeb = 0, totalb = 0;
   cudaMemGetInfo(&freeb, &totalb);
   // hard-data distance maps depend on the data only: one map per data tile, all held at once
@@ -530,13 +556,16 @@ extern "C" int iq_simulate(iq_ctx* ctx, const iq_sim_params* p, const iq_hard_da
   uint32_t* d_v1 = (uint32_t*)iq_scratch(ctx, S_PICK_V1, sizeof(uint32_t) * pk);
   double* d_w = (double*)iq_scratch(ctx, S_PICK_W, sizeof(double) * pk);
   double* d_prod = (double*)iq_scratch(ctx, S_PICK_PROD, sizeof(double) * pk);
+  double* d_rv = need_ref ? (double*)iq_scratch(ctx, S_PICK_RV, sizeof(double) * pk) : nullptr;
+  double* d_rr = need_ref ? (double*)iq_scratch(ctx, S_PICK_RR, sizeof(double) * pk) : nullptr;
+  uint8_t* d_rl = need_ref ? (uint8_t*)iq_scratch(ctx, S_PICK_RL, 2 * pk) : nullptr;
   int64_t* d_rind = (int64_t*)iq_scratch(ctx, S_RIND, sizeof(int64_t) * R * cmax);
   int64_t* d_ncand = (int64_t*)iq_scratch(ctx, S_NCAND, sizeof(int64_t) * R * cmax);
   uint8_t* d_cutbuf = (uint8_t*)iq_scratch(ctx, S_CUTBUF, (size_t)R * cmax * 6 * slabmax);
   void* d_cutscr = cutscr_per ? iq_scratch(ctx, S_CUTSCR, (size_t)cutscr_per * 6 * R * cmax) : nullptr;
   if (!d_sim || (debug && !d_cut) || !d_D || !d_Dh || !d_tv || !d_b2 || !d_kl || !d_mm || !d_hk ||
       !d_hkv || !d_cand || !d_k0 || !d_v0 || !d_k1 || !d_v1 || !d_w || !d_prod || !d_rind ||
-      !d_ncand || !d_cutbuf || (cutscr_per && !d_cutscr))
+      !d_ncand || !d_cutbuf || (cutscr_per && !d_cutscr) || (need_ref && (!d_rv || !d_rr || !d_rl)))
     return IQ_ERR_ALLOC;
   float* d_tvh = d_tv + (size_t)T * std::max(rpad, 16) * cmax;  // hard templates (T x 1 each)
   // per-step scratch of group g starts at its first realization's share
@@ -550,6 +579,7 @@ extern "C" int iq_simulate(iq_ctx* ctx, const iq_sim_params* p, const iq_hard_da
   IQ_CUDA_OK(cudaMemcpyAsync(d_hk, hk.data(), sizeof(uint32_t) * hk.size(), cudaMemcpyHostToDevice, st));
   IQ_CUDA_OK(cudaMemcpyAsync(d_hkv, hkv.data(), sizeof(float) * hkv.size(), cudaMemcpyHostToDevice, st));
   IQ_CUDA_OK(cudaMemsetAsync(ctx->d_status, 0, sizeof(int), st));
+  IQ_CUDA_OK(cudaMemsetAsync(ctx->d_ties, 0, sizeof(unsigned long long), st));
   // ---- tensor-core launches: union stage lists keyed by their set of masks ----
   // Mask configuration c < ncfg is "tile minus [lo, hi)"; c == ncfg is the full tile.
   auto cfg_box = [&](int c) {
@@ -639,13 +669,6 @@ extern "C" int iq_simulate(iq_ctx* ctx, const iq_sim_params* p, const iq_hard_da
   }
   const TcStageRef soft_st = (tc && nsoft > 0 && T > 0) ? stages_for(std::vector<int>{ncfg})
                                                          : TcStageRef{0, 0, 0, 0, 0, 0};
-  // the simulation grid holds TI values, hard data and zeros only
-  IqValueStats sim_stats = ctx->ti_stats;
-  {
-    std::vector<float> hvf(nh);
-    for (int64_t i = 0; i < nh; ++i) hvf[i] = (float)hv[i];
-    sim_stats.merge(iq_host_stats(hvf.data(), nh));
-  }
   uint32_t* d_tcst = nullptr;  // stage words of every list, then their prefixes
   void* d_tcb = nullptr;        // packed templates of one launch, per group
   size_t tcb_bytes = 0;
@@ -702,6 +725,9 @@ extern "C" int iq_simulate(iq_ctx* ctx, const iq_sim_params* p, const iq_hard_da
   // ---- soft data: padded aux grids, auxTI integral images, per-tile distance maps ----
   std::vector<float*> d_aux(nsoft), d_auxti(nsoft);
   std::vector<double*> d_auxii(nsoft);
+  std::vector<Dim3> aux_dims(nsoft);
+  std::vector<double> soft_kappa(nsoft, 0.0), soft_eabs(nsoft, 0.0);
+  double* d_softb2 = nullptr;  // sum of squared soft template values, per (variable, tile slot)
   float* d_soft = nullptr;
   unsigned* d_softmm = nullptr;  // [min, max finite] bits of each soft map
   std::vector<int64_t> slot_of(g.ntot, -1);
@@ -722,7 +748,9 @@ extern "C" int iq_simulate(iq_ctx* ctx, const iq_sim_params* p, const iq_hard_da
     d_soft = (float*)iq_scratch(ctx, S_SOFT, sizeof(float) * P * nslot * nsoft);
     d_softmm = (unsigned*)iq_scratch(ctx, S_SOFTMM, sizeof(unsigned) * 2 * nslot * nsoft);
     int64_t* d_starts = (int64_t*)iq_scratch(ctx, S_STARTS, sizeof(int64_t) * (nslot + 16));
-    if (!a_aux || !a_ti || !a_ii || !a_raw || !d_soft || !d_softmm || !d_starts) return IQ_ERR_ALLOC;
+    d_softb2 = (double*)iq_scratch(ctx, S_SOFTB2, sizeof(double) * (nslot * nsoft + 16));
+    if (!a_aux || !a_ti || !a_ii || !a_raw || !d_soft || !d_softmm || !d_starts || !d_softb2)
+      return IQ_ERR_ALLOC;
     std::vector<int64_t> tl;
     for (int64_t t = 0; t < g.ntot; ++t)
       if (!skipped[t]) tl.push_back(t);
@@ -731,6 +759,7 @@ extern "C" int iq_simulate(iq_ctx* ctx, const iq_sim_params* p, const iq_hard_da
       for (int d = 0; d < N; ++d) ae[d] = soft[s].auxsize[d];
       const Dim3 asz{ae[0], ae[1], ae[2]};
       const Dim3 psz{std::max(ae[0], g.pad[0]), std::max(ae[1], g.pad[1]), std::max(ae[2], g.pad[2])};
+      aux_dims[s] = psz;
       d_aux[s] = a_aux + auxvol * s;
       d_auxti[s] = a_ti + tivol * s;
       d_auxii[s] = a_ii + iivol * s;
@@ -750,6 +779,15 @@ extern "C" int iq_simulate(iq_ctx* ctx, const iq_sim_params* p, const iq_hard_da
       }
       IQ_CUDA_OK(cudaMemcpyAsync(d_starts, starts.data(), sizeof(int64_t) * starts.size(),
                                  cudaMemcpyHostToDevice, st));
+      IqValueStats aux_stats, auxti_stats;
+      RET_IF(iq_value_stats(ctx, d_aux[s], psz.vol(), aux_stats));
+      RET_IF(iq_value_stats(ctx, d_auxti[s], tivol, auxti_stats));
+      {
+        const int form = !(tc && T > 0) ? 0 : (ctx->corr_engine == 2 && auxti_stats.fp16_range() &&
+                                                aux_stats.fp16_range()) ? 1 : 2;
+        soft_kappa[s] = iq_map_kappa(auxti_stats, aux_stats, T, form);
+        soft_eabs[s] = iq_map_eabs(auxti_stats, tivol);
+      }
       if (tc && T > 0) {
         // per-tile soft distance maps on the tensor cores, up to 256 tiles per launch
         std::vector<TcCol> cols;
@@ -760,15 +798,13 @@ extern "C" int iq_simulate(iq_ctx* ctx, const iq_sim_params* p, const iq_hard_da
           for (int i = 0; i < launches.back().second; ++i) {
             if (i < nb) {
               const int64_t slot = (int64_t)s * nslot + slot_of[tl[b0 + i]];
-              cols.push_back(TcCol{starts[b0 + i], d_soft + slot * P, d_tcb2 + i, d_softmm + 2 * slot, 0, 0});
+              cols.push_back(TcCol{starts[b0 + i], d_soft + slot * P, d_softb2 + slot,
+                                   d_softmm + 2 * slot, 0, 0});
             } else {
               cols.push_back(TcCol{-1, nullptr, nullptr, nullptr, 0, 0});
             }
           }
         }
-        IqValueStats aux_stats, auxti_stats;
-        RET_IF(iq_value_stats(ctx, d_aux[s], psz.vol(), aux_stats));
-        RET_IF(iq_value_stats(ctx, d_auxti[s], tivol, auxti_stats));
         TcCol* d_cols = (TcCol*)iq_scratch(ctx, S_TCSOFT, sizeof(TcCol) * cols.size());
         if (!d_cols) return IQ_ERR_ALLOC;
         IQ_CUDA_OK(cudaMemcpyAsync(d_cols, cols.data(), sizeof(TcCol) * cols.size(),
@@ -780,8 +816,8 @@ extern "C" int iq_simulate(iq_ctx* ctx, const iq_sim_params* p, const iq_hard_da
           GatherLaunch G;
           G.grid = d_aux[s]; G.grid_dims = psz; G.grid_stride = 0; G.starts = d_starts + b0;
           G.ntmpl = nb; G.rpad = nb;
-          G.t0 = GatherTask{d_kl + (size_t)ncfg * T, (int)T, 0, nullptr, nullptr, d_tcb2,
-                            d_softmm + 2 * slot0};
+          G.t0 = GatherTask{d_kl + (size_t)ncfg * T, (int)T, 0, nullptr, nullptr,
+                            d_softb2 + slot0, d_softmm + 2 * slot0};
           RET_IF(iq_launch_gather(ctx, G));
           RET_IF(tc_launch(std::vector<int>{ncfg}, soft_st, d_auxti[s], d_auxii[s], d_aux[s], psz,
                            d_cols + launches[l].first, launches[l].second, auxti_stats, aux_stats,
@@ -796,12 +832,14 @@ extern "C" int iq_simulate(iq_ctx* ctx, const iq_sim_params* p, const iq_hard_da
           GatherLaunch G;
           G.grid = d_aux[s]; G.grid_dims = psz; G.grid_stride = 0; G.starts = d_starts + b0;
           G.ntmpl = nb; G.rpad = 16;
-          G.t0 = GatherTask{d_kl + (size_t)ncfg * T, (int)T, 0, nullptr, d_tv, d_b2, d_softmm + 2 * slot0};
+          G.t0 = GatherTask{d_kl + (size_t)ncfg * T, (int)T, 0, nullptr, d_tv, d_softb2 + slot0,
+                            d_softmm + 2 * slot0};
           RET_IF(iq_launch_gather(ctx, G));
           CorrLaunch C;
           C.img = d_auxti[s]; C.img_dims = ctx->ti; C.out_dims = distD; C.tile = tileD;
           C.rpad = 16; C.ntmpl = nb; C.out_stride = P; C.disabled = d_dis;
-          C.t0 = CorrTask{d_kl + (size_t)ncfg * T, (int)T, d_tv, d_b2, d_auxii[s], {0, 0, 0}, {0, 0, 0},
+          C.t0 = CorrTask{d_kl + (size_t)ncfg * T, (int)T, d_tv, d_softb2 + slot0, d_auxii[s],
+                          {0, 0, 0}, {0, 0, 0},
                           d_soft + slot0 * P, d_softmm + 2 * slot0};
           RET_IF(iq_launch_corr(ctx, C));
         }
@@ -869,19 +907,54 @@ extern "C" int iq_simulate(iq_ctx* ctx, const iq_sim_params* p, const iq_hard_da
         PickTask& q = pt[grp * nsteps + k];
         memset(&q, 0, sizeof(q));
         q.tile = s.tile;
+        // direct re-evaluation of the overlap map of realization r: the TI against the group's
+        // simulation grid at the tile, over the mask's offsets
+        ExactSrc xo{};
+        if (cfg_kappa[s.cfg] > 0.0) {
+          xo.img = ctx->d_ti; xo.isx = ctx->ti.x; xo.isxy = ctx->ti.x * ctx->ti.y;
+          xo.klist = d_kl + (size_t)s.cfg * T; xo.K = m.K;
+          xo.tmpl = d_sim + (size_t)r0 * padvol + s.startlin; xo.tgx = padD.x;
+          xo.tgxy = padD.x * padD.y; xo.tmpl_rs = padvol;
+          xo.b2 = b2 + r0; xo.b2_rs = 1;
+          xo.kappa = cfg_kappa[s.cfg]; xo.eabs = ovl_eabs;
+        }
         int na = 0;
         if (s.hardtile) {
           q.D0 = Dh; q.D0_rs = 0; q.mm0 = mmh; q.mm0_rs = 0;
+          const int64_t h0 = hoff[s.tile], hn = hoff[s.tile + 1] - hoff[s.tile];
+          const double hk_kappa = iq_map_kappa(ctx->ti_stats, hard_stats, hn, 0);
+          if (hk_kappa > 0.0) {
+            ExactSrc& xh = q.x0;
+            xh.img = ctx->d_ti; xh.isx = ctx->ti.x; xh.isxy = ctx->ti.x * ctx->ti.y;
+            xh.klist = d_hk + h0; xh.K = (int)hn; xh.kval = d_hkv + h0;
+            xh.b2 = Dh == nullptr ? nullptr : d_b2h + (hi - 1); xh.b2_rs = 0;
+            xh.kappa = hk_kappa; xh.eabs = 0.0;
+          }
           q.aux[na] = D + r0 * P; q.aux_rs[na] = P; q.aux_mm[na] = mm + 2 * r0; q.aux_mm_rs[na] = 2;
+          q.xa[na] = xo;
           ++na;
         } else {
           q.D0 = D + r0 * P; q.D0_rs = P; q.mm0 = mm + 2 * r0; q.mm0_rs = 2;
+          q.x0 = xo;
         }
         for (int sv = 0; sv < nsoft; ++sv) {
           const int64_t slot = (int64_t)sv * nslot + slot_of[s.tile];
           q.aux[na] = d_soft + slot * P; q.aux_rs[na] = 0;
           q.aux_mm[na] = d_softmm + 2 * slot; q.aux_mm_rs[na] = 0;
-          if (d_softkeys) { q.aux_keys[na] = d_softkeys + slot * nkeys; q.nkeys = nkeys; }
+          if (soft_kappa[sv] > 0.0) {
+            // the auxiliary TI against the padded auxiliary grid at the tile, full tile
+            ExactSrc& xs = q.xa[na];
+            xs.img = d_auxti[sv]; xs.isx = ctx->ti.x; xs.isxy = ctx->ti.x * ctx->ti.y;
+            xs.klist = d_kl + (size_t)ncfg * T; xs.K = (int)T;
+            const Dim3 ad = aux_dims[sv];
+            xs.tmpl = d_aux[sv] + s.start[0] + ad.x * (s.start[1] + ad.y * s.start[2]);
+            xs.tgx = ad.x; xs.tgxy = ad.x * ad.y; xs.tmpl_rs = 0;
+            xs.b2 = d_softb2 + slot; xs.b2_rs = 0;
+            xs.kappa = soft_kappa[sv]; xs.eabs = soft_eabs[sv];
+          } else if (d_softkeys) {  // exact map: its keys are shared by all realizations
+            q.aux_keys[na] = d_softkeys + slot * nkeys;
+            q.nkeys = nkeys;
+          }
           ++na;
         }
         q.naux = na;
@@ -985,6 +1058,10 @@ extern "C" int iq_simulate(iq_ctx* ctx, const iq_sim_params* p, const iq_hard_da
         const size_t po = grp_pick(grp);
         L.cand = d_cand + po; L.k0 = d_k0 + po; L.v0 = d_v0 + po; L.k1 = d_k1 + po; L.v1 = d_v1 + po;
         L.w = d_w + po; L.prod = d_prod + po;
+        L.rv = d_rv ? d_rv + po : nullptr; L.rr = d_rr ? d_rr + po : nullptr;
+        L.rl = d_rl ? d_rl + 2 * po : nullptr;
+        L.dx = distD.x; L.dxy = distD.x * distD.y;
+        L.ties = ctx->d_ties;
         L.rind = rind; L.ncand = d_ncand + grp_rind(grp); L.status = ctx->d_status;
         L.stats = ctx->prof ? ctx->d_stats : nullptr;
         RET_IF(iq_launch_pick(ctx, L));

@@ -88,6 +88,19 @@ int iq_ctx_destroy(iq_ctx* ctx);
 void* iq_ctx_stream(iq_ctx* ctx);
 
 /*
+ * Near-ties of the last iq_simulate or iq_pick call on this context: the number of
+ * (position, decision) pairs whose distance lies within 1e-6 (relative) of a decision value of
+ * a pick, |D - t| <= 1e-6 t, summed over every pick of the call. The decisions are the
+ * threshold (1 + tol) * min D (src/iqsim.jl:237; every position counts), and for the
+ * relaxation the dbsize boundary of the primary distance and each auxiliary boundary of the
+ * final round (src/relaxation.jl:11-12,22-27; the boundary position itself does not count).
+ * No counterpart in the reference. Membership at those positions is decided on the exact
+ * Float64 distance all the same; the count says how many decisions a 1e-6 change of the
+ * distances could flip.
+ */
+int iq_ties(iq_ctx* ctx, int64_t* out);
+
+/*
  * Upload the training image and keep it resident: prepare (src/utils.jl:96-102, NaN -> 0,
  * Float32 on the device like the reference's GPU path src/utils.jl:59), its NaN mask and the
  * Float64 integral image of its squares. dtype IQ_F32 or IQ_F64; NaN marks inactive voxels.

@@ -54,14 +54,14 @@ _lib = None
 
 
 def build_native(force=False):
-    """Compile oracle/bkcut.c into oracle/liboracle.so (gcc; plain C, any host)."""
-    src = os.path.join(_HERE, "bkcut.c")
+    """Compile oracle/bkcut.c and oracle/direct.c into oracle/liboracle.so (gcc; plain C)."""
+    srcs = [os.path.join(_HERE, f) for f in ("bkcut.c", "direct.c")]
     if (not force and os.path.exists(_LIBPATH)
-            and os.path.getmtime(_LIBPATH) >= os.path.getmtime(src)):
+            and all(os.path.getmtime(_LIBPATH) >= os.path.getmtime(s) for s in srcs)):
         return _LIBPATH
     tmp = _LIBPATH + ".%d.tmp" % os.getpid()
-    subprocess.check_call(["gcc", "-O2", "-ffp-contract=off", "-fPIC", "-shared", "-o", tmp, src,
-                           "-lm"])
+    subprocess.check_call(["gcc", "-O2", "-ffp-contract=off", "-fPIC", "-shared", "-o", tmp]
+                          + srcs + ["-lm", "-lpthread"])
     os.replace(tmp, _LIBPATH)
     return _LIBPATH
 
@@ -76,6 +76,10 @@ def _native():
                                         ctypes.c_int, ctypes.POINTER(ctypes.c_longlong),
                                         ctypes.c_int, ctypes.c_void_p,
                                         ctypes.POINTER(ctypes.c_double)]
+        lib.oracle_direct_ssd.restype = ctypes.c_int
+        lib.oracle_direct_ssd.argtypes = [ctypes.c_void_p] + [ctypes.c_longlong] * 3 + [
+            ctypes.c_void_p, ctypes.c_void_p] + [ctypes.c_longlong] * 3 + [ctypes.c_void_p,
+                                                                           ctypes.c_int]
         lib.oracle_capacities.restype = ctypes.c_longlong
         lib.oracle_capacities.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int,
                                           ctypes.c_int, ctypes.POINTER(ctypes.c_longlong),
@@ -356,8 +360,9 @@ def fastdistance(img, kern, weights=None, method="direct", workers=None):
     """D[p] = |sum_k w_k img[p+k]^2 - 2 sum_k w_k kern_k img[p+k] + sum_k w_k kern_k^2|.
 
     method="fft" follows src/utils.jl:5-13 literally (two FFT correlations); "direct" sums
-    w_k (img[p+k] - kern_k)^2 over the nonzero weights, which equals it for 0/1 weights and is
-    exact for integer-valued data."""
+    w_k (img[p+k] - kern_k)^2 over the nonzero weights in a fixed Float64 order (direct_ssd),
+    which equals it for 0/1 weights, is exact for integer-valued data and is the value the
+    library's exact re-rank reproduces."""
     img = np.asarray(img, np.float64)
     kern = np.asarray(kern, np.float64)
     w = np.ones(kern.shape) if weights is None else np.asarray(weights, np.float64)
@@ -367,24 +372,58 @@ def fastdistance(img, kern, weights=None, method="direct", workers=None):
         AB = imfilter_valid(img, wk, workers)
         B2 = float(np.sum(wk * kern))
         return np.abs(A2 - 2 * AB + B2)
+    return direct_ssd(img, kern, w, workers)
+
+
+def direct_ssd(img, kern, w, workers=None):
+    """D[p] = sum over the mask of w_k (img[p+k] - kern_k)^2 in Float64, one fixed evaluation:
+    offsets in column-major order (x fastest), each term and each partial sum a separately
+    rounded Float64 operation (oracle/direct.c). The library's exact re-rank evaluates the same
+    sequence bit for bit."""
+    img = np.asarray(img, np.float64)
+    kern = np.asarray(kern, np.float64)
+    w = np.asarray(w, np.float64)
+    N = img.ndim
+    sh = tuple(img.shape) + (1,) * (3 - N)
+    ts = tuple(kern.shape) + (1,) * (3 - N)
     out_shape = tuple(i - k + 1 for i, k in zip(img.shape, kern.shape))
-    out = np.zeros(out_shape)
-    for k in zip(*np.nonzero(w)):
-        diff = img[tuple(slice(o, o + s) for o, s in zip(k, out_shape))] - kern[k]
-        if w[k] == 1:
-            out += diff * diff
-        else:
-            out += w[k] * diff * diff
-    return out
+    out3 = tuple(i - k + 1 for i, k in zip(sh, ts))
+    a = np.asfortranarray(img.reshape(sh))
+    kf = np.asfortranarray(kern.reshape(ts))
+    wf = np.asfortranarray(w.reshape(ts))
+    out = np.zeros(out3, np.float64, order="F")
+    nt = workers if workers and workers > 0 else (os.cpu_count() or 1)
+    rc = _native().oracle_direct_ssd(a.ctypes.data, sh[0], sh[1], sh[2], kf.ctypes.data,
+                                     wf.ctypes.data, ts[0], ts[1], ts[2], out.ctypes.data, nt)
+    if rc != 0:
+        raise RuntimeError("oracle direct distance failed")
+    return np.ascontiguousarray(out.reshape(out_shape, order="F"))
 
 
 # --------------------------------------------------------------------------------------
 # candidate pick (src/iqsim.jl:237), relaxation, taumodel, draw
 # --------------------------------------------------------------------------------------
-def threshold_pick(D, tol):
-    """findall(vec(D .<= (1 + tol) * minimum(D))) (src/iqsim.jl:237)."""
+TIE_RTOL = 1e-6
+
+
+def count_ties(d, t, boundary_is_member):
+    """Near-ties of one decision: enabled positions whose distance lies within 1e-6 (relative)
+    of the decision value t, |d - t| <= 1e-6 * t, evaluated in Float64. For a top-k boundary
+    (t = the k-th smallest value) the k-th position itself is not counted. None when t is 0,
+    Inf or NaN (no relative window)."""
+    if not (np.isfinite(t) and t > 0):
+        return 0
+    n = int(np.count_nonzero(np.abs(d - t) <= TIE_RTOL * t))
+    return n - 1 if boundary_is_member else n
+
+
+def threshold_pick(D, tol, ties=None):
+    """findall(vec(D .<= (1 + tol) * minimum(D))) (src/iqsim.jl:237). `ties` (a list) receives
+    the number of positions within 1e-6 of the threshold."""
     d = np.asarray(D).ravel(order="F")
     thr = (1 + tol) * float(d.min())
+    if ties is not None:
+        ties.append(count_ties(d, thr, False))
     return np.flatnonzero(d <= thr)
 
 
@@ -396,11 +435,12 @@ def _fastintersect(A, B, nbits):
     return np.flatnonzero(bits & bitsB)
 
 
-def relaxation(distance, auxdistances, cutoff):
+def relaxation(distance, auxdistances, cutoff, ties=None):
     """Candidate database under auxiliary data (src/relaxation.jl:5-39).
 
     partialsortperm(v, 1:k) selects the k smallest by (value, index); a stable argsort gives
-    the same set."""
+    the same set. `ties` (a list) receives the near-ties (count_ties) at the dbsize boundary of
+    the primary distance plus those at each auxiliary boundary of the final round."""
     d = np.asarray(distance, np.float64).ravel(order="F")
     enabled = ~np.isinf(d)
     npat = int(enabled.sum())
@@ -427,6 +467,17 @@ def relaxation(distance, auxdistances, cutoff):
         if len(patterndb):
             break
         frac = min(frac + 0.1, 1.0)
+    if ties is not None:
+        # boundaries of proper top-k selections only (0 < k < number of positions)
+        nt = 0
+        if dbsize < len(d):
+            nt += count_ties(d, d[np.argsort(d, kind="stable")[dbsize - 1]], True)
+        for n in range(naux):
+            a = np.asarray(auxdistances[n], np.float64).ravel(order="F")
+            k = len(softdb[n])
+            if 0 < k < len(a):
+                nt += count_ties(a, a[np.argsort(a, kind="stable")[k - 1]], True)
+        ties.append(nt)
     return patterndb
 
 
@@ -500,12 +551,13 @@ def sample_index(u, w):
     return lo + (int(hits[0]) if len(hits) else min(DRAW_CHUNK, n - lo) - 1)
 
 
-def pick(D, Ds, tol, seed, tile, real):
-    """Candidate set, weights and the drawn linear index for one tile of one realization."""
+def pick(D, Ds, tol, seed, tile, real, ties=None):
+    """Candidate set, weights and the drawn linear index for one tile of one realization.
+    `ties` (a list) receives the pick's near-tie count."""
     if len(Ds) == 0:
-        cands = threshold_pick(D, tol)
+        cands = threshold_pick(D, tol, ties)
     else:
-        cands = relaxation(D, Ds, tol)
+        cands = relaxation(D, Ds, tol, ties)
     w = taumodel(cands, D, Ds)
     u = philox.draw_uniform(seed, tile, real)
     i = sample_index(u, w)
@@ -574,14 +626,15 @@ def cut_cost(A, B, mask):
 # --------------------------------------------------------------------------------------
 def iqsim(trainimg, tilesize, simsize=None, overlap=None, soft=(), hard=None, tol=0.1,
           path="raster", nreal=1, debug=False, seed=0, method="direct", workers=None,
-          trace=None, max_steps=None, real0=0):
+          trace=None, max_steps=None, real0=0, ties=None):
     """Image quilting simulation, the reference's loop in Float64.
 
     `seed` keys the Philox streams (path and draws). `method` picks the distance form
     ("direct" exact SSD or "fft" as the reference). `trace`, when a list, receives one tuple
     (real, tile, rind, ncand) per simulated tile. `max_steps` stops each realization after
     that many tiles (used to time a bounded sample). `real0` is the global index of the first
-    realization (its Philox draws use counter (tile, real0 + r))."""
+    realization (its Philox draws use counter (tile, real0 + r)). `ties`, when a list, receives
+    the near-tie count of every pick (count_ties)."""
     tisize = tuple(np.shape(trainimg))
     N = len(tisize)
     tilesize = tuple(int(t) for t in tilesize)
@@ -653,7 +706,7 @@ def iqsim(trainimg, tilesize, simsize=None, overlap=None, soft=(), hard=None, to
             else:
                 D, Ds = ovldist, softdists
 
-            rind, cands, _ = pick(D, Ds, tol, seed, ind, real0 + real)
+            rind, cands, _ = pick(D, Ds, tol, seed, ind, real0 + real, ties)
             if trace is not None:
                 trace.append((real, ind, rind, len(cands)))
             rstart = lin2cart(geo.distsize, rind)

@@ -370,3 +370,34 @@ def test_properties_hold_on_oracle_output():
     bad[1][5, 5, 5] = -1.0
     with pytest.raises(AssertionError):
         check_realizations(bad, ti, hard)
+
+
+# ---- the Float64 evaluation the exact re-rank reproduces (oracle/direct.c) ----------------
+def test_direct_distance_is_the_sequential_column_major_sum():
+    rng = np.random.default_rng(71)
+    img = np.exp(rng.normal(size=(14, 12, 9))).astype(np.float32)
+    k = np.exp(rng.normal(size=(5, 4, 3))).astype(np.float32)
+    w = rng.random((5, 4, 3)) < 0.6
+    got = O.fastdistance(img, k, w, "direct")
+    out_shape = tuple(i - t + 1 for i, t in zip(img.shape, k.shape))
+    ref = np.zeros(out_shape)
+    I, K = img.astype(np.float64), k.astype(np.float64)
+    for lin in np.flatnonzero(w.ravel(order="F")):
+        kk = np.unravel_index(lin, w.shape, order="F")
+        d = I[tuple(slice(o, o + s) for o, s in zip(kk, out_shape))] - K[kk]
+        ref = ref + d * d
+    assert np.array_equal(got, ref)
+    # 1-D and 2-D go through the same 3-D routine
+    a1 = rng.normal(size=40)
+    assert np.allclose(O.fastdistance(a1, a1[:7], None, "direct"),
+                       O.fastdistance(a1, a1[:7], None, "fft"), atol=1e-9)
+
+
+def test_count_ties_rules():
+    d = np.array([1.0, 2.0, 2.0 * (1 + 5e-7), 2.0 * (1 - 9e-7), 2.0 * (1 + 2e-6), np.inf])
+    assert O.count_ties(d, 2.0, False) == 3
+    assert O.count_ties(d, 2.0, True) == 2  # the boundary position itself is not counted
+    assert O.count_ties(d, 0.0, False) == 0 and O.count_ties(d, np.inf, True) == 0
+    ties = []
+    O.threshold_pick(np.array([1.0, 1.1, 1.1 * (1 + 1e-7), 3.0]), 0.1, ties)
+    assert ties == [2]
