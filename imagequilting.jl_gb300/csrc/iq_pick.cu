@@ -928,6 +928,13 @@ __device__ __noinline__ unsigned long long ref_count_ties(Smem& s, const Ref& f,
     bool tex;
     if (b >= 0) { tv = a.v[b]; tr = a.r[b]; tex = ref_exact(a, (uint32_t)b); }
     else { tv = tfix; tr = 0.0; tex = true; }
+    if (tex && !(tv > 0.0 && tv < 1e300)) return 0;  // no relative window around 0 or Inf
+    if (!tex && tv - tr <= 0.0) {  // the decision value may be 0: make it exact first
+      if (threadIdx.x == 0) ref_mark(a, (uint32_t)b);
+      __syncthreads();
+      ref_raise(f, pos, n, a, true);
+      continue;
+    }
     unsigned long long cnt = 0;
     int und = 0;
     for (int64_t i = threadIdx.x; i < n; i += PT) {
