@@ -428,6 +428,33 @@ int iq_launch_pad_symmetric(iq_ctx* ctx, const float* src, Dim3 src_dims, float*
 int iq_launch_prepare(iq_ctx* ctx, float* data, int64_t n, uint8_t* nanmask);
 int iq_launch_to_f32(iq_ctx* ctx, const double* src, float* dst, int64_t n);
 
+// ---------------------------------------------------------------------------------------
+// Learned proposal (iq_proposal.cu)
+// ---------------------------------------------------------------------------------------
+#define IQ_LP_CH 32      // channels of the encoder's convolutions
+#define IQ_LP_EMB 64     // embedding width
+#define IQ_LP_MAXG 256   // cells of the input grid (8 x 8 x 4)
+#define IQ_LP_MAXG2 32   // after the first stride-2 convolution (4 x 4 x 2)
+#define IQ_LP_MAXG3 4    // after the second (2 x 2 x 1)
+// parameter offsets (floats): w1 [32][3], b1, w2 [32][32][27], b2, w3 [32][32][27], b3,
+// w4 [64][nf], b4 (nf = 32 x cells of layer 3, channel fastest)
+#define LP_OFF_W1 0
+#define LP_OFF_B1 (LP_OFF_W1 + IQ_LP_CH * 3)
+#define LP_OFF_W2 (LP_OFF_B1 + IQ_LP_CH)
+#define LP_OFF_B2 (LP_OFF_W2 + IQ_LP_CH * IQ_LP_CH * 27)
+#define LP_OFF_W3 (LP_OFF_B2 + IQ_LP_CH)
+#define LP_OFF_B3 (LP_OFF_W3 + IQ_LP_CH * IQ_LP_CH * 27)
+#define LP_OFF_W4 (LP_OFF_B3 + IQ_LP_CH)
+
+struct LpGeo {
+  int t[3];        // tile
+  int g[3], c[3];  // cell grid and cell size
+  int g2[3], g3[3];
+  int ng, ng2, ng3, nf;
+  int off_b4, npar;
+};
+LpGeo iq_lp_geo(Dim3 tile);
+
 // relaxation sizes of src/relaxation.jl:11-36 for a given npatterns (iq_sim.cu)
 void iq_relax_sizes(int64_t npat, double tol, int64_t& dbnorm, int64_t& dbzero, int& nnorm,
                     int64_t* seqnorm, int& nzero, int64_t* seqzero);

@@ -727,17 +727,72 @@ __device__ __forceinline__ void df_add(float& h, float& l, float x, float y) {
   l = __fsub_rn(e, __fsub_rn(h, s));
 }
 
-// Warp-collective: value and radius of D[p] at `level` (every lane gets the same result).
-__device__ __noinline__ void ref_eval(const Ref& f, int64_t p, int level, double& v, double& r) {
+// The terms of one map, staged in the CTA's dynamic shared memory for a batch of evaluations:
+// off[j] = image offset of mask offset j from the window origin, tv[j] = its template value.
+// (The region is free whenever entries are evaluated: histograms and sorts use it in between.)
+constexpr int REF_CACHE = (2 * NBIN * 4 + SORT_CAP * 8) / 8;  // terms that fit: 12288
+
+struct RefCache {
+  const int32_t* off;
+  const float* tv;
+  bool on;
+};
+
+__device__ RefCache ref_cache_load(const Ref& f) {
+  extern __shared__ __align__(16) unsigned char dyn[];
+  int32_t* off = reinterpret_cast<int32_t*>(dyn);
+  float* tv = reinterpret_cast<float*>(dyn + 4 * REF_CACHE);
+  const bool on = f.K <= REF_CACHE && f.isxy * 1024 < ((int64_t)1 << 31);
+  __syncthreads();  // earlier users of the region are done
+  if (on) {
+    for (int j = threadIdx.x; j < f.K; j += PT) {
+      const uint32_t k = __ldg(f.kl + j);
+      const int kx = kx_of(k), ky = ky_of(k), kz = kz_of(k);
+      off[j] = (int32_t)(kx + f.isx * ky + f.isxy * kz);
+      tv[j] = f.kv ? __ldg(f.kv + j) : __ldg(f.tm + kx + f.tgx * ky + f.tgxy * kz);
+    }
+  }
+  __syncthreads();
+  return RefCache{off, tv, on};
+}
+
+__device__ __forceinline__ void ref_term_c(const Ref& f, const RefCache& c, int64_t base, int j,
+                                           float& a, float& b) {
+  if (c.on) {
+    a = __ldg(f.img + base + c.off[j]);
+    b = c.tv[j];
+  } else {
+    ref_term(f, base, j, a, b);
+  }
+}
+
+// Warp-collective: value and radius of D[p] at `level` (every lane gets the same result). Each
+// lane keeps four loads in flight (the image is L2-resident; the loop is bound by its latency).
+__device__ __noinline__ void ref_eval(const Ref& f, const RefCache& c, int64_t p, int level,
+                                      double& v, double& r) {
   const int lane = threadIdx.x & 31;
   const int64_t base = ref_base(f, p);
   const int nl = (f.K + 31) / 32;
   const double tail = (double)(f.K + 2) * RU64 * 1.02;   // level 3 vs the exact sum
   if (level <= 1) {
     float acc = 0.f;
-    for (int j = lane; j < f.K; j += 32) {
+    int j = lane;
+    for (; j + 96 < f.K; j += 128) {
+      float a0, b0, a1, b1, a2, b2, a3, b3;
+      ref_term_c(f, c, base, j, a0, b0);
+      ref_term_c(f, c, base, j + 32, a1, b1);
+      ref_term_c(f, c, base, j + 64, a2, b2);
+      ref_term_c(f, c, base, j + 96, a3, b3);
+      const float d0 = __fsub_rn(a0, b0), d1 = __fsub_rn(a1, b1);
+      const float d2 = __fsub_rn(a2, b2), d3 = __fsub_rn(a3, b3);
+      acc = __fmaf_rn(d0, d0, acc);
+      acc = __fmaf_rn(d1, d1, acc);
+      acc = __fmaf_rn(d2, d2, acc);
+      acc = __fmaf_rn(d3, d3, acc);
+    }
+    for (; j < f.K; j += 32) {
       float a, b;
-      ref_term(f, base, j, a, b);
+      ref_term_c(f, c, base, j, a, b);
       const float d = __fsub_rn(a, b);
       acc = __fmaf_rn(d, d, acc);
     }
@@ -747,15 +802,23 @@ __device__ __noinline__ void ref_eval(const Ref& f, int64_t p, int level, double
     r = v * ((double)(nl + 8) * RU32 * 1.02 + tail) + (double)(f.K + 8) * TINY32 * 4.0;
   } else if (level == 2) {
     float h = 0.f, l = 0.f;
-    for (int j = lane; j < f.K; j += 32) {
-      float a, b;
-      ref_term(f, base, j, a, b);
-      float dh, dl;
-      two_sum(a, -b, dh, dl);                               // a - b = dh + dl exactly
-      const float p2 = __fmul_rn(dh, dh);
-      const float pe = __fmaf_rn(dh, dh, -p2);              // dh^2 = p2 + pe exactly
-      const float q = __fmaf_rn(__fadd_rn(dh, dh), dl, pe);  // + 2 dh dl (dl^2 dropped)
-      df_add(h, l, p2, q);
+    int j = lane;
+    for (; j < f.K; j += 64) {
+      float a0, b0, a1 = 0.f, b1 = 0.f;
+      ref_term_c(f, c, base, j, a0, b0);
+      const bool two = j + 32 < f.K;
+      if (two) ref_term_c(f, c, base, j + 32, a1, b1);
+#pragma unroll
+      for (int u = 0; u < 2; ++u) {
+        if (u == 1 && !two) break;
+        const float a = u ? a1 : a0, b = u ? b1 : b0;
+        float dh, dl;
+        two_sum(a, -b, dh, dl);                               // a - b = dh + dl exactly
+        const float p2 = __fmul_rn(dh, dh);
+        const float pe = __fmaf_rn(dh, dh, -p2);              // dh^2 = p2 + pe exactly
+        const float q = __fmaf_rn(__fadd_rn(dh, dh), dl, pe);  // + 2 dh dl (dl^2 dropped)
+        df_add(h, l, p2, q);
+      }
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
@@ -775,7 +838,7 @@ __device__ __noinline__ void ref_eval(const Ref& f, int64_t p, int level, double
       const int j = j0 + lane;
       if (j < f.K) {
         float a, b;
-        ref_term(f, base, j, a, b);
+        ref_term_c(f, c, base, j, a, b);
         const double d = __dsub_rn((double)a, (double)b);
         t = __dmul_rn(d, d);
       }
@@ -808,9 +871,10 @@ struct RefArr {
 // Level 1 for entries [0, n) of pos (warp per entry).
 __device__ __noinline__ void ref_init(const Ref& f, const int32_t* pos, int64_t n, RefArr a) {
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const RefCache c = ref_cache_load(f);
   for (int64_t i = warp; i < n; i += NW) {
     double v, r;
-    ref_eval(f, pos[i] & 0x7FFFFFFF, 1, v, r);
+    ref_eval(f, c, pos[i] & 0x7FFFFFFF, 1, v, r);
     if (lane == 0) { a.v[i] = v; a.r[i] = r; a.l[i] = 1; }
   }
   __syncthreads();
@@ -819,12 +883,13 @@ __device__ __noinline__ void ref_init(const Ref& f, const int32_t* pos, int64_t 
 // Raise every marked entry by one level, or to level 3 when `to3`.
 __device__ __noinline__ void ref_raise(const Ref& f, const int32_t* pos, int64_t n, RefArr a, bool to3) {
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const RefCache c = ref_cache_load(f);
   for (int64_t i = warp; i < n; i += NW) {
     const uint8_t l = a.l[i];
     if (!(l & 0x80)) continue;
     const int nl = to3 ? 3 : min((l & 0x7F) + 1, 3);
     double v, r;
-    ref_eval(f, pos[i] & 0x7FFFFFFF, nl, v, r);
+    ref_eval(f, c, pos[i] & 0x7FFFFFFF, nl, v, r);
     if (lane == 0) { a.v[i] = v; a.r[i] = r; a.l[i] = (uint8_t)nl; }
   }
   __syncthreads();
@@ -950,6 +1015,46 @@ __device__ __noinline__ unsigned long long ref_count_ties(Smem& s, const Ref& f,
   return 0;  // not reached: level-3 tests always decide
 }
 
+__device__ double block_min_f64(Smem& s, double v) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = fmin(v, __shfl_xor_sync(0xffffffffu, v, o));
+  double* red = reinterpret_cast<double*>(s.wred);
+  if (lane == 0) red[wid] = v;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double m = red[0];
+    for (int i = 1; i < NW; ++i) m = fmin(m, red[i]);
+    red[0] = m;
+  }
+  __syncthreads();
+  const double m = red[0];
+  __syncthreads();
+  return m;
+}
+
+__device__ double block_max_f64(Smem& s, double v) { return -block_min_f64(s, -v); }
+
+__device__ unsigned long long block_max_u64(Smem& s, unsigned long long v) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const unsigned long long w = __shfl_xor_sync(0xffffffffu, v, o);
+    v = v > w ? v : w;
+  }
+  if (lane == 0) s.wred[wid] = v;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    unsigned long long m = s.wred[0];
+    for (int i = 1; i < NW; ++i) m = m > s.wred[i] ? m : s.wred[i];
+    s.wred[0] = m;
+  }
+  __syncthreads();
+  const unsigned long long m = s.wred[0];
+  __syncthreads();
+  return m;
+}
+
 // Ordered compaction of the positions of `src` with lo <= D <= hi into out; `below` receives
 // the count of positions with D < lo (Inf and NaN are neither).
 __device__ __noinline__ int64_t band_collect(Smem& s, const float* __restrict__ src, int64_t P, double lo,
@@ -1005,10 +1110,77 @@ __device__ __noinline__ long long band_topk(Smem& s, unsigned long long* sbuf, c
   if (kk < 1 || kk > b.n) { b.n = 0; return -1; }
   ref_init(f, list, b.n, a);
   uint32_t* ord = const_cast<uint32_t*>(ref_sort(s, sbuf, b.n, a, k0, v0, k1, v1));
-  ref_resolve(s, f, list, b.n, ord, a);
+  // The set is the first kk entries of the order once every entry on the left lies below every
+  // entry on the right: raise only the entries that may cross the split, else (equal values
+  // across it) put the whole band in exact (value, position) order.
+  bool split = false;
+  for (int round = 0; round < 4; ++round) {
+    double mh = -1e308, ml = 1e308;
+    for (int64_t t = threadIdx.x; t < b.n; t += PT) {
+      const uint32_t i = ord[t];
+      if (t < kk) mh = fmax(mh, a.v[i] + a.r[i]);
+      else ml = fmin(ml, a.v[i] - a.r[i]);
+    }
+    mh = block_max_f64(s, mh);
+    ml = block_min_f64(s, ml);
+    if (mh < ml) { split = true; break; }
+    int any = 0;
+    for (int64_t t = threadIdx.x; t < b.n; t += PT) {
+      const uint32_t i = ord[t];
+      const bool cross = t < kk ? a.v[i] + a.r[i] >= ml : a.v[i] - a.r[i] <= mh;
+      if (cross && !ref_exact(a, i)) { ref_mark(a, i); any = 1; }
+    }
+    if (!__syncthreads_or(any)) break;
+    ref_raise(f, list, b.n, a, round >= 1);
+    ord = const_cast<uint32_t*>(ref_sort(s, sbuf, b.n, a, k0, v0, k1, v1));
+  }
+  if (!split) ref_resolve(s, f, list, b.n, ord, a);
   for (int64_t t = threadIdx.x; t < kk; t += PT) list[ord[t]] |= (int32_t)0x80000000;
   __syncthreads();
-  const int64_t bi = ord[kk - 1];
+  // the boundary: the largest (value, position) of the set
+  int64_t bi = split ? -1 : (int64_t)ord[kk - 1];
+  for (int round = 0; bi < 0 && round < 8; ++round) {
+    double mlo = -1e308;
+    for (int64_t t = threadIdx.x; t < kk; t += PT) mlo = fmax(mlo, a.v[ord[t]] - a.r[ord[t]]);
+    mlo = block_max_f64(s, mlo);
+    unsigned long long cnt = 0, inexact = 0, best = 0;
+    for (int64_t t = threadIdx.x; t < kk; t += PT) {
+      const uint32_t i = ord[t];
+      if (a.v[i] + a.r[i] >= mlo) {
+        cnt++;
+        if (!ref_exact(a, i)) inexact++;
+      }
+    }
+    cnt = block_sum_u64(s, cnt);
+    inexact = block_sum_u64(s, inexact);
+    if (cnt == 1 || inexact == 0) {
+      // unique candidate, or exact values: the largest (value, position)
+      double vmax = -1e308;
+      for (int64_t t = threadIdx.x; t < kk; t += PT) {
+        const uint32_t i = ord[t];
+        if (a.v[i] + a.r[i] >= mlo) vmax = fmax(vmax, a.v[i]);
+      }
+      vmax = block_max_f64(s, vmax);
+      for (int64_t t = threadIdx.x; t < kk; t += PT) {
+        const uint32_t i = ord[t];
+        if (a.v[i] + a.r[i] >= mlo && (cnt == 1 || a.v[i] == vmax)) {
+          const unsigned long long key =
+              ((unsigned long long)(uint32_t)(list[i] & 0x7FFFFFFF) << 32) | i;
+          best = best > key ? best : key;
+        }
+      }
+      best = block_max_u64(s, best);
+      bi = (int64_t)(uint32_t)best;
+      break;
+    }
+    for (int64_t t = threadIdx.x; t < kk; t += PT) {
+      const uint32_t i = ord[t];
+      if (a.v[i] + a.r[i] >= mlo && !ref_exact(a, i)) ref_mark(a, i);
+    }
+    __syncthreads();
+    ref_raise(f, list, b.n, a, round >= 1);
+  }
+  if (bi < 0) bi = ord[kk - 1];  // not reached: level-3 values decide within 3 rounds
   __syncthreads();
   return (long long)ref_count_ties(s, f, list, b.n, a, bi, true, 0.0);
 }
@@ -1087,24 +1259,6 @@ __device__ __noinline__ int64_t ref_filter(Smem& s, int32_t* pos, int64_t n, Ref
     __syncthreads();
   }
   return base;
-}
-
-__device__ double block_min_f64(Smem& s, double v) {
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) v = fmin(v, __shfl_xor_sync(0xffffffffu, v, o));
-  double* red = reinterpret_cast<double*>(s.wred);
-  if (lane == 0) red[wid] = v;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    double m = red[0];
-    for (int i = 1; i < NW; ++i) m = fmin(m, red[i]);
-    red[0] = m;
-  }
-  __syncthreads();
-  const double m = red[0];
-  __syncthreads();
-  return m;
 }
 
 // Threshold pick of a refined map (src/iqsim.jl:237): the candidates D <= (1 + tol) min D of the
