@@ -112,6 +112,7 @@ enum IqSlot {
   S_CUTBUF, S_CUTSCR, S_DIS, S_AUX, S_AUXTI, S_AUXII, S_HARDLIST, S_HARDPTS, S_OUT,
   S_TMP0, S_TMP1, S_TMP2, S_STARTS, S_SOFTMM, S_TASKS, S_VOX, S_TCB, S_TCCOLS, S_TCSTAGE, S_TCB2, S_TCFLAG, S_TCSOFT, S_SOFTKEYS,
   S_PICK_RV, S_PICK_RR, S_PICK_RL, S_SOFTB2,
+  S_PB_RV, S_PB_RR, S_PB_RL, S_PB_LIST, S_PB_K, S_PB_OUT, S_PB_POOL, S_PB_SRC,
   S_COUNT
 };
 
@@ -294,6 +295,18 @@ struct ExactSrc {
   double kappa, eabs;
 };
 
+// Refined top-k selection of a map shared by all realizations of a tile (a soft-data map),
+// computed once per (map, relaxation step): positions with D < lo are in, D > hi out, and the
+// positions in between are listed at pool + off (ascending, bit 31 set when in).
+struct PreBand {
+  double lo, hi;
+  int64_t off, n;
+  unsigned long long key;   // the FP32 (value, index) key of the selection
+  long long ties;           // near-ties at its boundary (the boundary position excluded)
+  int32_t ok;               // 0: not precomputed (the pick selects itself)
+  int32_t pad_;
+};
+
 // Sources of one tile; realization r of the tile reads D0 + r * D0_rs etc.
 struct PickTask {
   const float* D0; int64_t D0_rs;           // primary distance
@@ -306,6 +319,8 @@ struct PickTask {
   // selection keys of aux j, (value bits << 32 | index), precomputed for the first nkeys steps
   // of the normal softdbsize sequence (sources shared by all realizations; nullable)
   const unsigned long long* aux_keys[IQ_MAX_AUX];
+  const PreBand* aux_pb[IQ_MAX_AUX];        // refined selections of shared maps (nullable)
+  const int32_t* pb_pool;                   // their band lists
   int nkeys;
   int64_t tile;                             // Philox counter of the draw
   // direct re-evaluation of D0 and of each auxiliary map (kappa == 0, or img == nullptr:
@@ -358,6 +373,12 @@ inline ExactSrc iq_exact_none() {
 constexpr int IQ_PRE_KEYS = 3;  // softdbsize steps precomputed per shared map
 int iq_launch_select_keys(iq_ctx* ctx, const float* maps, const unsigned* mm, int64_t nmaps,
                           int64_t P, const int64_t* seq, int nq, unsigned long long* keys);
+// Refined selections of nmaps shared maps (map m at maps + m * P, its re-evaluation srcs[m],
+// a device array) for the sizes seq[0..nq): out[m * nq + q], lists in pool (cap entries each).
+int iq_launch_select_bands(iq_ctx* ctx, const float* maps, const unsigned* mm,
+                           const ExactSrc* srcs, int64_t nmaps, int64_t P, int64_t dx,
+                           int64_t dxy, const int64_t* seq, int nq, PreBand* out, int32_t* pool,
+                           int64_t cap);
 
 // ---------------------------------------------------------------------------------------
 // Graph cut (iq_graphcut.cu) and paste (iq_paste.cu)
@@ -454,6 +475,35 @@ struct LpGeo {
   int off_b4, npar;
 };
 LpGeo iq_lp_geo(Dim3 tile);
+
+// One training step's data (device pointers): nA anchors with features feats[feat row], their
+// positives and nneg negatives per anchor as windows of the image (integral images ii1, ii2);
+// items: anchors, then positives, then negatives (iq_proposal.cu TrainItem layout, 16 bytes).
+struct LpTrainBatch {
+  const float* w;          // FP32 parameters
+  const void* items;
+  int nA, nneg;
+  float temp;
+  const float* feats;      // [rows][3 * ng]
+  const int32_t* boxes;    // [rows][6]
+  const double* ii1;
+  const double* ii2;
+  Dim3 img, dist;
+  float* X;                // scratch [items][3 * ng]
+  float* E;                // scratch [items][64]
+  float* gE;               // scratch [items][64]
+  float* grad;             // [npar]
+  double* loss;            // device scalar
+};
+int iq_lp_train_batch(iq_ctx* ctx, const LpGeo& g, const LpTrainBatch& B, double* loss_out);
+int iq_lp_adam(iq_ctx* ctx, float* p, const float* g, float* m, float* v, int n, float lr, int step);
+struct __nv_bfloat16;
+int iq_lp_encode_windows(iq_ctx* ctx, const LpGeo& g, const float* w, const double* ii1,
+                         const double* ii2, Dim3 img, Dim3 dist, const int* lo, const int* hi,
+                         __nv_bfloat16* out, float* norm);
+int iq_lp_encode_templates(iq_ctx* ctx, const LpGeo& g, const float* w, const float* grid,
+                           Dim3 gdims, const int64_t* tsrc, const int* tbox, int64_t n,
+                           __nv_bfloat16* out, float* norm);
 
 // relaxation sizes of src/relaxation.jl:11-36 for a given npatterns (iq_sim.cu)
 void iq_relax_sizes(int64_t npat, double tol, int64_t& dbnorm, int64_t& dbzero, int& nnorm,

@@ -1434,7 +1434,8 @@ __global__ void __launch_bounds__(PT) pick_kernel(const PickArgs a) {
       int j0 = 0;
       if (q == 0) {
         req[0] = SelReq{D, mm[0], mm[1], dbsize};
-        const bool pre0 = !allzero && tk.aux_keys[0] && q < tk.nkeys;
+        const bool pre0 = !allzero && q < tk.nkeys &&
+                          (tk.aux_keys[0] || (tk.aux_pb[0] && tk.aux_pb[0][q].ok));
         if (NAUX > 0 && naux > 0 && sz > 0 && sz < P && !pre0) {
           req[1] = SelReq{aux[0], amm[0][0], amm[0][1], sz};
           hist_select<2>(s, hist, sbuf, req, P, res);
@@ -1460,6 +1461,17 @@ __global__ void __launch_bounds__(PT) pick_kernel(const PickArgs a) {
         if (j >= naux) continue;
         tiesA[j] = -1;
         pr.ba[j] = nullptr;
+        if (j >= j0 && !allzero && tk.aux_pb[j] && q < tk.nkeys && tk.aux_pb[j][q].ok) {
+          // shared source with an error bound: its refined selection is precomputed
+          const PreBand& pb = tk.aux_pb[j][q];
+          pr.ka[j] = Key{(uint32_t)(pb.key >> 32), (uint32_t)pb.key};
+          if (threadIdx.x == 0)
+            sband[1 + j] = Band{pb.lo, pb.hi, const_cast<int32_t*>(tk.pb_pool) + pb.off, pb.n};
+          __syncthreads();
+          pr.ba[j] = &sband[1 + j];
+          tiesA[j] = pb.ties;
+          continue;
+        }
         if (j >= j0) {
           if (!allzero && tk.aux_keys[j] && q < tk.nkeys) {  // shared source: key precomputed
             const unsigned long long kk = tk.aux_keys[j][q];
@@ -1692,5 +1704,123 @@ int iq_launch_select_keys(iq_ctx* ctx, const float* maps, const unsigned* mm, in
   iq_timer_stop(ctx, "pick", 0);
   iq_count(ctx);
   IQ_CUDA_OK(cudaGetLastError());
+  return IQ_OK;
+}
+
+// ---- refined selections of shared maps ---------------------------------------------------------
+namespace {
+
+struct BandArgs {
+  const float* maps;
+  const unsigned* mm;
+  const ExactSrc* srcs;
+  int64_t m0, nmaps;  // maps [m0, m0 + nmaps) of this launch
+  int64_t P, dx, dxy;
+  int nq;
+  int64_t seq[IQ_PRE_KEYS];
+  PreBand* out;
+  int32_t* pool;
+  int64_t cap;
+  // per-CTA scratch, P entries each
+  double* rv;
+  double* rr;
+  uint8_t* rl;
+  int32_t* list;
+  uint32_t *k0, *v0, *k1, *v1;
+};
+
+// One CTA per (map, step): the key of the step's size, then, for a map with an error bound, the
+// band of positions whose order against it is uncertain, resolved exactly (band_topk).
+__global__ void __launch_bounds__(PT) select_bands_kernel(const BandArgs a) {
+  __shared__ Smem s;
+  extern __shared__ __align__(16) unsigned char dyn[];
+  uint32_t* hist = reinterpret_cast<uint32_t*>(dyn);
+  unsigned long long* sbuf = reinterpret_cast<unsigned long long*>(dyn + 2 * NBIN * 4);
+  const int64_t b = blockIdx.x;
+  const int64_t m = a.m0 + b / a.nq;
+  const int q = (int)(b % a.nq);
+  const int64_t k = a.seq[q];
+  const int64_t P = a.P;
+  PreBand* o = a.out + m * a.nq + q;
+  const float* src = a.maps + m * P;
+  Key key;
+  if (k >= P) key = Key{0xFFFFFFFFu, 0xFFFFFFFFu};
+  else if (k <= 0) key = Key{0u, 0u};
+  else {
+    SelReq req[1] = {SelReq{src, a.mm[2 * m], a.mm[2 * m + 1], k}};
+    Key res[1];
+    hist_select<1>(s, hist, sbuf, req, P, res);
+    key = res[0];
+  }
+  int ok = 0;
+  long long ties = 0;
+  Band band{};
+  if (k > 0 && k < P && ref_on(a.srcs[m])) {
+    const Ref f = make_ref(a.srcs[m], 0, a.dx, a.dxy);
+    RefArr ra;
+    ra.v = a.rv + b * P;
+    ra.r = a.rr + b * P;
+    ra.l = a.rl + 2 * b * P;
+    ra.link = ra.l + P;
+    int32_t* list = a.list + b * P;
+    ties = band_topk(s, sbuf, f, src, P, k, key, list, ra, a.k0 + b * P, a.v0 + b * P,
+                     a.k1 + b * P, a.v1 + b * P, band);
+    if (ties >= 0 && band.n <= a.cap) {
+      ok = 1;
+      int32_t* dst = a.pool + (m * a.nq + q) * a.cap;
+      for (int64_t i = threadIdx.x; i < band.n; i += PT) dst[i] = list[i];
+    }
+  }
+  if (threadIdx.x == 0) {
+    o->lo = band.lo;
+    o->hi = band.hi;
+    o->off = (m * a.nq + q) * a.cap;
+    o->n = band.n;
+    o->key = ((unsigned long long)key.v << 32) | key.i;
+    o->ties = ok ? ties : 0;
+    o->ok = ok;
+  }
+}
+
+}  // namespace
+
+int iq_launch_select_bands(iq_ctx* ctx, const float* maps, const unsigned* mm,
+                           const ExactSrc* srcs, int64_t nmaps, int64_t P, int64_t dx,
+                           int64_t dxy, const int64_t* seq, int nq, PreBand* out, int32_t* pool,
+                           int64_t cap) {
+  if (nmaps <= 0 || nq <= 0) return IQ_OK;
+  if (nq > IQ_PRE_KEYS) return iq_set_error(IQ_ERR_ARG, "too many precomputed selections");
+  // per-CTA scratch for a batch of CTAs (38 bytes per position each)
+  const int64_t per = P * (8 + 8 + 2 + 4 + 16);
+  size_t freeb = 0, totalb = 0;
+  cudaMemGetInfo(&freeb, &totalb);
+  const int64_t batch = std::max<int64_t>(1, std::min<int64_t>(nmaps * nq, (int64_t)(freeb / 8) / per));
+  // (slots of their own: the caller may hold pointers into the pick's scratch slots)
+  double* rv = (double*)iq_scratch(ctx, S_PB_RV, sizeof(double) * P * batch);
+  double* rr = (double*)iq_scratch(ctx, S_PB_RR, sizeof(double) * P * batch);
+  uint8_t* rl = (uint8_t*)iq_scratch(ctx, S_PB_RL, 2 * P * batch);
+  int32_t* list = (int32_t*)iq_scratch(ctx, S_PB_LIST, sizeof(int32_t) * P * batch);
+  uint32_t* kk = (uint32_t*)iq_scratch(ctx, S_PB_K, 4 * sizeof(uint32_t) * P * batch);
+  if (!rv || !rr || !rl || !list || !kk) return IQ_ERR_ALLOC;
+  uint32_t* k0 = kk;
+  uint32_t* v0 = kk + P * batch;
+  uint32_t* k1 = kk + 2 * P * batch;
+  uint32_t* v1 = kk + 3 * P * batch;
+  IQ_CUDA_OK(cudaFuncSetAttribute(select_bands_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)DYN_BYTES));
+  const int64_t mper = std::max<int64_t>(1, batch / nq);
+  for (int64_t m0 = 0; m0 < nmaps; m0 += mper) {
+    BandArgs a{};
+    a.maps = maps; a.mm = mm; a.srcs = srcs; a.m0 = m0; a.nmaps = std::min(mper, nmaps - m0);
+    a.P = P; a.dx = dx; a.dxy = dxy; a.nq = nq;
+    for (int q = 0; q < IQ_PRE_KEYS; ++q) a.seq[q] = q < nq ? seq[q] : 0;
+    a.out = out; a.pool = pool; a.cap = cap;
+    a.rv = rv; a.rr = rr; a.rl = rl; a.list = list; a.k0 = k0; a.v0 = v0; a.k1 = k1; a.v1 = v1;
+    iq_timer_start(ctx, "pick");
+    select_bands_kernel<<<(unsigned)(a.nmaps * nq), PT, DYN_BYTES, ctx->stream>>>(a);
+    iq_timer_stop(ctx, "pick", 0);
+    iq_count(ctx);
+    IQ_CUDA_OK(cudaGetLastError());
+  }
   return IQ_OK;
 }

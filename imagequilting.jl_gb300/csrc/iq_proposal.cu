@@ -314,3 +314,311 @@ int iq_lp_encode_templates(iq_ctx* ctx, const LpGeo& g, const float* w, const fl
   IQ_CUDA_OK(cudaGetLastError());
   return IQ_OK;
 }
+
+// =============================================================================================
+// Training: FP32 forward, InfoNCE loss, backward with parameter gradients, Adam
+// =============================================================================================
+namespace {
+
+// One training item: the features of a template (feat >= 0: row of `feats`) or a window of the
+// image at distance-map position `pos` under the mask box of anchor `box`.
+struct TrainItem {
+  int32_t feat;   // row of the anchor feature table, or -1
+  int32_t pos;    // window position when feat < 0
+  int32_t box;    // row of the box table
+  int32_t pad_;
+};
+
+struct TrainArgs {
+  LpGeo g;
+  const float* w;              // FP32 parameters
+  const TrainItem* items;
+  int64_t nitems;
+  const float* feats;          // [rows][NIN * ng]
+  const int32_t* boxes;        // [rows][6]
+  const double* ii1;
+  const double* ii2;
+  int64_t isx, isxy, dx, dxy;
+  float* X;                    // [nitems][NIN * ng] features (written by the forward pass)
+  float* E;                    // [nitems][EMB]
+  const float* gE;             // [nitems][EMB] d loss / d embedding (backward)
+  float* grad;                 // parameter gradients (accumulated)
+};
+
+__device__ void item_features(const TrainArgs& a, const TrainItem& it, float* X) {
+  const int G = a.g.ng;
+  if (it.feat >= 0) {
+    for (int i = threadIdx.x; i < NIN * G; i += blockDim.x) X[i] = a.feats[(int64_t)it.feat * NIN * G + i];
+  } else {
+    int lo[3], hi[3];
+    for (int d = 0; d < 3; ++d) { lo[d] = a.boxes[6 * it.box + d]; hi[d] = a.boxes[6 * it.box + 3 + d]; }
+    const int64_t p = it.pos;
+    const int64_t z = p / a.dxy, r = p - z * a.dxy, y = r / a.dx, x = r - y * a.dx;
+    for (int cell = threadIdx.x; cell < G; cell += blockDim.x) {
+      float f[3];
+      window_cell(a.g, a.ii1, a.ii2, a.isx, a.isxy, x, y, z, lo, hi, cell, f);
+      for (int c = 0; c < NIN; ++c) X[c * G + cell] = f[c];
+    }
+  }
+  __syncthreads();
+}
+
+__global__ void __launch_bounds__(LT) lp_train_fwd_kernel(const TrainArgs a) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  float* sm = reinterpret_cast<float*>(smraw);
+  const int G = a.g.ng;
+  for (int64_t item = blockIdx.x; item < a.nitems; item += gridDim.x) {
+    float* X = sm + SM_X;
+    item_features(a, a.items[item], X);
+    for (int i = threadIdx.x; i < NIN * G; i += blockDim.x) a.X[item * NIN * G + i] = X[i];
+    enc_forward<float>(a.g, a.w, X, sm + SM_H1, nullptr, sm + SM_H2, nullptr, sm + SM_H3, nullptr,
+                       sm + SM_E);
+    for (int o = threadIdx.x; o < EMB; o += blockDim.x) a.E[item * EMB + o] = sm[SM_E + o];
+    __syncthreads();
+  }
+}
+
+// Backward of one item. Shared memory (floats): X, h1, h2, h3, e (as the forward), then gh1
+// [CH][G], gh2 [CH][G2], gz3 [CH][G3], gf [nf], ge [EMB].
+constexpr int SB_GH1 = SM_END;
+constexpr int SB_GH2 = SB_GH1 + CH * IQ_LP_MAXG;
+constexpr int SB_GZ3 = SB_GH2 + CH * IQ_LP_MAXG2;
+constexpr int SB_GF = SB_GZ3 + CH * IQ_LP_MAXG3;
+constexpr int SB_GE = SB_GF + CH * IQ_LP_MAXG3;
+constexpr int SB_END = SB_GE + EMB;
+
+// Cell of the layer below that output cell m reads through tap t (-1: padding), as tap_cell;
+// the inverse: output cell of grid Go reading input cell j through tap t (-1: none).
+__device__ __forceinline__ int tap_out(const int* Gi, const int* Go, int j, int t) {
+  const int jx = j % Gi[0], jy = (j / Gi[0]) % Gi[1], jz = j / (Gi[0] * Gi[1]);
+  const int dx = t % 3, dy = (t / 3) % 3, dz = t / 9;
+  const int ax = jx + 1 - dx, ay = jy + 1 - dy, az = jz + 1 - dz;
+  if ((ax | ay | az) & 1) return -1;
+  if (ax < 0 || ay < 0 || az < 0) return -1;
+  const int mx = ax >> 1, my = ay >> 1, mz = az >> 1;
+  if (mx >= Go[0] || my >= Go[1] || mz >= Go[2]) return -1;
+  return mx + Go[0] * (my + Go[1] * mz);
+}
+
+__global__ void __launch_bounds__(LT) lp_train_bwd_kernel(const TrainArgs a) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  float* sm = reinterpret_cast<float*>(smraw);
+  const LpGeo& g = a.g;
+  const int G = g.ng, G2 = g.ng2, G3 = g.ng3, nf = g.nf;
+  const float* w = a.w;
+  float* gr = a.grad;
+  for (int64_t item = blockIdx.x; item < a.nitems; item += gridDim.x) {
+    float* X = sm + SM_X;
+    float* h1 = sm + SM_H1;
+    float* h2 = sm + SM_H2;
+    float* h3 = sm + SM_H3;
+    for (int i = threadIdx.x; i < NIN * G; i += blockDim.x) X[i] = a.X[item * NIN * G + i];
+    __syncthreads();
+    enc_forward<float>(g, w, X, h1, nullptr, h2, nullptr, h3, nullptr, sm + SM_E);
+    float* ge = sm + SB_GE;
+    float* gf = sm + SB_GF;
+    float* gz3 = sm + SB_GZ3;
+    float* gh2 = sm + SB_GH2;
+    float* gh1 = sm + SB_GH1;
+    for (int o = threadIdx.x; o < EMB; o += blockDim.x) ge[o] = a.gE[item * EMB + o];
+    __syncthreads();
+    // output layer
+    for (int i = threadIdx.x; i < EMB * nf; i += blockDim.x) {
+      const int o = i / nf, f = i - o * nf;
+      const int c = f % CH, m = f / CH;
+      atomicAdd(gr + LP_OFF_W4 + i, ge[o] * h3[c * G3 + m]);
+    }
+    for (int o = threadIdx.x; o < EMB; o += blockDim.x) atomicAdd(gr + g.off_b4 + o, ge[o]);
+    for (int f = threadIdx.x; f < nf; f += blockDim.x) {
+      float acc = 0.f;
+      for (int o = 0; o < EMB; ++o) acc = fmaf(w[LP_OFF_W4 + o * nf + f], ge[o], acc);
+      gf[f] = acc;
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < CH * G3; i += blockDim.x) {
+      const int c = i / G3, m = i - c * G3;
+      gz3[i] = h3[i] > 0.f ? gf[c + CH * m] : 0.f;
+    }
+    __syncthreads();
+    // layer 3: weights and bias, then the gradient of h2 (masked by ReLU into gz2 in place)
+    for (int i = threadIdx.x; i < CH * CH * 27; i += blockDim.x) {
+      const int c = i / (CH * 27), rem = i - c * CH * 27, ci = rem / 27, t = rem - ci * 27;
+      float acc = 0.f;
+      for (int m = 0; m < G3; ++m) {
+        const int ox = m % g.g3[0], oy = (m / g.g3[0]) % g.g3[1], oz = m / (g.g3[0] * g.g3[1]);
+        const int src = tap_cell(g.g2, ox, oy, oz, t);
+        if (src >= 0) acc = fmaf(gz3[c * G3 + m], h2[ci * G2 + src], acc);
+      }
+      if (acc != 0.f) atomicAdd(gr + LP_OFF_W3 + i, acc);
+    }
+    for (int c = threadIdx.x; c < CH; c += blockDim.x) {
+      float acc = 0.f;
+      for (int m = 0; m < G3; ++m) acc += gz3[c * G3 + m];
+      atomicAdd(gr + LP_OFF_B3 + c, acc);
+    }
+    for (int i = threadIdx.x; i < CH * G2; i += blockDim.x) {
+      const int ci = i / G2, j = i - ci * G2;
+      float acc = 0.f;
+      if (h2[i] > 0.f) {
+        for (int t = 0; t < 27; ++t) {
+          const int m = tap_out(g.g2, g.g3, j, t);
+          if (m < 0) continue;
+          for (int c = 0; c < CH; ++c) acc = fmaf(w[LP_OFF_W3 + (c * CH + ci) * 27 + t], gz3[c * G3 + m], acc);
+        }
+      }
+      gh2[i] = acc;  // already d/dz2 (zero where the ReLU was off)
+    }
+    __syncthreads();
+    // layer 2
+    for (int i = threadIdx.x; i < CH * CH * 27; i += blockDim.x) {
+      const int c = i / (CH * 27), rem = i - c * CH * 27, ci = rem / 27, t = rem - ci * 27;
+      float acc = 0.f;
+      for (int m = 0; m < G2; ++m) {
+        const float gzm = gh2[c * G2 + m];
+        if (gzm == 0.f) continue;
+        const int ox = m % g.g2[0], oy = (m / g.g2[0]) % g.g2[1], oz = m / (g.g2[0] * g.g2[1]);
+        const int src = tap_cell(g.g, ox, oy, oz, t);
+        if (src >= 0) acc = fmaf(gzm, h1[ci * G + src], acc);
+      }
+      if (acc != 0.f) atomicAdd(gr + LP_OFF_W2 + i, acc);
+    }
+    for (int c = threadIdx.x; c < CH; c += blockDim.x) {
+      float acc = 0.f;
+      for (int m = 0; m < G2; ++m) acc += gh2[c * G2 + m];
+      atomicAdd(gr + LP_OFF_B2 + c, acc);
+    }
+    for (int i = threadIdx.x; i < CH * G; i += blockDim.x) {
+      const int ci = i / G, j = i - ci * G;
+      float acc = 0.f;
+      if (h1[i] > 0.f) {
+        for (int t = 0; t < 27; ++t) {
+          const int m = tap_out(g.g, g.g2, j, t);
+          if (m < 0) continue;
+          for (int c = 0; c < CH; ++c) acc = fmaf(w[LP_OFF_W2 + (c * CH + ci) * 27 + t], gh2[c * G2 + m], acc);
+        }
+      }
+      gh1[i] = acc;  // d/dz1
+    }
+    __syncthreads();
+    // layer 1
+    for (int i = threadIdx.x; i < CH * NIN; i += blockDim.x) {
+      const int c = i / NIN, ci = i - c * NIN;
+      float acc = 0.f;
+      for (int cell = 0; cell < G; ++cell) acc = fmaf(gh1[c * G + cell], X[ci * G + cell], acc);
+      atomicAdd(gr + LP_OFF_W1 + i, acc);
+    }
+    for (int c = threadIdx.x; c < CH; c += blockDim.x) {
+      float acc = 0.f;
+      for (int cell = 0; cell < G; ++cell) acc += gh1[c * G + cell];
+      atomicAdd(gr + LP_OFF_B1 + c, acc);
+    }
+    __syncthreads();
+  }
+}
+
+// InfoNCE of anchor b (one warp): items b (anchor), nA + b (positive), 2 nA + b * nneg + n
+// (negatives). Writes d loss / d embedding of those items (scaled by 1 / nA) and adds the loss.
+__global__ void lp_loss_kernel(const float* __restrict__ E, int nA, int nneg, float temp,
+                               float* gE, double* loss) {
+  const int lane = threadIdx.x & 31;
+  const int b = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (b >= nA) return;
+  const int nj = 1 + nneg;
+  auto item_of = [&](int j) -> int64_t {
+    return j == 0 ? (int64_t)nA + b : 2 * (int64_t)nA + (int64_t)b * nneg + (j - 1);
+  };
+  const float a0 = E[(int64_t)b * EMB + lane], a1 = E[(int64_t)b * EMB + 32 + lane];
+  // logits
+  float zmax = -1e30f;
+  for (int j = 0; j < nj; ++j) {
+    const int64_t it = item_of(j);
+    const float d0 = a0 - E[it * EMB + lane], d1 = a1 - E[it * EMB + 32 + lane];
+    float s = d0 * d0 + d1 * d1;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    zmax = fmaxf(zmax, -s / temp);
+  }
+  float den = 0.f, z0 = 0.f;
+  for (int j = 0; j < nj; ++j) {
+    const int64_t it = item_of(j);
+    const float d0 = a0 - E[it * EMB + lane], d1 = a1 - E[it * EMB + 32 + lane];
+    float s = d0 * d0 + d1 * d1;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    const float z = -s / temp;
+    if (j == 0) z0 = z;
+    den += expf(z - zmax);
+  }
+  if (lane == 0) atomicAdd(loss, (double)(-z0 + zmax + logf(den)) / nA);
+  float ga0 = 0.f, ga1 = 0.f;
+  const float sc = 1.f / (float)nA;
+  for (int j = 0; j < nj; ++j) {
+    const int64_t it = item_of(j);
+    const float d0 = a0 - E[it * EMB + lane], d1 = a1 - E[it * EMB + 32 + lane];
+    float s = d0 * d0 + d1 * d1;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    float gz = expf(-s / temp - zmax) / den - (j == 0 ? 1.f : 0.f);
+    gz *= sc;
+    // z_j = -|ea - ej|^2 / T: dz/dea = -2 d / T, dz/dej = 2 d / T
+    ga0 += gz * (-2.f * d0 / temp);
+    ga1 += gz * (-2.f * d1 / temp);
+    gE[it * EMB + lane] = gz * (2.f * d0 / temp);
+    gE[it * EMB + 32 + lane] = gz * (2.f * d1 / temp);
+  }
+  gE[(int64_t)b * EMB + lane] = ga0;
+  gE[(int64_t)b * EMB + 32 + lane] = ga1;
+}
+
+__global__ void lp_adam_kernel(float* p, const float* g, float* m, float* v, int n, float lr,
+                               float b1, float b2, float eps, float c1, float c2) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float gi = g[i];
+  const float mi = b1 * m[i] + (1.f - b1) * gi;
+  const float vi = b2 * v[i] + (1.f - b2) * gi * gi;
+  m[i] = mi;
+  v[i] = vi;
+  p[i] -= lr * (mi / c1) / (sqrtf(vi / c2) + eps);
+}
+
+}  // namespace
+
+int iq_lp_train_batch(iq_ctx* ctx, const LpGeo& g, const LpTrainBatch& B, double* loss_out) {
+  const int64_t nitems = (int64_t)B.nA * (2 + B.nneg);
+  TrainArgs a{};
+  a.g = g; a.w = B.w; a.items = static_cast<const TrainItem*>(B.items); a.nitems = nitems;
+  a.feats = B.feats; a.boxes = B.boxes; a.ii1 = B.ii1; a.ii2 = B.ii2;
+  a.isx = B.img.x + 1; a.isxy = (B.img.x + 1) * (B.img.y + 1);
+  a.dx = B.dist.x; a.dxy = B.dist.x * B.dist.y;
+  a.X = B.X; a.E = B.E; a.gE = B.gE; a.grad = B.grad;
+  const size_t smf = sizeof(float) * SM_END + 16;
+  const size_t smb = sizeof(float) * SB_END + 16;
+  IQ_CUDA_OK(cudaFuncSetAttribute(lp_train_fwd_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smf));
+  IQ_CUDA_OK(cudaFuncSetAttribute(lp_train_bwd_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smb));
+  cudaStream_t st = ctx->stream;
+  const unsigned blocks = (unsigned)std::min<int64_t>(nitems, 2048);
+  lp_train_fwd_kernel<<<blocks, LT, smf, st>>>(a);
+  IQ_CUDA_OK(cudaGetLastError());
+  IQ_CUDA_OK(cudaMemsetAsync(B.loss, 0, sizeof(double), st));
+  lp_loss_kernel<<<(unsigned)((B.nA + 7) / 8), 256, 0, st>>>(B.E, B.nA, B.nneg, B.temp, B.gE, B.loss);
+  IQ_CUDA_OK(cudaGetLastError());
+  IQ_CUDA_OK(cudaMemsetAsync(B.grad, 0, sizeof(float) * g.npar, st));
+  lp_train_bwd_kernel<<<blocks, LT, smb, st>>>(a);
+  IQ_CUDA_OK(cudaGetLastError());
+  iq_count(ctx, 3);
+  if (loss_out) {
+    IQ_CUDA_OK(cudaMemcpyAsync(loss_out, B.loss, sizeof(double), cudaMemcpyDeviceToHost, st));
+    IQ_CUDA_OK(cudaStreamSynchronize(st));
+  }
+  return IQ_OK;
+}
+
+int iq_lp_adam(iq_ctx* ctx, float* p, const float* g, float* m, float* v, int n, float lr, int step) {
+  const float b1 = 0.9f, b2 = 0.999f;
+  const float c1 = 1.f - std::pow(b1, (float)step), c2 = 1.f - std::pow(b2, (float)step);
+  lp_adam_kernel<<<(unsigned)((n + 255) / 256), 256, 0, ctx->stream>>>(p, g, m, v, n, lr, b1, b2, 1e-8f, c1, c2);
+  iq_count(ctx);
+  IQ_CUDA_OK(cudaGetLastError());
+  return IQ_OK;
+}

@@ -856,11 +856,48 @@ extern "C" int iq_simulate(iq_ctx* ctx, const iq_sim_params* p, const iq_hard_da
   if (npat > 0) iq_relax_sizes(npat, p->tol, dbn, dbz, nsn, seqn, nsz, seqz);
   const int nkeys = std::min(nsn, IQ_PRE_KEYS);
   unsigned long long* d_softkeys = nullptr;
+  PreBand* d_pb = nullptr;      // refined selections of the soft maps (maps with an error bound)
+  int32_t* d_pbpool = nullptr;
+  const int64_t pb_cap = 8192;  // listed band positions per selection
   if (nsoft > 0 && npat > 0 && nkeys > 0 && nslot > 0) {
     d_softkeys = (unsigned long long*)iq_scratch(ctx, S_SOFTKEYS,
                                                  sizeof(unsigned long long) * nslot * nsoft * nkeys);
     if (!d_softkeys) return IQ_ERR_ALLOC;
     RET_IF(iq_launch_select_keys(ctx, d_soft, d_softmm, nslot * nsoft, P, seqn, nkeys, d_softkeys));
+    bool any_ref = false;
+    for (int sv = 0; sv < nsoft; ++sv) any_ref = any_ref || soft_kappa[sv] > 0.0;
+    if (any_ref) {
+      // the re-evaluation of every soft map: the auxiliary TI against the padded auxiliary grid
+      // at the tile, over the full tile
+      std::vector<ExactSrc> xs((size_t)nslot * nsoft);
+      for (int64_t t = 0; t < g.ntot; ++t) {
+        if (slot_of[t] < 0) continue;
+        const int64_t st3[3] = {(t % g.ntiles[0]) * g.spacing[0],
+                                ((t / g.ntiles[0]) % g.ntiles[1]) * g.spacing[1],
+                                (t / (g.ntiles[0] * g.ntiles[1])) * g.spacing[2]};
+        for (int sv = 0; sv < nsoft; ++sv) {
+          const int64_t slot = (int64_t)sv * nslot + slot_of[t];
+          ExactSrc& x = xs[slot];
+          if (!(soft_kappa[sv] > 0.0)) continue;
+          const Dim3 ad = aux_dims[sv];
+          x.img = d_auxti[sv]; x.isx = ctx->ti.x; x.isxy = ctx->ti.x * ctx->ti.y;
+          x.klist = d_kl + (size_t)ncfg * T; x.K = (int)T;
+          x.tmpl = d_aux[sv] + st3[0] + ad.x * (st3[1] + ad.y * st3[2]);
+          x.tgx = ad.x; x.tgxy = ad.x * ad.y; x.tmpl_rs = 0;
+          x.b2 = d_softb2 + slot; x.b2_rs = 0;
+          x.kappa = soft_kappa[sv]; x.eabs = soft_eabs[sv];
+        }
+      }
+      ExactSrc* d_xs = (ExactSrc*)iq_scratch(ctx, S_PB_SRC, sizeof(ExactSrc) * xs.size());
+      d_pb = (PreBand*)iq_scratch(ctx, S_PB_OUT, sizeof(PreBand) * nslot * nsoft * nkeys);
+      d_pbpool = (int32_t*)iq_scratch(ctx, S_PB_POOL, sizeof(int32_t) * nslot * nsoft * nkeys * pb_cap);
+      if (!d_xs || !d_pb || !d_pbpool) return IQ_ERR_ALLOC;
+      IQ_CUDA_OK(cudaMemcpyAsync(d_xs, xs.data(), sizeof(ExactSrc) * xs.size(),
+                                 cudaMemcpyHostToDevice, st));
+      RET_IF(iq_launch_select_bands(ctx, d_soft, d_softmm, d_xs, nslot * nsoft, P, distD.x,
+                                    distD.x * distD.y, seqn, nkeys, d_pb, d_pbpool, pb_cap));
+      IQ_CUDA_OK(cudaStreamSynchronize(st));  // `xs` is a host vector
+    }
   }
 
   // ---- task descriptors of every step, uploaded once ----
@@ -942,6 +979,11 @@ extern "C" int iq_simulate(iq_ctx* ctx, const iq_sim_params* p, const iq_hard_da
           q.aux[na] = d_soft + slot * P; q.aux_rs[na] = 0;
           q.aux_mm[na] = d_softmm + 2 * slot; q.aux_mm_rs[na] = 0;
           if (soft_kappa[sv] > 0.0) {
+            if (d_pb) {  // refined selections shared by all realizations
+              q.aux_pb[na] = d_pb + slot * nkeys;
+              q.pb_pool = d_pbpool;
+              q.nkeys = nkeys;
+            }
             // the auxiliary TI against the padded auxiliary grid at the tile, full tile
             ExactSrc& xs = q.xa[na];
             xs.img = d_auxti[sv]; xs.isx = ctx->ti.x; xs.isxy = ctx->ti.x * ctx->ti.y;
