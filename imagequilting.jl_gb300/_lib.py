@@ -55,6 +55,20 @@ SIGNATURES = {
     "iq_ctx_destroy": (ctypes.c_int, [ctypes.c_void_p]),
     "iq_ctx_stream": (ctypes.c_void_p, [ctypes.c_void_p]),
     "iq_ties": (ctypes.c_int, [ctypes.c_void_p, c_i64p]),
+    "iq_lp_init": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, c_i64p, ctypes.c_uint64]),
+    "iq_lp_params": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, c_i64p]),
+    "iq_lp_set_params": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, c_i64p, ctypes.c_void_p,
+                                        ctypes.c_int64]),
+    "iq_lp_embed": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int64, c_i64p, ctypes.c_void_p,
+                                   ctypes.c_void_p]),
+    "iq_lp_loss_grad": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32,
+                                       ctypes.c_void_p, c_i64p, c_i64p, ctypes.c_void_p,
+                                       ctypes.c_double, ctypes.POINTER(ctypes.c_double),
+                                       ctypes.c_void_p]),
+    "iq_lp_train": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
+                                   ctypes.c_double, ctypes.c_double, ctypes.c_uint64,
+                                   ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]),
+    "iq_lp_stats": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32]),
     "iq_set_ti": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32,
                                  c_i64p]),
     "iq_simulate": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(SimParams),

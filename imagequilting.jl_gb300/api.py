@@ -104,6 +104,65 @@ class Context:
         check(load().iq_ties(self.h, ctypes.byref(v)))
         return int(v.value)
 
+    # ---- learned proposal (no counterpart in the reference) ------------------------------
+    def lp_init(self, tilesize, seed=0):
+        """Fresh encoder parameters for tiles of this shape."""
+        check(load().iq_lp_init(self.h, len(tilesize), i64arr(tilesize), int(seed)))
+        self._lp_tile = tuple(int(t) for t in tilesize)
+
+    def lp_params(self):
+        """The encoder's FP32 parameters (flat, the layout of oracle/proposal_oracle.py)."""
+        n = ctypes.c_int64()
+        check(load().iq_lp_params(self.h, None, 0, ctypes.byref(n)))
+        out = np.empty(n.value, np.float32)
+        check(load().iq_lp_params(self.h, out.ctypes.data, n.value, ctypes.byref(n)))
+        return out
+
+    def lp_set_params(self, tilesize, params):
+        p = np.ascontiguousarray(params, np.float32)
+        check(load().iq_lp_set_params(self.h, len(tilesize), i64arr(tilesize), p.ctypes.data,
+                                      p.size))
+        self._lp_tile = tuple(int(t) for t in tilesize)
+
+    def lp_embed(self, positions, box):
+        """Window embeddings (n x 64) of the resident TI at linear distance-map positions under
+        the mask "tile minus box" (box = (lo0, lo1, lo2, hi0, hi1, hi2))."""
+        pos = np.ascontiguousarray(positions, np.int64)
+        b = np.ascontiguousarray(box, np.int32)
+        out = np.empty((pos.size, 64), np.float32)
+        check(load().iq_lp_embed(self.h, pos.size, pos.ctypes.data_as(_lib.c_i64p), b.ctypes.data,
+                                 out.ctypes.data))
+        return out
+
+    def lp_loss_grad(self, anchor_feats, pos_positions, neg_positions, box, temp):
+        a = np.ascontiguousarray(anchor_feats, np.float32)
+        pp = np.ascontiguousarray(pos_positions, np.int64)
+        nn = np.ascontiguousarray(neg_positions, np.int64)
+        b = np.ascontiguousarray(box, np.int32)
+        nA = pp.size
+        nneg = nn.size // max(nA, 1)
+        loss = ctypes.c_double()
+        grad = np.empty(self.lp_params().size, np.float32)
+        check(load().iq_lp_loss_grad(self.h, nA, nneg, a.ctypes.data, pp.ctypes.data_as(_lib.c_i64p),
+                                     nn.ctypes.data_as(_lib.c_i64p), b.ctypes.data, float(temp),
+                                     ctypes.byref(loss), grad.ctypes.data))
+        return loss.value, grad
+
+    def lp_train(self, steps, batch=128, nneg=16, lr=1e-3, temp=8.0, seed=0):
+        """Adam steps on the captured pairs; returns (first batch loss, last batch loss)."""
+        l0, l1 = ctypes.c_double(), ctypes.c_double()
+        check(load().iq_lp_train(self.h, int(steps), int(batch), int(nneg), float(lr), float(temp),
+                                 int(seed), ctypes.byref(l0), ctypes.byref(l1)))
+        return l0.value, l1.value
+
+    def lp_stats(self):
+        """Statistics of the last iqsim call (see include/iqgpu.h, iq_lp_stats)."""
+        out = np.zeros(9)
+        check(load().iq_lp_stats(self.h, out.ctypes.data, 9))
+        keys = ("cols_shortlist", "cols_full", "monitored", "true_candidates", "shortlisted",
+                "recall", "fell_back", "mean_shortlist", "captured")
+        return dict(zip(keys, out.tolist()))
+
     @property
     def launches(self):
         return int(load().iq_ctx_launches(self.h))

@@ -11,7 +11,8 @@ ROOT = os.path.dirname(HERE)
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libiqgpu.so")
 SOURCES = ["iq_abi.cu", "iq_sim.cu", "iq_distance.cu", "iq_pick.cu", "iq_graphcut.cu",
-           "iq_paste.cu", "iq_noalloc.cu", "iq_corr_tc.cu"]
+           "iq_paste.cu", "iq_noalloc.cu", "iq_corr_tc.cu", "iq_proposal.cu", "iq_proposal_pick.cu",
+           "iq_proposal_host.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

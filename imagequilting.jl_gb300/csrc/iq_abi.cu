@@ -210,6 +210,7 @@ extern "C" int iq_ctx_destroy(iq_ctx* ctx) {
   cudaFree(ctx->d_status);
   cudaFree(ctx->d_stats);
   cudaFree(ctx->d_ties);
+  iq_lp_free(ctx);
   if (ctx->stream2) {
     cudaStreamSynchronize(ctx->stream2);
     cudaStreamDestroy(ctx->stream2);
@@ -268,6 +269,34 @@ extern "C" int iq_set_option(iq_ctx* ctx, const char* name, int64_t value) {
   if (!strcmp(name, "sim.streams")) {
     if (value < 1 || value > 2) return iq_set_error(IQ_ERR_ARG, "sim.streams must be 1 or 2");
     ctx->sim_streams = (int)value;
+    return IQ_OK;
+  }
+  if (!strcmp(name, "lp.enable")) {
+    if (value < 0 || value > 1) return iq_set_error(IQ_ERR_ARG, "lp.enable must be 0 or 1");
+    ctx->lp_enable = (int)value;
+    return IQ_OK;
+  }
+  if (!strcmp(name, "lp.k")) {
+    if (value < 16 || value > (1 << 20)) return iq_set_error(IQ_ERR_ARG, "lp.k out of range");
+    ctx->lp_k = value;
+    return IQ_OK;
+  }
+  if (!strcmp(name, "lp.monitor")) {
+    if (value < 0 || value > (1 << 20)) return iq_set_error(IQ_ERR_ARG, "lp.monitor out of range");
+    ctx->lp_monitor = (int)value;
+    return IQ_OK;
+  }
+  if (!strcmp(name, "lp.fallback")) {
+    if (value < 0 || value > 1) return iq_set_error(IQ_ERR_ARG, "lp.fallback must be 0 or 1");
+    ctx->lp_fallback = (int)value;
+    return IQ_OK;
+  }
+  if (!strcmp(name, "lp.capture")) {
+    if (value < 0 || value > (1 << 24)) return iq_set_error(IQ_ERR_ARG, "lp.capture out of range");
+    IQ_CUDA_OK(cudaSetDevice(ctx->device));
+    const int rc = iq_lp_capture_reserve(ctx, value);
+    if (rc) return rc;
+    ctx->lp_capture = value;
     return IQ_OK;
   }
   return iq_set_error(IQ_ERR_ARG, "unknown option '%s'", name);
@@ -333,6 +362,7 @@ extern "C" int iq_set_ti(iq_ctx* ctx, const void* ti, int32_t dtype, int32_t ndi
   ctx->ti_nan = total;
   ctx->ti_stats = st;
   ctx->has_ti = true;
+  ctx->ti_version += 1;
   return IQ_OK;
 }
 

@@ -224,7 +224,7 @@ __global__ void gather_kernel(const GatherArgs g) {
 template <typename T>
 __global__ void ii_fill_kernel(const float* __restrict__ img, const uint8_t* __restrict__ nan,
                                int64_t nx, int64_t ny, int64_t nz, T* __restrict__ ii, int mode) {
-  // mode 0: v^2, mode 1: nan indicator; writes the (x+1, y+1, z+1) cell
+  // mode 0: v^2, mode 1: nan indicator, mode 2: v; writes the (x+1, y+1, z+1) cell
   const int64_t n = nx * ny * nz;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x) {
@@ -233,6 +233,8 @@ __global__ void ii_fill_kernel(const float* __restrict__ img, const uint8_t* __r
     if (mode == 0) {
       double f = (double)img[i];
       v = (T)(f * f);
+    } else if (mode == 2) {
+      v = (T)img[i];
     } else {
       v = (T)(nan[i] ? 1 : 0);
     }
@@ -343,6 +345,22 @@ int iq_launch_gather(iq_ctx* ctx, const GatherLaunch& G) {
   dim3 grid((unsigned)G.rpad, (unsigned)G.ntask);
   gather_kernel<<<grid, 256, 0, ctx->stream>>>(g);
   iq_count(ctx);
+  IQ_CUDA_OK(cudaGetLastError());
+  return IQ_OK;
+}
+
+int iq_build_value_integral(iq_ctx* ctx, const float* d_img, Dim3 dims, double* d_ii) {
+  const int64_t sx = dims.x + 1, sy = dims.y + 1, sz = dims.z + 1;
+  const int64_t n = dims.vol();
+  const int blocks = (int)std::min<int64_t>((n + 255) / 256, 4096);
+  IQ_CUDA_OK(cudaMemsetAsync(d_ii, 0, sizeof(double) * sx * sy * sz, ctx->stream));
+  ii_fill_kernel<double><<<blocks, 256, 0, ctx->stream>>>(d_img, nullptr, dims.x, dims.y, dims.z,
+                                                         d_ii, 2);
+  iq_count(ctx, 4);
+  for (int ax = 0; ax < 3; ++ax) {
+    const int64_t nl = ax == 0 ? sy * sz : ax == 1 ? sx * sz : sx * sy;
+    ii_scan_kernel<double><<<(int)((nl + 127) / 128), 128, 0, ctx->stream>>>(d_ii, sx, sy, sz, ax);
+  }
   IQ_CUDA_OK(cudaGetLastError());
   return IQ_OK;
 }

@@ -87,6 +87,13 @@ struct iq_ctx {
   int64_t max_steps = -1;       // tiles simulated per realization (< 0: all)
   int sim_streams = 1;          // realization groups of iq_simulate, each on its own stream
   cudaStream_t stream2 = nullptr;  // stream of the second realization group (made on first use)
+  struct IqLp* lp = nullptr;       // learned proposal state (iq_proposal_host.cu)
+  int lp_enable = 0;               // iq_simulate shortlists with the proposal where it applies
+  int64_t lp_k = 4096;             // shortlist size the proposal aims at
+  int64_t lp_capture = 0;          // training pairs iq_simulate records (0: none)
+  int lp_monitor = 16;             // every lp_monitor-th proposal chunk checks its recall
+  int lp_fallback = 1;             // 0: keep the shortlists even below 0.99 recall (measuring)
+  int64_t ti_version = 0;          // bumped by every iq_set_ti (keys the proposal's caches)
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
 };
 enum IqStat { ST_CUT_ROUNDS = 0, ST_CUT_LEVELS, ST_CUT_CTAS, ST_PICK_ITERS, ST_PICK_CAND,
@@ -113,6 +120,8 @@ enum IqSlot {
   S_TMP0, S_TMP1, S_TMP2, S_STARTS, S_SOFTMM, S_TASKS, S_VOX, S_TCB, S_TCCOLS, S_TCSTAGE, S_TCB2, S_TCFLAG, S_TCSOFT, S_SOFTKEYS,
   S_PICK_RV, S_PICK_RR, S_PICK_RL, S_SOFTB2,
   S_PB_RV, S_PB_RR, S_PB_RL, S_PB_LIST, S_PB_K, S_PB_OUT, S_PB_POOL, S_PB_SRC,
+  S_LP_T, S_LP_NT, S_LP_TAU, S_LP_LIST, S_LP_CNT, S_LP_DL, S_LP_COLS, S_LP_TSRC, S_LP_TBOX,
+  S_LP_RIND, S_LP_NCAND, S_LP_D, S_LP_BITS, S_LP_ITEMS, S_LP_X, S_LP_E, S_LP_GE, S_LP_FEAT,
   S_COUNT
 };
 
@@ -271,6 +280,7 @@ int iq_value_stats(iq_ctx* ctx, const float* d, int64_t n, IqValueStats& out);
 // integral images and disabled windows
 int iq_build_integrals(iq_ctx* ctx, const float* d_img, Dim3 dims, double* d_sqii,
                        int32_t* d_nanii, const uint8_t* d_nan);
+int iq_build_value_integral(iq_ctx* ctx, const float* d_img, Dim3 dims, double* d_ii);
 int iq_launch_disabled(iq_ctx* ctx, const int32_t* d_nanii, Dim3 dims, Dim3 tile, uint8_t* out);
 
 // ---------------------------------------------------------------------------------------
@@ -498,9 +508,67 @@ struct LpTrainBatch {
 int iq_lp_train_batch(iq_ctx* ctx, const LpGeo& g, const LpTrainBatch& B, double* loss_out);
 int iq_lp_adam(iq_ctx* ctx, float* p, const float* g, float* m, float* v, int n, float lr, int step);
 struct __nv_bfloat16;
+// Window embeddings of every distance-map position (pos == nullptr) or of pos[0, npos).
 int iq_lp_encode_windows(iq_ctx* ctx, const LpGeo& g, const float* w, const double* ii1,
                          const double* ii2, Dim3 img, Dim3 dist, const int* lo, const int* hi,
-                         __nv_bfloat16* out, float* norm);
+                         __nv_bfloat16* out, float* norm, const int64_t* pos = nullptr,
+                         int64_t npos = 0);
+// One column of the proposal's pick: tile `tile` of global realization `real`, with the mask's
+// offsets and the simulation grid at the tile.
+struct LpColumn {
+  const uint32_t* klist;
+  int K;
+  int32_t pad_;
+  const float* tmpl;
+  int64_t tgx, tgxy;
+  int64_t tile, real;
+};
+int iq_lp_shortlist(iq_ctx* ctx, const __nv_bfloat16* W, const float* nW, int64_t P,
+                    const __nv_bfloat16* T, const float* nT, int N, int64_t k, float* tau,
+                    int32_t* list, int32_t* cnt, int cap);
+int iq_lp_pick(iq_ctx* ctx, const float* img, Dim3 imgd, Dim3 dist, const LpColumn* cols, int N,
+               const int32_t* list, const int32_t* cnt, int cap, float* dl, double tol,
+               uint64_t seed, int64_t* rind, int64_t* ncand, int maxK);
+int iq_lp_template_features(iq_ctx* ctx, const LpGeo& g, const float* grid, Dim3 gdims,
+                            const int64_t* tsrc, const int* tbox, int64_t n, float* out);
+int iq_lp_recall(iq_ctx* ctx, const float* img, Dim3 imgd, Dim3 dist, const LpColumn& col,
+                 const int32_t* list, const int32_t* cnt, int cap, double tol, float* Dbuf,
+                 unsigned* dmin, uint32_t* bits, unsigned long long* counters);
+void iq_lp_free(iq_ctx* ctx);
+// The proposal's part of one dependency-level chunk of iq_simulate (iq_proposal_host.cu):
+// columns = tiles of the chunk x realizations of the group.
+struct LpChunk {
+  int ncol;
+  const int* cfg;                // per column: mask configuration
+  const int32_t* lohi;           // per configuration: box lo[3], hi[3]
+  const uint32_t* d_klist;       // device: offsets of configuration c at c * T
+  const int* cfgK;               // per configuration: offsets of its mask
+  int64_t T;
+  const int64_t* tile;           // per column: tile index
+  const int64_t* start;          // per column: linear start of the tile in a realization's grid
+  const int64_t* real;           // per column: global realization index
+  const int* rloc;               // per column: realization within the group
+  const int* slot;               // per column: index into rind (step in chunk * R + realization)
+  const float* sim;              // simulation grids of the group (its first realization at 0)
+  int64_t sim_rstride;
+  Dim3 sim_dims, tile_dims, dist;
+  double tol;
+  uint64_t seed;
+  int64_t* d_rind;
+};
+// Whether iq_simulate may use the proposal for this call: parameters for the tile's shape,
+// integer-valued data whose FP32 direct sums are exact, no hard or soft data.
+bool iq_lp_applies(iq_ctx* ctx, Dim3 tile, int64_t maxK, bool data);
+// Runs the proposal for a chunk; *done = 1 when every column was picked (else the caller runs
+// the full scan for the chunk). Recall checks follow lp_monitor.
+int iq_lp_run_chunk(iq_ctx* ctx, const LpChunk& c, int64_t chunk_index, int* done);
+// Records training pairs from the full scan's picks of a chunk (when capturing).
+int iq_lp_capture(iq_ctx* ctx, const LpChunk& c, const int32_t* d_cand, const int64_t* d_ncand,
+                  int64_t P);
+// Resets the per-call statistics of the proposal (start of iq_simulate).
+void iq_lp_begin_call(iq_ctx* ctx);
+void iq_lp_count_full(iq_ctx* ctx, int64_t ncol);
+int iq_lp_capture_reserve(iq_ctx* ctx, int64_t n);
 int iq_lp_encode_templates(iq_ctx* ctx, const LpGeo& g, const float* w, const float* grid,
                            Dim3 gdims, const int64_t* tsrc, const int* tbox, int64_t n,
                            __nv_bfloat16* out, float* norm);

@@ -201,6 +201,7 @@ struct EncArgs {
   const int64_t* tsrc;
   int64_t gx, gxy;
   const int* tbox;       // per item: lo[3], hi[3] (nullable: lo/hi above)
+  const int64_t* pos;    // windows: per item the position (nullable: item i is position i)
   __nv_bfloat16* out;    // n x EMB
   float* norm;           // n: |e|^2 of the BF16 embedding
 };
@@ -223,7 +224,8 @@ __global__ void __launch_bounds__(LT) lp_encode_kernel(const EncArgs a) {
       if (a.tsrc) {
         template_cell(a.g, a.grid + a.tsrc[item], a.gx, a.gxy, lo, hi, cell, f);
       } else {
-        const int64_t z = item / a.dxy, r = item - z * a.dxy, y = r / a.dx, x = r - y * a.dx;
+        const int64_t q = a.pos ? a.pos[item] : item;
+        const int64_t z = q / a.dxy, r = q - z * a.dxy, y = r / a.dx, x = r - y * a.dx;
         window_cell(a.g, a.ii1, a.ii2, a.isx, a.isxy, x, y, z, lo, hi, cell, f);
       }
       for (int c = 0; c < NIN; ++c) X[c * a.g.ng + cell] = f[c];
@@ -276,9 +278,10 @@ static size_t enc_smem(const LpGeo& g) {
 
 int iq_lp_encode_windows(iq_ctx* ctx, const LpGeo& g, const float* w, const double* ii1,
                          const double* ii2, Dim3 img, Dim3 dist, const int* lo, const int* hi,
-                         __nv_bfloat16* out, float* norm) {
+                         __nv_bfloat16* out, float* norm, const int64_t* pos, int64_t npos) {
   EncArgs a{};
-  a.g = g; a.w = w; a.npar = g.npar; a.n = dist.vol();
+  a.g = g; a.w = w; a.npar = g.npar; a.n = pos ? npos : dist.vol();
+  a.pos = pos;
   a.ii1 = ii1; a.ii2 = ii2; a.isx = img.x + 1; a.isxy = (img.x + 1) * (img.y + 1);
   a.dx = dist.x; a.dxy = dist.x * dist.y;
   for (int d = 0; d < 3; ++d) { a.lo[d] = lo[d]; a.hi[d] = hi[d]; }
@@ -619,6 +622,267 @@ int iq_lp_adam(iq_ctx* ctx, float* p, const float* g, float* m, float* v, int n,
   const float c1 = 1.f - std::pow(b1, (float)step), c2 = 1.f - std::pow(b2, (float)step);
   lp_adam_kernel<<<(unsigned)((n + 255) / 256), 256, 0, ctx->stream>>>(p, g, m, v, n, lr, b1, b2, 1e-8f, c1, c2);
   iq_count(ctx);
+  IQ_CUDA_OK(cudaGetLastError());
+  return IQ_OK;
+}
+
+// =============================================================================================
+// Shortlist: sampled per-column threshold, then a tensor-core scan of every position
+// =============================================================================================
+namespace {
+
+constexpr int TAU_SAMPLES = 8192;  // positions sampled per column for its threshold
+
+__device__ __forceinline__ float bdot64(const __nv_bfloat16* x, const float* e) {
+  float acc = 0.f;
+  const __nv_bfloat162* x2 = reinterpret_cast<const __nv_bfloat162*>(x);
+#pragma unroll 8
+  for (int i = 0; i < EMB / 2; ++i) {
+    const float2 f = __bfloat1622float2(x2[i]);
+    acc = fmaf(f.x, e[2 * i], acc);
+    acc = fmaf(f.y, e[2 * i + 1], acc);
+  }
+  return acc;
+}
+
+// One CTA per column: scores of TAU_SAMPLES evenly spaced positions, sorted; tau = the m-th.
+__global__ void __launch_bounds__(1024) lp_tau_kernel(const __nv_bfloat16* __restrict__ W,
+                                                      const float* __restrict__ nW, int64_t P,
+                                                      const __nv_bfloat16* __restrict__ T,
+                                                      const float* __restrict__ nT, int m,
+                                                      float* tau) {
+  __shared__ float sc[TAU_SAMPLES];
+  __shared__ float e[EMB];
+  const int c = blockIdx.x;
+  for (int i = threadIdx.x; i < EMB; i += blockDim.x) e[i] = __bfloat162float(T[(int64_t)c * EMB + i]);
+  __syncthreads();
+  const int64_t stride = (P + TAU_SAMPLES - 1) / TAU_SAMPLES;
+  for (int i = threadIdx.x; i < TAU_SAMPLES; i += blockDim.x) {
+    const int64_t p = (int64_t)i * stride;
+    sc[i] = p < P ? nW[p] + nT[c] - 2.f * bdot64(W + p * EMB, e) : 3.4e38f;
+  }
+  __syncthreads();
+  for (int k = 2; k <= TAU_SAMPLES; k <<= 1)
+    for (int j = k >> 1; j > 0; j >>= 1) {
+      for (int i = threadIdx.x; i < TAU_SAMPLES; i += blockDim.x) {
+        const int l = i ^ j;
+        if (l > i) {
+          const float a = sc[i], b = sc[l];
+          if ((a > b) == ((i & k) == 0)) { sc[i] = b; sc[l] = a; }
+        }
+      }
+      __syncthreads();
+    }
+  if (threadIdx.x == 0) tau[c] = sc[min(m, TAU_SAMPLES) - 1];
+}
+
+__device__ __forceinline__ void mma_bf16(float* d, const uint32_t* a, uint32_t b0, uint32_t b1) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, "
+      "{%8,%9}, {%0,%1,%2,%3};\n"
+      : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
+// Scores of every position against 64 columns (blockIdx.y) with tensor-core MMAs (BF16 in, FP32
+// accumulation): s = |w|^2 + |e|^2 - 2 w.e; positions with s <= tau[col] are appended to the
+// column's list (cap entries; cnt keeps counting past it so that an overflow is seen).
+__global__ void __launch_bounds__(256) lp_scan_kernel(const __nv_bfloat16* __restrict__ W,
+                                                      const float* __restrict__ nW, int64_t P,
+                                                      const __nv_bfloat16* __restrict__ T,
+                                                      const float* __restrict__ nT,
+                                                      const float* __restrict__ tau, int N,
+                                                      int32_t* list, int32_t* cnt, int cap) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int gid = lane >> 2, tig = lane & 3;
+  const int n0 = blockIdx.y * 64;
+  uint32_t bf[8][4][2];
+  float ncol[8][2], tcol[8][2];
+#pragma unroll
+  for (int nt = 0; nt < 8; ++nt) {
+    const int c = n0 + nt * 8 + gid;
+    const bool ok = c < N;
+#pragma unroll
+    for (int ks = 0; ks < 4; ++ks) {
+      const uint32_t* src =
+          reinterpret_cast<const uint32_t*>(T + (int64_t)(ok ? c : 0) * EMB + ks * 16 + 2 * tig);
+      bf[nt][ks][0] = ok ? src[0] : 0u;
+      bf[nt][ks][1] = ok ? src[4] : 0u;
+    }
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      const int cc = n0 + nt * 8 + 2 * tig + h;
+      ncol[nt][h] = cc < N ? nT[cc] : 0.f;
+      tcol[nt][h] = cc < N ? tau[cc] : -1.f;
+    }
+  }
+  const int64_t nblk = (P + 15) / 16;
+  for (int64_t blk = (int64_t)blockIdx.x * 8 + warp; blk < nblk; blk += (int64_t)gridDim.x * 8) {
+    const int64_t p0 = blk * 16;
+    const int64_t r0 = p0 + gid, r1 = p0 + gid + 8;
+    const int64_t q0 = r0 < P ? r0 : P - 1, q1 = r1 < P ? r1 : P - 1;
+    uint32_t af[4][4];
+#pragma unroll
+    for (int ks = 0; ks < 4; ++ks) {
+      const uint32_t* x0 = reinterpret_cast<const uint32_t*>(W + q0 * EMB + ks * 16 + 2 * tig);
+      const uint32_t* x1 = reinterpret_cast<const uint32_t*>(W + q1 * EMB + ks * 16 + 2 * tig);
+      af[ks][0] = x0[0];
+      af[ks][1] = x1[0];
+      af[ks][2] = x0[4];
+      af[ks][3] = x1[4];
+    }
+    const float w0 = nW[q0], w1 = nW[q1];
+#pragma unroll
+    for (int nt = 0; nt < 8; ++nt) {
+      float acc[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+      for (int ks = 0; ks < 4; ++ks) mma_bf16(acc, af[ks], bf[nt][ks][0], bf[nt][ks][1]);
+#pragma unroll
+      for (int e = 0; e < 4; ++e) {
+        const int h = e & 1;
+        const int64_t row = e < 2 ? r0 : r1;
+        const float s = (e < 2 ? w0 : w1) + ncol[nt][h] - 2.f * acc[e];
+        if (row < P && s <= tcol[nt][h]) {
+          const int c = n0 + nt * 8 + 2 * tig + h;
+          const int idx = atomicAdd(cnt + c, 1);
+          if (idx < cap) list[(int64_t)c * cap + idx] = (int32_t)row;
+        }
+      }
+    }
+  }
+}
+
+__global__ void lp_template_features_kernel(LpGeo g, const float* grid, const int64_t* tsrc,
+                                            const int* tbox, int64_t gx, int64_t gxy, int64_t n,
+                                            float* out) {
+  for (int64_t item = blockIdx.x; item < n; item += gridDim.x) {
+    int lo[3], hi[3];
+    for (int d = 0; d < 3; ++d) { lo[d] = tbox[6 * item + d]; hi[d] = tbox[6 * item + 3 + d]; }
+    for (int cell = threadIdx.x; cell < g.ng; cell += blockDim.x) {
+      float f[3];
+      template_cell(g, grid + tsrc[item], gx, gxy, lo, hi, cell, f);
+      for (int c = 0; c < NIN; ++c) out[item * NIN * g.ng + c * g.ng + cell] = f[c];
+    }
+  }
+}
+
+// Exact (integer data) distance of one column at every position, and its minimum (the monitor).
+__global__ void __launch_bounds__(256) lp_full_kernel(const float* __restrict__ img, int64_t isx,
+                                                      int64_t isxy, int64_t dx, int64_t dxy,
+                                                      int64_t P, LpColumn col, float* D,
+                                                      unsigned* dmin) {
+  extern __shared__ __align__(16) unsigned char dyn[];
+  int32_t* off = reinterpret_cast<int32_t*>(dyn);
+  float* tv = reinterpret_cast<float*>(dyn + 4 * (size_t)col.K);
+  for (int j = threadIdx.x; j < col.K; j += blockDim.x) {
+    const uint32_t k = col.klist[j];
+    const int kx = kx_of(k), ky = ky_of(k), kz = kz_of(k);
+    off[j] = (int32_t)(kx + isx * ky + isxy * kz);
+    tv[j] = col.tmpl[kx + col.tgx * ky + col.tgxy * kz];
+  }
+  __syncthreads();
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  unsigned mn = 0x7F800000u;
+  for (int64_t p = (int64_t)blockIdx.x * 8 + warp; p < P; p += (int64_t)gridDim.x * 8) {
+    const int64_t z = p / dxy, r = p - z * dxy, y = r / dx, x = r - y * dx;
+    const float* base = img + x + isx * y + isxy * z;
+    float acc = 0.f;
+    for (int j = lane; j < col.K; j += 32) {
+      const float d = base[off[j]] - tv[j];
+      acc = fmaf(d, d, acc);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if (lane == 0) D[p] = acc;
+    mn = min(mn, __float_as_uint(acc));
+  }
+  if (lane == 0) atomicMin(dmin, mn);
+}
+
+__global__ void lp_mark_kernel(const int32_t* list, const int32_t* cnt, int cap, uint32_t* bits) {
+  const int n = min(*cnt, cap);
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    atomicOr(bits + (list[i] >> 5), 1u << (list[i] & 31));
+}
+
+// counters[0] += |{D <= (1 + tol) min D}|, counters[1] += those in the shortlist
+__global__ void lp_recall_kernel(const float* D, const unsigned* dmin, int64_t P, double tol,
+                                 const uint32_t* bits, unsigned long long* counters) {
+  const double thr = __dmul_rn(__dadd_rn(1.0, tol), (double)__uint_as_float(*dmin));
+  unsigned long long t = 0, h = 0;
+  for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < P;
+       p += (int64_t)gridDim.x * blockDim.x) {
+    if ((double)D[p] <= thr) {
+      t++;
+      if (bits[p >> 5] >> (p & 31) & 1u) h++;
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    t += __shfl_xor_sync(0xffffffffu, t, o);
+    h += __shfl_xor_sync(0xffffffffu, h, o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    atomicAdd(counters, t);
+    atomicAdd(counters + 1, h);
+  }
+}
+
+}  // namespace
+
+int iq_lp_shortlist(iq_ctx* ctx, const __nv_bfloat16* W, const float* nW, int64_t P,
+                    const __nv_bfloat16* T, const float* nT, int N, int64_t k, float* tau,
+                    int32_t* list, int32_t* cnt, int cap) {
+  if (N <= 0) return IQ_OK;
+  const int64_t stride = (P + TAU_SAMPLES - 1) / TAU_SAMPLES;
+  // the m-th smallest sampled score stands for about m * stride positions
+  const int m = (int)std::max<int64_t>(4, std::min<int64_t>(TAU_SAMPLES, (k + stride - 1) / stride));
+  cudaStream_t st = ctx->stream;
+  iq_timer_start(ctx, "lp.scan");
+  lp_tau_kernel<<<(unsigned)N, 1024, 0, st>>>(W, nW, P, T, nT, m, tau);
+  IQ_CUDA_OK(cudaGetLastError());
+  IQ_CUDA_OK(cudaMemsetAsync(cnt, 0, sizeof(int32_t) * N, st));
+  int dev = 0, nsm = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  const int ncb = (N + 63) / 64;
+  const int64_t nblk = (P + 15) / 16;
+  const int64_t gx = std::max<int64_t>(1, std::min<int64_t>((nblk + 7) / 8, (int64_t)nsm * 8 / ncb + 1));
+  lp_scan_kernel<<<dim3((unsigned)gx, (unsigned)ncb), 256, 0, st>>>(W, nW, P, T, nT, tau, N, list,
+                                                                    cnt, cap);
+  iq_timer_stop(ctx, "lp.scan", 2.0 * (double)P * N * EMB);
+  iq_count(ctx, 2);
+  IQ_CUDA_OK(cudaGetLastError());
+  return IQ_OK;
+}
+
+int iq_lp_template_features(iq_ctx* ctx, const LpGeo& g, const float* grid, Dim3 gdims,
+                            const int64_t* tsrc, const int* tbox, int64_t n, float* out) {
+  if (n <= 0) return IQ_OK;
+  lp_template_features_kernel<<<(unsigned)std::min<int64_t>(n, 4096), LT, 0, ctx->stream>>>(
+      g, grid, tsrc, tbox, gdims.x, gdims.x * gdims.y, n, out);
+  iq_count(ctx);
+  IQ_CUDA_OK(cudaGetLastError());
+  return IQ_OK;
+}
+
+int iq_lp_recall(iq_ctx* ctx, const float* img, Dim3 imgd, Dim3 dist, const LpColumn& col,
+                 const int32_t* list, const int32_t* cnt, int cap, double tol, float* Dbuf,
+                 unsigned* dmin, uint32_t* bits, unsigned long long* counters) {
+  const int64_t P = dist.vol();
+  const size_t sm = (size_t)8 * col.K + 16;
+  if (sm > 227 * 1024) return iq_set_error(IQ_ERR_LIMIT, "recall check: mask too large");
+  IQ_CUDA_OK(cudaFuncSetAttribute(lp_full_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+  const unsigned inf = 0x7F800000u;
+  IQ_CUDA_OK(cudaMemcpyAsync(dmin, &inf, sizeof(unsigned), cudaMemcpyHostToDevice, ctx->stream));
+  IQ_CUDA_OK(cudaMemsetAsync(bits, 0, sizeof(uint32_t) * ((P + 31) / 32), ctx->stream));
+  iq_timer_start(ctx, "lp.monitor");
+  lp_full_kernel<<<(unsigned)std::min<int64_t>((P + 7) / 8, 152 * 8), 256, sm, ctx->stream>>>(
+      img, imgd.x, imgd.x * imgd.y, dist.x, dist.x * dist.y, P, col, Dbuf, dmin);
+  lp_mark_kernel<<<64, 256, 0, ctx->stream>>>(list, cnt, cap, bits);
+  lp_recall_kernel<<<(unsigned)std::min<int64_t>((P + 255) / 256, 1024), 256, 0, ctx->stream>>>(
+      Dbuf, dmin, P, tol, bits, counters);
+  iq_timer_stop(ctx, "lp.monitor");
+  iq_count(ctx, 3);
   IQ_CUDA_OK(cudaGetLastError());
   return IQ_OK;
 }

@@ -580,6 +580,7 @@ extern "C" int iq_simulate(iq_ctx* ctx, const iq_sim_params* p, const iq_hard_da
   IQ_CUDA_OK(cudaMemcpyAsync(d_hkv, hkv.data(), sizeof(float) * hkv.size(), cudaMemcpyHostToDevice, st));
   IQ_CUDA_OK(cudaMemsetAsync(ctx->d_status, 0, sizeof(int), st));
   IQ_CUDA_OK(cudaMemsetAsync(ctx->d_ties, 0, sizeof(unsigned long long), st));
+  iq_lp_begin_call(ctx);
   // ---- tensor-core launches: union stage lists keyed by their set of masks ----
   // Mask configuration c < ncfg is "tile minus [lo, hi)"; c == ncfg is the full tile.
   auto cfg_box = [&](int c) {
@@ -1041,6 +1042,21 @@ extern "C" int iq_simulate(iq_ctx* ctx, const iq_sim_params* p, const iq_hard_da
   }
 
   // ---- the tile loop (src/iqsim.jl:172-285), one dependency level chunk at a time ----
+  // the learned proposal: applies to integer-valued data without hard or soft data
+  int64_t maxK = 0;
+  for (const MaskCfg& mc : cfgs) maxK = std::max<int64_t>(maxK, mc.K);
+  const bool lp_on = iq_lp_applies(ctx, tileD, maxK, nh > 0 || nsoft > 0);
+  const bool lp_cap = ctx->lp_capture > 0 && ctx->lp != nullptr;
+  std::vector<int32_t> lc_lohi(6 * std::max(ncfg, 1)), lc_cfgK(std::max(ncfg, 1));
+  for (int cf = 0; cf < ncfg; ++cf) {
+    for (int d = 0; d < 3; ++d) {
+      lc_lohi[6 * cf + d] = (int32_t)cfgs[cf].lo[d];
+      lc_lohi[6 * cf + 3 + d] = (int32_t)cfgs[cf].hi[d];
+    }
+    lc_cfgK[cf] = cfgs[cf].K;
+  }
+  std::vector<int> lc_cfg, lc_rloc, lc_slot;
+  std::vector<int64_t> lc_tile, lc_start, lc_real;
   cudaStream_t gstream[2] = {st, st};
   if (ngrp == 2) {
     if (!ctx->stream2) IQ_CUDA_OK(cudaStreamCreateWithFlags(&ctx->stream2, cudaStreamNonBlocking));
@@ -1072,6 +1088,30 @@ extern "C" int iq_simulate(iq_ctx* ctx, const iq_sim_params* p, const iq_hard_da
         float* sim = d_sim + (size_t)r0 * padvol;
         int64_t* rind = d_rind + grp_rind(grp);
         uint8_t* cutbuf = d_cutbuf + grp_rind(grp) * 6 * slabmax;
+        // The learned proposal: picks from shortlists instead of the full scan, where it applies.
+        // Columns of the chunk in pick-CTA order: step i of the chunk, realization r of the group.
+        const int ncol = m * Rg;
+        if (lp_on || lp_cap) {
+          lc_cfg.resize(ncol); lc_tile.resize(ncol); lc_start.resize(ncol); lc_real.resize(ncol);
+          lc_rloc.resize(ncol); lc_slot.resize(ncol);
+          for (int i = 0; i < m; ++i)
+            for (int r = 0; r < Rg; ++r) {
+              const Step& s = steps[k0 + i];
+              const int col = i * Rg + r;
+              lc_cfg[col] = s.cfg; lc_tile[col] = s.tile; lc_start[col] = s.startlin;
+              lc_real[col] = p->real0 + r0 + r; lc_rloc[col] = r; lc_slot[col] = col;
+            }
+        }
+        LpChunk lc{};
+        lc.ncol = ncol; lc.cfg = lc_cfg.data(); lc.lohi = lc_lohi.data(); lc.d_klist = d_kl;
+        lc.cfgK = lc_cfgK.data(); lc.T = T; lc.tile = lc_tile.data(); lc.start = lc_start.data();
+        lc.real = lc_real.data(); lc.rloc = lc_rloc.data(); lc.slot = lc_slot.data();
+        lc.sim = sim; lc.sim_rstride = padvol; lc.sim_dims = padD; lc.tile_dims = tileD;
+        lc.dist = distD; lc.tol = p->tol; lc.seed = p->seed; lc.d_rind = rind;
+        int lp_done = 0;
+        if (lp_on) RET_IF(iq_lp_run_chunk(ctx, lc, c, &lp_done));
+        if (!lp_done) {
+        iq_lp_count_full(ctx, ncol);
         // overlap distance of every realization of the group for every tile of the chunk
         GatherLaunch G;
         G.grid = sim; G.grid_dims = padD; G.grid_stride = padvol; G.ntmpl = Rg;
@@ -1107,6 +1147,8 @@ extern "C" int iq_simulate(iq_ctx* ctx, const iq_sim_params* p, const iq_hard_da
         L.rind = rind; L.ncand = d_ncand + grp_rind(grp); L.status = ctx->d_status;
         L.stats = ctx->prof ? ctx->d_stats : nullptr;
         RET_IF(iq_launch_pick(ctx, L));
+        if (lp_cap) RET_IF(iq_lp_capture(ctx, lc, L.cand, L.ncand, P));
+        }  // full scan
         // boundary cuts
         if (cslab[c] > 0) {
           CutLaunch K;

@@ -212,6 +212,47 @@ int64_t iq_ctx_launches(iq_ctx* ctx);
  */
 int iq_set_option(iq_ctx* ctx, const char* name, int64_t value);
 
+/*
+ * Learned proposal (no counterpart in the reference, which scans every training-image position
+ * for every tile, src/iqsim.jl:206). A small 3-D convolutional encoder embeds a tile's masked
+ * overlap and every training-image window under the same mask in 64 dimensions; iq_simulate
+ * then evaluates the exact distance only at the ~lp.k positions whose embeddings lie nearest
+ * the tile's, and picks among them. It applies to integer-valued (categorical) training images
+ * without hard or soft data, for the tile shape the encoder was made for. Every lp.monitor-th
+ * chunk compares one shortlist with the full exact scan; once the sampled recall of the true
+ * candidate set falls below 0.99 the call continues with the full scan. Options:
+ *   "lp.enable"   1: use the proposal where it applies (default 0)
+ *   "lp.k"        shortlist length aimed at (default 4096)
+ *   "lp.monitor"  chunks between recall checks (default 16; 0: none)
+ *   "lp.fallback" 1 (default): switch to the full scan below 0.99 sampled recall; 0: keep the
+ *                 shortlists (to measure the recall of an encoder)
+ *   "lp.capture"  capacity of training pairs recorded by iq_simulate's full-scan picks
+ *                 (template features + 8 of its exact candidates); setting it clears them
+ */
+/* Fresh encoder parameters (Philox-seeded He initialization) for tiles of this shape. */
+int iq_lp_init(iq_ctx* ctx, int32_t ndim, const int64_t* tilesize, uint64_t seed);
+/* Copy the FP32 parameters out (n receives their count; out may be NULL to query it). */
+int iq_lp_params(iq_ctx* ctx, float* out, int64_t cap, int64_t* n);
+/* Set the parameters (trained elsewhere) for tiles of this shape. */
+int iq_lp_set_params(iq_ctx* ctx, int32_t ndim, const int64_t* tilesize, const float* in,
+                     int64_t n);
+/* Window embeddings (n x 64 floats) of the resident TI at `positions` under the mask
+ * "tile minus box" (box: lo[3], hi[3]). */
+int iq_lp_embed(iq_ctx* ctx, int64_t n, const int64_t* positions, const int32_t* box,
+                float* out);
+/* Loss and parameter gradients of one InfoNCE batch (no update): nA anchors by their cell
+ * features, one positive and nneg negatives per anchor by their positions, mask box `box`. */
+int iq_lp_loss_grad(iq_ctx* ctx, int32_t nA, int32_t nneg, const float* anchor_feats,
+                    const int64_t* pos_positions, const int64_t* neg_positions,
+                    const int32_t* box, double temp, double* loss, float* grad);
+/* Train on the captured pairs: `steps` Adam steps of `batch` anchors, `nneg` random negatives. */
+int iq_lp_train(iq_ctx* ctx, int32_t steps, int32_t batch, int32_t nneg, double lr, double temp,
+                uint64_t seed, double* loss_first, double* loss_last);
+/* Statistics of the last iq_simulate (n >= 9): columns from shortlists, columns of the full
+ * scan, monitored columns, their exact candidates, those shortlisted, sampled recall (-1: none),
+ * fell back (1/0), mean shortlist length, captured training pairs. */
+int iq_lp_stats(iq_ctx* ctx, double* out, int32_t n);
+
 #ifdef __cplusplus
 }
 #endif
