@@ -121,7 +121,7 @@ enum IqSlot {
   S_PICK_RV, S_PICK_RR, S_PICK_RL, S_SOFTB2,
   S_PB_RV, S_PB_RR, S_PB_RL, S_PB_LIST, S_PB_K, S_PB_OUT, S_PB_POOL, S_PB_SRC,
   S_LP_T, S_LP_NT, S_LP_TAU, S_LP_LIST, S_LP_CNT, S_LP_DL, S_LP_COLS, S_LP_TSRC, S_LP_TBOX,
-  S_LP_RIND, S_LP_NCAND, S_LP_D, S_LP_BITS, S_LP_ITEMS, S_LP_X, S_LP_E, S_LP_GE, S_LP_FEAT,
+  S_LP_RIND, S_LP_NCAND, S_LP_D, S_LP_BITS, S_LP_ITEMS, S_LP_X, S_LP_E, S_LP_GE, S_LP_FEAT, S_LP_BH1, S_LP_BGZ1, S_LP_BH2,
   S_COUNT
 };
 

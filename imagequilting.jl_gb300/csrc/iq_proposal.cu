@@ -403,13 +403,22 @@ __device__ __forceinline__ int tap_out(const int* Gi, const int* Go, int j, int 
   return mx + Go[0] * (my + Go[1] * mz);
 }
 
-__global__ void __launch_bounds__(LT) lp_train_bwd_kernel(const TrainArgs a) {
+// Backward, phase 1 (one CTA per item): recompute the forward pass, then the gradients of the
+// pre-activations of every layer (zero where the ReLU was off): gz3, gz2, gz1. They and the
+// activations go to per-item buffers; phase 2 reduces them over the batch into the weight
+// gradients (no atomics).
+struct BwdBufs {
+  float* h1; float* gz1;   // [items][CH * G]
+  float* h2; float* gz2;   // [items][CH * G2]
+  float* h3; float* gz3;   // [items][CH * G3]
+};
+
+__global__ void __launch_bounds__(LT) lp_train_bwd_kernel(const TrainArgs a, const BwdBufs o) {
   extern __shared__ __align__(16) unsigned char smraw[];
   float* sm = reinterpret_cast<float*>(smraw);
   const LpGeo& g = a.g;
   const int G = g.ng, G2 = g.ng2, G3 = g.ng3, nf = g.nf;
   const float* w = a.w;
-  float* gr = a.grad;
   for (int64_t item = blockIdx.x; item < a.nitems; item += gridDim.x) {
     float* X = sm + SM_X;
     float* h1 = sm + SM_H1;
@@ -422,19 +431,11 @@ __global__ void __launch_bounds__(LT) lp_train_bwd_kernel(const TrainArgs a) {
     float* gf = sm + SB_GF;
     float* gz3 = sm + SB_GZ3;
     float* gh2 = sm + SB_GH2;
-    float* gh1 = sm + SB_GH1;
-    for (int o = threadIdx.x; o < EMB; o += blockDim.x) ge[o] = a.gE[item * EMB + o];
+    for (int i = threadIdx.x; i < EMB; i += blockDim.x) ge[i] = a.gE[item * EMB + i];
     __syncthreads();
-    // output layer
-    for (int i = threadIdx.x; i < EMB * nf; i += blockDim.x) {
-      const int o = i / nf, f = i - o * nf;
-      const int c = f % CH, m = f / CH;
-      atomicAdd(gr + LP_OFF_W4 + i, ge[o] * h3[c * G3 + m]);
-    }
-    for (int o = threadIdx.x; o < EMB; o += blockDim.x) atomicAdd(gr + g.off_b4 + o, ge[o]);
     for (int f = threadIdx.x; f < nf; f += blockDim.x) {
       float acc = 0.f;
-      for (int o = 0; o < EMB; ++o) acc = fmaf(w[LP_OFF_W4 + o * nf + f], ge[o], acc);
+      for (int oo = 0; oo < EMB; ++oo) acc = fmaf(w[LP_OFF_W4 + oo * nf + f], ge[oo], acc);
       gf[f] = acc;
     }
     __syncthreads();
@@ -443,22 +444,6 @@ __global__ void __launch_bounds__(LT) lp_train_bwd_kernel(const TrainArgs a) {
       gz3[i] = h3[i] > 0.f ? gf[c + CH * m] : 0.f;
     }
     __syncthreads();
-    // layer 3: weights and bias, then the gradient of h2 (masked by ReLU into gz2 in place)
-    for (int i = threadIdx.x; i < CH * CH * 27; i += blockDim.x) {
-      const int c = i / (CH * 27), rem = i - c * CH * 27, ci = rem / 27, t = rem - ci * 27;
-      float acc = 0.f;
-      for (int m = 0; m < G3; ++m) {
-        const int ox = m % g.g3[0], oy = (m / g.g3[0]) % g.g3[1], oz = m / (g.g3[0] * g.g3[1]);
-        const int src = tap_cell(g.g2, ox, oy, oz, t);
-        if (src >= 0) acc = fmaf(gz3[c * G3 + m], h2[ci * G2 + src], acc);
-      }
-      if (acc != 0.f) atomicAdd(gr + LP_OFF_W3 + i, acc);
-    }
-    for (int c = threadIdx.x; c < CH; c += blockDim.x) {
-      float acc = 0.f;
-      for (int m = 0; m < G3; ++m) acc += gz3[c * G3 + m];
-      atomicAdd(gr + LP_OFF_B3 + c, acc);
-    }
     for (int i = threadIdx.x; i < CH * G2; i += blockDim.x) {
       const int ci = i / G2, j = i - ci * G2;
       float acc = 0.f;
@@ -469,27 +454,10 @@ __global__ void __launch_bounds__(LT) lp_train_bwd_kernel(const TrainArgs a) {
           for (int c = 0; c < CH; ++c) acc = fmaf(w[LP_OFF_W3 + (c * CH + ci) * 27 + t], gz3[c * G3 + m], acc);
         }
       }
-      gh2[i] = acc;  // already d/dz2 (zero where the ReLU was off)
+      gh2[i] = acc;  // d/dz2
     }
     __syncthreads();
-    // layer 2
-    for (int i = threadIdx.x; i < CH * CH * 27; i += blockDim.x) {
-      const int c = i / (CH * 27), rem = i - c * CH * 27, ci = rem / 27, t = rem - ci * 27;
-      float acc = 0.f;
-      for (int m = 0; m < G2; ++m) {
-        const float gzm = gh2[c * G2 + m];
-        if (gzm == 0.f) continue;
-        const int ox = m % g.g2[0], oy = (m / g.g2[0]) % g.g2[1], oz = m / (g.g2[0] * g.g2[1]);
-        const int src = tap_cell(g.g, ox, oy, oz, t);
-        if (src >= 0) acc = fmaf(gzm, h1[ci * G + src], acc);
-      }
-      if (acc != 0.f) atomicAdd(gr + LP_OFF_W2 + i, acc);
-    }
-    for (int c = threadIdx.x; c < CH; c += blockDim.x) {
-      float acc = 0.f;
-      for (int m = 0; m < G2; ++m) acc += gh2[c * G2 + m];
-      atomicAdd(gr + LP_OFF_B2 + c, acc);
-    }
+    float* gz1 = o.gz1 + item * CH * G;
     for (int i = threadIdx.x; i < CH * G; i += blockDim.x) {
       const int ci = i / G, j = i - ci * G;
       float acc = 0.f;
@@ -500,22 +468,103 @@ __global__ void __launch_bounds__(LT) lp_train_bwd_kernel(const TrainArgs a) {
           for (int c = 0; c < CH; ++c) acc = fmaf(w[LP_OFF_W2 + (c * CH + ci) * 27 + t], gh2[c * G2 + m], acc);
         }
       }
-      gh1[i] = acc;  // d/dz1
+      gz1[i] = acc;  // d/dz1
+      o.h1[item * CH * G + i] = h1[i];
+    }
+    for (int i = threadIdx.x; i < CH * G2; i += blockDim.x) {
+      o.h2[item * CH * G2 + i] = h2[i];
+      o.gz2[item * CH * G2 + i] = gh2[i];
+    }
+    for (int i = threadIdx.x; i < CH * G3; i += blockDim.x) {
+      o.h3[item * CH * G3 + i] = h3[i];
+      o.gz3[item * CH * G3 + i] = gz3[i];
     }
     __syncthreads();
-    // layer 1
-    for (int i = threadIdx.x; i < CH * NIN; i += blockDim.x) {
-      const int c = i / NIN, ci = i - c * NIN;
-      float acc = 0.f;
-      for (int cell = 0; cell < G; ++cell) acc = fmaf(gh1[c * G + cell], X[ci * G + cell], acc);
-      atomicAdd(gr + LP_OFF_W1 + i, acc);
+  }
+}
+
+// Phase 2, convolution layers: CTA (tap t, output channel c); thread (input channel ci, part):
+// grad W[c][ci][t] = sum over items and output cells m of gz[c][m] * h_in[ci][tap(m, t)];
+// the bias gradient of c with tap 0.
+__global__ void lp_grad_conv_kernel(LpGeo g, int layer, const float* __restrict__ gz,
+                                    const float* __restrict__ hin, int64_t nitems, float* grad) {
+  __shared__ float red[8][CH];
+  __shared__ float bred[8];
+  const int t = blockIdx.x, c = blockIdx.y;
+  const int ci = threadIdx.x & 31, part = threadIdx.x >> 5;
+  const int* Gin = layer == 2 ? g.g : g.g2;
+  const int* Go = layer == 2 ? g.g2 : g.g3;
+  const int nin = layer == 2 ? g.ng : g.ng2;
+  const int nout = layer == 2 ? g.ng2 : g.ng3;
+  float acc = 0.f, bacc = 0.f;
+  for (int64_t item = part; item < nitems; item += 8) {
+    const float* gzi = gz + item * CH * nout + c * nout;
+    const float* hi = hin + item * CH * nin + ci * nin;
+    for (int m = 0; m < nout; ++m) {
+      const float gv = gzi[m];
+      if (t == 0 && ci == 0) bacc += gv;
+      if (gv == 0.f) continue;
+      const int ox = m % Go[0], oy = (m / Go[0]) % Go[1], oz = m / (Go[0] * Go[1]);
+      const int src = tap_cell(Gin, ox, oy, oz, t);
+      if (src >= 0) acc = fmaf(gv, hi[src], acc);
     }
-    for (int c = threadIdx.x; c < CH; c += blockDim.x) {
-      float acc = 0.f;
-      for (int cell = 0; cell < G; ++cell) acc += gh1[c * G + cell];
-      atomicAdd(gr + LP_OFF_B1 + c, acc);
+  }
+  red[part][ci] = acc;
+  if (ci == 0) bred[part] = bacc;
+  __syncthreads();
+  if (part == 0) {
+    float s = 0.f;
+    for (int q = 0; q < 8; ++q) s += red[q][ci];
+    const int woff = layer == 2 ? LP_OFF_W2 : LP_OFF_W3;
+    grad[woff + (c * CH + ci) * 27 + t] = s;
+    if (t == 0 && ci == 0) {
+      float bs = 0.f;
+      for (int q = 0; q < 8; ++q) bs += bred[q];
+      grad[(layer == 2 ? LP_OFF_B2 : LP_OFF_B3) + c] = bs;
     }
-    __syncthreads();
+  }
+}
+
+// Phase 2, first layer: CTA per channel c: grad W1[c][ci] = sum gz1[c][cell] X[ci][cell], bias.
+__global__ void lp_grad_w1_kernel(LpGeo g, const float* __restrict__ gz1, const float* __restrict__ X,
+                                  int64_t nitems, float* grad) {
+  __shared__ float red[4][LT];
+  const int c = blockIdx.x, G = g.ng;
+  float acc[4] = {0.f, 0.f, 0.f, 0.f};
+  for (int64_t i = threadIdx.x; i < nitems * G; i += blockDim.x) {
+    const int64_t item = i / G;
+    const int cell = (int)(i - item * G);
+    const float gv = gz1[item * CH * G + c * G + cell];
+    for (int q = 0; q < NIN; ++q) acc[q] = fmaf(gv, X[item * NIN * G + q * G + cell], acc[q]);
+    acc[3] += gv;
+  }
+  for (int q = 0; q < 4; ++q) red[q][threadIdx.x] = acc[q];
+  __syncthreads();
+  if (threadIdx.x < 4) {
+    float s = 0.f;
+    for (int i = 0; i < LT; ++i) s += red[threadIdx.x][i];
+    if (threadIdx.x < NIN) grad[LP_OFF_W1 + c * NIN + threadIdx.x] = s;
+    else grad[LP_OFF_B1 + c] = s;
+  }
+}
+
+// Phase 2, output layer: one thread per weight (and per bias): sums over the items.
+__global__ void lp_grad_w4_kernel(LpGeo g, const float* __restrict__ gE, const float* __restrict__ h3,
+                                  int64_t nitems, float* grad) {
+  const int nf = g.nf, G3 = g.ng3;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < EMB * nf) {
+    const int oo = i / nf, f = i - oo * nf;
+    const int c = f % CH, m = f / CH;
+    float acc = 0.f;
+    for (int64_t item = 0; item < nitems; ++item)
+      acc = fmaf(gE[item * EMB + oo], h3[item * CH * G3 + c * G3 + m], acc);
+    grad[LP_OFF_W4 + i] = acc;
+  } else if (i < EMB * nf + EMB) {
+    const int oo = i - EMB * nf;
+    float acc = 0.f;
+    for (int64_t item = 0; item < nitems; ++item) acc += gE[item * EMB + oo];
+    grad[g.off_b4 + oo] = acc;
   }
 }
 
@@ -606,10 +655,23 @@ int iq_lp_train_batch(iq_ctx* ctx, const LpGeo& g, const LpTrainBatch& B, double
   IQ_CUDA_OK(cudaMemsetAsync(B.loss, 0, sizeof(double), st));
   lp_loss_kernel<<<(unsigned)((B.nA + 7) / 8), 256, 0, st>>>(B.E, B.nA, B.nneg, B.temp, B.gE, B.loss);
   IQ_CUDA_OK(cudaGetLastError());
-  IQ_CUDA_OK(cudaMemsetAsync(B.grad, 0, sizeof(float) * g.npar, st));
-  lp_train_bwd_kernel<<<blocks, LT, smb, st>>>(a);
+  BwdBufs o;
+  const int64_t G = g.ng, G2 = g.ng2, G3 = g.ng3;
+  o.h1 = (float*)iq_scratch(ctx, S_LP_BH1, sizeof(float) * nitems * CH * G);
+  o.gz1 = (float*)iq_scratch(ctx, S_LP_BGZ1, sizeof(float) * nitems * CH * G);
+  o.h2 = (float*)iq_scratch(ctx, S_LP_BH2, sizeof(float) * nitems * CH * (G2 + G3) * 2);
+  if (!o.h1 || !o.gz1 || !o.h2) return IQ_ERR_ALLOC;
+  o.gz2 = o.h2 + nitems * CH * G2;
+  o.h3 = o.gz2 + nitems * CH * G2;
+  o.gz3 = o.h3 + nitems * CH * G3;
+  lp_train_bwd_kernel<<<blocks, LT, smb, st>>>(a, o);
   IQ_CUDA_OK(cudaGetLastError());
-  iq_count(ctx, 3);
+  lp_grad_conv_kernel<<<dim3(27, CH), LT, 0, st>>>(g, 2, o.gz2, o.h1, nitems, B.grad);
+  lp_grad_conv_kernel<<<dim3(27, CH), LT, 0, st>>>(g, 3, o.gz3, o.h2, nitems, B.grad);
+  lp_grad_w1_kernel<<<CH, LT, 0, st>>>(g, o.gz1, B.X, nitems, B.grad);
+  lp_grad_w4_kernel<<<(EMB * g.nf + EMB + 255) / 256, 256, 0, st>>>(g, B.gE, o.h3, nitems, B.grad);
+  IQ_CUDA_OK(cudaGetLastError());
+  iq_count(ctx, 7);
   if (loss_out) {
     IQ_CUDA_OK(cudaMemcpyAsync(loss_out, B.loss, sizeof(double), cudaMemcpyDeviceToHost, st));
     IQ_CUDA_OK(cudaStreamSynchronize(st));

@@ -389,3 +389,70 @@ def test_full_size_properties(iq, ctx):
     b = iq.iqsim(W["ti"], W["tilesize"], W["simsize"], **kw)
     for x, y in zip(a, b):
         assert np.array_equal(x, y)
+
+
+# ---- the cut cost clause on the GPU's masks (tests/cutcost.py) ----------------------------
+@pytest.mark.parametrize("shape,dim,kind", [((6, 24, 12), 0, "cont"), ((24, 24, 3), 2, "cont"),
+                                            ((6, 12, 5), 0, "cat")])
+def test_gpu_cut_is_a_minimum_cut_of_the_unquantized_graph(iq, ctx, shape, dim, kind):
+    import cutcost
+    rng = np.random.default_rng(18)
+    for trial in range(2):
+        if kind == "cont":
+            A = np.exp(rng.normal(size=shape)).astype(np.float32)
+            B = np.exp(rng.normal(size=shape)).astype(np.float32)
+        else:
+            A = rng.integers(0, 4, shape).astype(np.float32)
+            B = rng.integers(0, 4, shape).astype(np.float32)
+        M = iq.graphcut(A, B, dim, ctx=ctx)
+        cost = cutcost.cut_cost(A, B, M)
+        flow = cutcost.maxflow_value(A, B, dim)
+        big = max(c for _, _, c in cutcost.edges(A, B))
+        assert abs(cost - flow) <= max(1e-9 * flow, 1e-12 * big), (trial, cost, flow)
+
+
+# ---- the benchmark's configurations (bench.workload) ----------------------------------------
+def test_cfg1_full_size_bit_exact(iq, ctx):
+    """Config 1 in full (128x128 binary TI, 256x256 output, 100 tiles): realizations, boundary
+    cuts and voxel reuse equal to the oracle's."""
+    import bench
+    W = bench.workload("cfg1")
+    kw = dict(overlap=W["overlap"], tol=W["tol"], path=W["path"], nreal=2, debug=True)
+    g = iq.iqsim(W["ti"], W["tilesize"], W["simsize"], rng=3, ctx=ctx, **kw)
+    r = O.iqsim(W["ti"], W["tilesize"], W["simsize"], seed=3, **kw)
+    _same_reals(g[0], r[0])
+    _same_reals(g[1], r[1])
+    assert g[2] == r[2]
+
+
+def test_cfg3_sample_bit_exact(iq, ctx):
+    """Config 3's categorical workload (256x256x128 TI, 32x32x16 tiles, 5.7 M positions): the
+    first 10 tiles of the path for one realization equal the oracle's."""
+    import bench
+    W = bench.workload("cfg3")
+    steps = 10
+    ctx.set_option("sim.max_steps", steps)
+    try:
+        g = iq.iqsim(W["ti"], W["tilesize"], W["simsize"], overlap=W["overlap"], tol=W["tol"],
+                     path=W["path"], nreal=1, rng=8, ctx=ctx)
+    finally:
+        ctx.set_option("sim.max_steps", -1)
+    r = O.iqsim(W["ti"], W["tilesize"], W["simsize"], overlap=W["overlap"], tol=W["tol"],
+                path=W["path"], nreal=1, seed=8, max_steps=steps)
+    _same_reals(g, r)
+    assert np.count_nonzero(np.asarray(g[0])) > 0
+
+
+def test_cfg3_full_size_properties(iq, ctx):
+    """Config 3 at full size for two realizations: every voxel a TI value, identical calls
+    identical, realizations distinct (tests/props.py)."""
+    import bench
+    from props import check_realizations
+    W = bench.workload("cfg3")
+    kw = dict(overlap=W["overlap"], tol=W["tol"], path=W["path"], nreal=2, rng=4, ctx=ctx)
+    a = iq.iqsim(W["ti"], W["tilesize"], W["simsize"], **kw)
+    assert len(a) == 2 and a[0].shape == W["simsize"]
+    check_realizations(a, W["ti"], {})
+    b = iq.iqsim(W["ti"], W["tilesize"], W["simsize"], **kw)
+    for x, y in zip(a, b):
+        assert np.array_equal(x, y)

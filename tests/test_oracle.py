@@ -401,3 +401,24 @@ def test_count_ties_rules():
     ties = []
     O.threshold_pick(np.array([1.0, 1.1, 1.1 * (1 + 1e-7), 3.0]), 0.1, ties)
     assert ties == [2]
+
+
+# ---- the cut cost clause: equal cost with unquantized capacities (tests/cutcost.py) --------
+@pytest.mark.parametrize("shape,dim,kind", [((6, 20), 0, "cont"), ((6, 10, 8), 0, "cont"),
+                                            ((10, 8, 3), 2, "cont"), ((4, 9, 6), 0, "cat")])
+def test_quantized_cut_is_a_minimum_cut_of_the_unquantized_graph(shape, dim, kind):
+    import cutcost
+    rng = np.random.default_rng(17)
+    for trial in range(3):
+        if kind == "cont":
+            A = np.exp(rng.normal(size=shape)).astype(np.float32)
+            B = np.exp(rng.normal(size=shape)).astype(np.float32)
+        else:
+            A = rng.integers(0, 4, shape).astype(np.float32)
+            B = rng.integers(0, 4, shape).astype(np.float32)
+        M = O.graphcut(A, B, dim)
+        cost = cutcost.cut_cost(A, B, M)
+        flow = cutcost.maxflow_value(A, B, dim)
+        # quantization keeps 47 bits relative to the largest capacity
+        tol = 1e-9 if kind == "cont" else 1e-12 * max(c for _, _, c in cutcost.edges(A, B)) / max(flow, 1e-300)
+        assert abs(cost - flow) <= max(tol, 1e-9) * max(flow, 1e-300), (trial, cost, flow)
