@@ -277,6 +277,65 @@ def run_reference(args, W, dist, rank, world):
     print(json.dumps(line), flush=True)
 
 
+FORMS = {"plain": "plain: every training-image position scanned (tensor-core correlation, "
+                  "FP32-accurate split FP16/TF32 MMAs, exact re-rank near each decision)",
+         "proposal": "BF16 + learned proposal: a 3-D conv encoder (BF16 weights, FP32 "
+                     "accumulation) shortlists positions, the exact distance is summed there, "
+                     "full-scan fallback below 0.99 sampled recall"}
+
+
+def train_proposal(args, W, ctx, lib, _lib, p, hd, sd, out_d):
+    """Training pairs from full-scan runs (seeds 1..n, the first tiles of the path), then Adam
+    steps of the library's own forward and backward kernels. Returns what was done."""
+    import ctypes
+    t0 = time.perf_counter()
+    ctx.lp_init(W["tilesize"], seed=0)
+    ctx.set_option("lp.capture", args.lp_pairs)
+    nreal0, seed0 = p.nreal, p.seed
+    p.nreal = args.lp_capture_reals
+    ctx.set_option("sim.max_steps", args.lp_capture_steps)
+    for s in range(1, args.lp_seeds + 1):
+        p.seed = s
+        _lib.check(lib.iq_simulate(ctx.h, ctypes.byref(p), ctypes.byref(hd), len(W["soft"]),
+                                   sd if W["soft"] else None, out_d.data_ptr(), None, None))
+        if ctx.lp_stats()["captured"] >= args.lp_pairs:
+            break
+    ctx.set_option("sim.max_steps", -1)
+    p.nreal, p.seed = nreal0, seed0
+    pairs = int(ctx.lp_stats()["captured"])
+    t1 = time.perf_counter()
+    l0, l1 = ctx.lp_train(args.lp_train_steps, batch=128, nneg=32, lr=2e-3, temp=8.0, seed=7)
+    t2 = time.perf_counter()
+    ctx.set_option("lp.capture", 0)
+    return {"pairs": pairs, "capture_s": t1 - t0, "train_steps": args.lp_train_steps,
+            "train_s": t2 - t1, "loss_first": l0, "loss_last": l1,
+            "pairs_from": "full-scan runs, seeds 1..%d, first %d tiles x %d realizations" % (
+                args.lp_seeds, args.lp_capture_steps, args.lp_capture_reals)}
+
+
+def proposal_roofline(dom, prof, lp_kernels, W, peaks, peak_kind, st, args):
+    """Roofline of the proposal's dominant kernel: the scan against the measured tensor peak
+    (2 x positions x columns x 64 FLOPs per launch); the shortlist pick against HBM (4 bytes of
+    the training image read per shortlisted position and mask offset, the direct sums)."""
+    ms, n, work = prof[dom]
+    if dom == "lp.scan":
+        ach = work / (ms / 1e3) / 1e12
+        return {"bound": "tensor", "kernel": dom, "achieved": ach, "unit": "TFLOP/s",
+                "peak": peaks.get("bf16_tflops"), "peak_kind": "%s (bf16 dense, burst)" % peak_kind,
+                "frac": ach / peaks.get("bf16_tflops"), "traffic": None,
+                "flops_per_launch": work / n if n else None}
+    ovl = [math.ceil(o * t) for o, t in zip(W["overlap"], W["tilesize"])]
+    K = int(np.prod(W["tilesize"])) - int(np.prod([t - o for t, o in zip(W["tilesize"], ovl)]))
+    cols = st["cols_shortlist"] if st else 0
+    byts = cols * (st["mean_shortlist"] if st else 0) * K * 4.0
+    ach = byts / (ms / 1e3) / 1e9 if ms else None
+    return {"bound": "hbm", "kernel": dom, "achieved": ach, "unit": "GB/s",
+            "peak": peaks.get("hbm_gbs"), "peak_kind": "%s (copy)" % peak_kind,
+            "frac": ach / peaks.get("hbm_gbs") if ach else None, "traffic": None,
+            "bytes_note": "algorithmic bytes = shortlisted positions x interior mask offsets x 4 "
+                          "(the training-image values the direct sums read; L2-resident)"}
+
+
 def run_ours(args, W, dist, rank, world):
     import ctypes
 
@@ -361,6 +420,11 @@ def run_ours(args, W, dist, rank, world):
 
     # ---- resident arm ----
     _lib.check(lib.iq_set_ti(ctx.h, ti_h.ctypes.data, ti_dt, N, size))
+    lp_info = None
+    if args.form == "proposal":
+        lp_info = train_proposal(args, W, ctx, lib, _lib, p, hd_dev, sd_dev, out_d)
+        ctx.set_option("lp.enable", 1)
+        ctx.set_option("lp.k", args.lp_k)
     for i in range(args.warmup):
         step_resident(i)
     torch.cuda.synchronize()
@@ -403,9 +467,30 @@ def run_ours(args, W, dist, rank, world):
     counters["graphcut_cycles_per_cta"] = {k: (v[2] / v[1]) if v[1] else None for k, v in gc.items()}
     pk = {k: ctx.profile_get("pick." + k) for k in ("select_cycles", "weight_cycles", "draw_cycles")}
     counters["pick_cycles_per_cta"] = {k: (v[2] / v[1]) if v[1] else None for k, v in pk.items()}
+    lp_stats = ctx.lp_stats() if args.form == "proposal" else None
+    lp_kernels = {k: ctx.profile_get(k) for k in ("lp.encode", "lp.scan", "lp.pick", "lp.monitor")} \
+        if args.form == "proposal" else {}
     ctx.profile(False)
     ms_max = reduce_max(dist, ms)
     barrier(dist)
+    plain = None
+    if args.form == "proposal" and not args.no_plain:
+        # the full-scan form on the same workload, for the comparison the metric names
+        ctx.set_option("lp.enable", 0)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        ep0 = torch.cuda.Event(enable_timing=True)
+        ep1 = torch.cuda.Event(enable_timing=True)
+        ep0.record(stream)
+        for i in range(args.plain_steps):
+            step_resident(10000 + i)
+        ep1.record(stream)
+        torch.cuda.synchronize()
+        ms_plain = max(ep0.elapsed_time(ep1), (time.perf_counter() - t0) * 1e3) / args.plain_steps
+        plain = {"value": voxels * world / (ms_plain / 1e3), "unit": "voxels/s",
+                 "ms_per_step": ms_plain, "steps": args.plain_steps}
+        ctx.set_option("lp.enable", 1)
+        barrier(dist)
 
     # ---- end-to-end arm (host buffers through the C ABI) ----
     if args.no_e2e:
@@ -434,6 +519,9 @@ def run_ours(args, W, dist, rank, world):
     value = aggregate_rate(voxels, args.steps, world, ms_max)
     e2e_value = aggregate_rate(voxels, args.steps, world, ms_e2e_max)
     peaks, peak_kind = measured_peaks()
+    for k, v in lp_kernels.items():
+        if v[1]:
+            prof[k] = v
     shares = {k: v[0] for k, v in prof.items()}
     dom = max(shares, key=lambda k: shares[k])
     corr_ms, corr_n, corr_flops = prof["corr"]
@@ -482,7 +570,7 @@ def run_ours(args, W, dist, rank, world):
                        "l2": "working set > L2 (simulation grids %.0f MB%s)" % (
                            padvol * nreal * 4 / 1e6,
                            ", soft maps %.1f GB" % (soft_bytes / 1e9) if soft_bytes else ""),
-                       "form": "plain (FP32-accurate correlation as split FP16/TF32 MMAs on the tensor cores)"},
+                       "form": FORMS[args.form]},
             "roofline": roof, "dominant_kernel": dom, "kernels": kernel_share,
             "counters": counters,
             "cpu_baseline": cpu,
@@ -490,6 +578,15 @@ def run_ours(args, W, dist, rank, world):
                    {"value": e2e_value, "unit": "voxels/s", "h2d_bytes_per_step": int(h2d),
                     "d2h_bytes_per_step": int(d2h), "ms_per_step": ms_e2e_max / args.steps},
             "clocks": clk, "gpu_launches": int(launches)}
+    if args.form == "proposal":
+        line["proposal"] = dict(lp_info or {}, **{"stats": lp_stats, "k": args.lp_k})
+        line["plain"] = plain
+        if plain:
+            line["proposal"]["speedup_vs_plain"] = value / plain["value"]
+        if dom in lp_kernels:
+            line["roofline"] = proposal_roofline(dom, prof, lp_kernels, W, peaks, peak_kind,
+                                                 lp_stats, args)
+            line["dominant_kernel"] = dom
     print(json.dumps(line), flush=True)
     ctx.close()
 
@@ -501,6 +598,17 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="cfg2", choices=["cfg2", "cfg1", "cfg3", "cfg4"])
+    ap.add_argument("--form", default=None, choices=["plain", "proposal"],
+                    help="plain full scan, or the learned proposal (default: the proposal for "
+                         "the categorical configurations 3 and 4, plain otherwise)")
+    ap.add_argument("--lp-k", type=int, default=4096, help="shortlist length of the proposal")
+    ap.add_argument("--lp-pairs", type=int, default=200000, help="training pairs to capture")
+    ap.add_argument("--lp-seeds", type=int, default=50)
+    ap.add_argument("--lp-capture-steps", type=int, default=1500)
+    ap.add_argument("--lp-capture-reals", type=int, default=2)
+    ap.add_argument("--lp-train-steps", type=int, default=1500)
+    ap.add_argument("--plain-steps", type=int, default=1)
+    ap.add_argument("--no-plain", action="store_true", help="skip the full-scan comparison step")
     ap.add_argument("--cpu-budget", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer arm")
@@ -509,6 +617,8 @@ def main():
     args = ap.parse_args()
     dist, rank, world = dist_setup()
     W = workload(args.workload)
+    if args.form is None:
+        args.form = "proposal" if args.workload in ("cfg3", "cfg4") else "plain"
     if args.impl == "reference":
         run_reference(args, W, dist, rank, world)
     else:

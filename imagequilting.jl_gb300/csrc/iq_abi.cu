@@ -349,11 +349,16 @@ extern "C" int iq_set_ti(iq_ctx* ctx, const void* ti, int32_t dtype, int32_t ndi
     IQ_CUDA_OK(cudaMemcpyAsync(tmp, ti, sizeof(double) * n, cudaMemcpyDefault, ctx->stream));
     if ((rc = iq_launch_to_f32(ctx, tmp, ctx->d_ti, n))) return rc;
   }
-  if ((rc = iq_launch_prepare(ctx, ctx->d_ti, n, nanm))) return rc;
+  unsigned long long* dhash = (unsigned long long*)iq_scratch(ctx, S_TIHASH, 2 * sizeof(int64_t));
+  if (!dhash) return IQ_ERR_ALLOC;
+  IQ_CUDA_OK(cudaMemsetAsync(dhash, 0, sizeof(unsigned long long), ctx->stream));
+  if ((rc = iq_launch_prepare(ctx, ctx->d_ti, n, nanm, dhash))) return rc;
   if ((rc = iq_build_integrals(ctx, ctx->d_ti, d, ctx->d_ti2ii, ctx->d_nanii, nanm))) return rc;
   int32_t total = 0;
+  unsigned long long hash = 0;
   IQ_CUDA_OK(cudaMemcpyAsync(&total, ctx->d_nanii + (d.x + 1) * (d.y + 1) * (d.z + 1) - 1,
                              sizeof(int32_t), cudaMemcpyDeviceToHost, ctx->stream));
+  IQ_CUDA_OK(cudaMemcpyAsync(&hash, dhash, sizeof(hash), cudaMemcpyDeviceToHost, ctx->stream));
   IQ_CUDA_OK(cudaStreamSynchronize(ctx->stream));
   IqValueStats st;
   if ((rc = iq_value_stats(ctx, ctx->d_ti, n, st))) return rc;
@@ -362,7 +367,10 @@ extern "C" int iq_set_ti(iq_ctx* ctx, const void* ti, int32_t dtype, int32_t ndi
   ctx->ti_nan = total;
   ctx->ti_stats = st;
   ctx->has_ti = true;
-  ctx->ti_version += 1;
+  hash ^= (unsigned long long)d.x * 0x100000001B3ull ^ (unsigned long long)d.y << 21 ^
+          (unsigned long long)d.z << 42 ^ (unsigned long long)ndim << 60;
+  if (!same || hash != ctx->ti_hash || ctx->ti_version == 0) ctx->ti_version += 1;
+  ctx->ti_hash = hash;
   return IQ_OK;
 }
 

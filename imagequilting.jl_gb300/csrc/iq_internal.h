@@ -93,7 +93,9 @@ struct iq_ctx {
   int64_t lp_capture = 0;          // training pairs iq_simulate records (0: none)
   int lp_monitor = 16;             // every lp_monitor-th proposal chunk checks its recall
   int lp_fallback = 1;             // 0: keep the shortlists even below 0.99 recall (measuring)
-  int64_t ti_version = 0;          // bumped by every iq_set_ti (keys the proposal's caches)
+  int64_t ti_version = 0;          // bumped by every iq_set_ti whose content differs from the
+                                   // resident image's (keys the proposal's caches)
+  unsigned long long ti_hash = 0;  // content key of the resident image (values and extents)
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
 };
 enum IqStat { ST_CUT_ROUNDS = 0, ST_CUT_LEVELS, ST_CUT_CTAS, ST_PICK_ITERS, ST_PICK_CAND,
@@ -117,11 +119,12 @@ enum IqSlot {
   S_SIM = 0, S_CUT, S_D, S_DHARD, S_SOFT, S_TV, S_B2, S_KLIST, S_MINMAX, S_PICK_CAND,
   S_PICK_K0, S_PICK_V0, S_PICK_K1, S_PICK_V1, S_PICK_W, S_PICK_PROD, S_RIND, S_NCAND,
   S_CUTBUF, S_CUTSCR, S_DIS, S_AUX, S_AUXTI, S_AUXII, S_HARDLIST, S_HARDPTS, S_OUT,
-  S_TMP0, S_TMP1, S_TMP2, S_STARTS, S_SOFTMM, S_TASKS, S_VOX, S_TCB, S_TCCOLS, S_TCSTAGE, S_TCB2, S_TCFLAG, S_TCSOFT, S_SOFTKEYS,
+  S_TMP0, S_TMP1, S_TMP2, S_TIHASH, S_STARTS, S_SOFTMM, S_TASKS, S_VOX, S_TCB, S_TCCOLS, S_TCSTAGE, S_TCB2, S_TCFLAG, S_TCSOFT, S_SOFTKEYS,
   S_PICK_RV, S_PICK_RR, S_PICK_RL, S_SOFTB2,
   S_PB_RV, S_PB_RR, S_PB_RL, S_PB_LIST, S_PB_K, S_PB_OUT, S_PB_POOL, S_PB_SRC,
+  S_PBH_OUT, S_PBH_POOL, S_PBH_SRC,
   S_LP_T, S_LP_NT, S_LP_TAU, S_LP_LIST, S_LP_CNT, S_LP_DL, S_LP_COLS, S_LP_TSRC, S_LP_TBOX,
-  S_LP_RIND, S_LP_NCAND, S_LP_D, S_LP_BITS, S_LP_ITEMS, S_LP_X, S_LP_E, S_LP_GE, S_LP_FEAT, S_LP_BH1, S_LP_BGZ1, S_LP_BH2,
+  S_LP_RIND, S_LP_NCAND, S_LP_D, S_LP_BITS, S_LP_ITEMS, S_LP_X, S_LP_E, S_LP_GE, S_LP_FEAT, S_LP_BH1, S_LP_BGZ1, S_LP_BH2, S_LP_DENSE,
   S_COUNT
 };
 
@@ -313,7 +316,8 @@ struct PreBand {
   int64_t off, n;
   unsigned long long key;   // the FP32 (value, index) key of the selection
   long long ties;           // near-ties at its boundary (the boundary position excluded)
-  int32_t ok;               // 0: not precomputed (the pick selects itself)
+  int32_t ok;               // 0: not precomputed (the pick selects itself); 1: band; 2: the
+                            // map is exact and the key alone decides
   int32_t pad_;
 };
 
@@ -330,6 +334,8 @@ struct PickTask {
   // of the normal softdbsize sequence (sources shared by all realizations; nullable)
   const unsigned long long* aux_keys[IQ_MAX_AUX];
   const PreBand* aux_pb[IQ_MAX_AUX];        // refined selections of shared maps (nullable)
+  const PreBand* x0_pb;                     // D's dbsize selection, shared (nullable)
+  const int32_t* x0_pool;                   // its band list
   const int32_t* pb_pool;                   // their band lists
   int nkeys;
   int64_t tile;                             // Philox counter of the draw
@@ -388,7 +394,7 @@ int iq_launch_select_keys(iq_ctx* ctx, const float* maps, const unsigned* mm, in
 int iq_launch_select_bands(iq_ctx* ctx, const float* maps, const unsigned* mm,
                            const ExactSrc* srcs, int64_t nmaps, int64_t P, int64_t dx,
                            int64_t dxy, const int64_t* seq, int nq, PreBand* out, int32_t* pool,
-                           int64_t cap);
+                           int64_t cap, int keys_exact = 0);
 
 // ---------------------------------------------------------------------------------------
 // Graph cut (iq_graphcut.cu) and paste (iq_paste.cu)
@@ -456,7 +462,8 @@ int iq_launch_voxsum(iq_ctx* ctx, int nreal, const float* cut, int64_t n, int64_
                      double* out);
 int iq_launch_pad_symmetric(iq_ctx* ctx, const float* src, Dim3 src_dims, float* dst,
                             Dim3 dst_dims);
-int iq_launch_prepare(iq_ctx* ctx, float* data, int64_t n, uint8_t* nanmask);
+int iq_launch_prepare(iq_ctx* ctx, float* data, int64_t n, uint8_t* nanmask,
+                      unsigned long long* hash = nullptr);
 int iq_launch_to_f32(iq_ctx* ctx, const double* src, float* dst, int64_t n);
 
 // ---------------------------------------------------------------------------------------
@@ -523,9 +530,16 @@ struct LpColumn {
   int64_t tgx, tgxy;
   int64_t tile, real;
 };
+#define IQ_LP_SAMPLES 8192  // positions sampled per column for its shortlist threshold
+// Rows i * ceil(P / IQ_LP_SAMPLES) of the window embeddings (the sampled positions).
+int iq_lp_sample_rows(iq_ctx* ctx, const __nv_bfloat16* W, const float* nW, int64_t P,
+                      __nv_bfloat16* Ws, float* nWs);
+// Shortlists of N columns: per column the threshold of about k positions from the sampled
+// rows' scores (dense: N x IQ_LP_SAMPLES scratch), then every position at or below it.
 int iq_lp_shortlist(iq_ctx* ctx, const __nv_bfloat16* W, const float* nW, int64_t P,
-                    const __nv_bfloat16* T, const float* nT, int N, int64_t k, float* tau,
-                    int32_t* list, int32_t* cnt, int cap);
+                    const __nv_bfloat16* Ws, const float* nWs, const __nv_bfloat16* T,
+                    const float* nT, int N, int64_t k, float* tau, float* dense, int32_t* list,
+                    int32_t* cnt, int cap);
 int iq_lp_pick(iq_ctx* ctx, const float* img, Dim3 imgd, Dim3 dist, const LpColumn* cols, int N,
                const int32_t* list, const int32_t* cnt, int cap, float* dl, double tol,
                uint64_t seed, int64_t* rind, int64_t* ncand, int maxK);

@@ -104,13 +104,29 @@ __global__ void pad_kernel(const float* src, int64_t sx, int64_t sy, int64_t sz,
   }
 }
 
-__global__ void prepare_kernel(float* data, int64_t n, uint8_t* nanmask) {
+// splitmix64 finalizer
+__device__ __forceinline__ unsigned long long mix64(unsigned long long z) {
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+
+// NaN -> 0 with the NaN mask; `hash` (nullable) accumulates sum_i mix64(bits_i + i * phi), a
+// content key of the values as given (independent of the summation order).
+__global__ void prepare_kernel(float* data, int64_t n, uint8_t* nanmask, unsigned long long* hash) {
+  unsigned long long h = 0;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x) {
     const float v = data[i];
+    h += mix64((unsigned long long)__float_as_uint(v) + (unsigned long long)i * 0x9E3779B97F4A7C15ull);
     const bool isn = isnan(v);
     if (nanmask) nanmask[i] = isn ? 1 : 0;
     if (isn) data[i] = 0.f;
+  }
+  if (hash) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) h += __shfl_xor_sync(0xffffffffu, h, o);
+    if ((threadIdx.x & 31) == 0) atomicAdd(hash, h);
   }
 }
 
@@ -188,8 +204,9 @@ int iq_launch_pad_symmetric(iq_ctx* ctx, const float* src, Dim3 src_dims, float*
   return IQ_OK;
 }
 
-int iq_launch_prepare(iq_ctx* ctx, float* data, int64_t n, uint8_t* nanmask) {
-  prepare_kernel<<<blocks_for(n), 256, 0, ctx->stream>>>(data, n, nanmask);
+int iq_launch_prepare(iq_ctx* ctx, float* data, int64_t n, uint8_t* nanmask,
+                      unsigned long long* hash) {
+  prepare_kernel<<<blocks_for(n), 256, 0, ctx->stream>>>(data, n, nanmask, hash);
   iq_count(ctx);
   IQ_CUDA_OK(cudaGetLastError());
   return IQ_OK;

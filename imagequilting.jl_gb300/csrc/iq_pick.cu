@@ -1432,10 +1432,23 @@ __global__ void __launch_bounds__(PT) pick_kernel(const PickArgs a) {
       SelReq req[2];
       Key res[2];
       int j0 = 0;
-      if (q == 0) {
+      // D's selection shared by all realizations of the tile (a hard-data map), precomputed
+      const bool preD = q == 0 && !allzero && tk.x0_pb && tk.x0_pb->ok;
+      if (preD) {
+        const PreBand& pb = *tk.x0_pb;
+        pr.kD = Key{(uint32_t)(pb.key >> 32), (uint32_t)pb.key};
+        if (pb.ok == 1) {
+          if (threadIdx.x == 0)
+            sband[0] = Band{pb.lo, pb.hi, const_cast<int32_t*>(tk.x0_pool) + pb.off, pb.n};
+          __syncthreads();
+          pr.bD = &sband[0];
+          tiesD = pb.ties;
+        }
+      }
+      if (q == 0 && !preD) {
         req[0] = SelReq{D, mm[0], mm[1], dbsize};
         const bool pre0 = !allzero && q < tk.nkeys &&
-                          (tk.aux_keys[0] || (tk.aux_pb[0] && tk.aux_pb[0][q].ok));
+                          (tk.aux_keys[0] || (tk.aux_pb[0] && tk.aux_pb[0][q].ok == 1));
         if (NAUX > 0 && naux > 0 && sz > 0 && sz < P && !pre0) {
           req[1] = SelReq{aux[0], amm[0][0], amm[0][1], sz};
           hist_select<2>(s, hist, sbuf, req, P, res);
@@ -1461,7 +1474,7 @@ __global__ void __launch_bounds__(PT) pick_kernel(const PickArgs a) {
         if (j >= naux) continue;
         tiesA[j] = -1;
         pr.ba[j] = nullptr;
-        if (j >= j0 && !allzero && tk.aux_pb[j] && q < tk.nkeys && tk.aux_pb[j][q].ok) {
+        if (j >= j0 && !allzero && tk.aux_pb[j] && q < tk.nkeys && tk.aux_pb[j][q].ok == 1) {
           // shared source with an error bound: its refined selection is precomputed
           const PreBand& pb = tk.aux_pb[j][q];
           pr.ka[j] = Key{(uint32_t)(pb.key >> 32), (uint32_t)pb.key};
@@ -1721,6 +1734,7 @@ struct BandArgs {
   PreBand* out;
   int32_t* pool;
   int64_t cap;
+  int keys_exact;     // exact maps get their key (ok = 2)
   // per-CTA scratch, P entries each
   double* rv;
   double* rr;
@@ -1771,6 +1785,7 @@ __global__ void __launch_bounds__(PT) select_bands_kernel(const BandArgs a) {
       for (int64_t i = threadIdx.x; i < band.n; i += PT) dst[i] = list[i];
     }
   }
+  if (!ref_on(a.srcs[m]) && a.keys_exact) ok = 2;  // an exact map: its key decides
   if (threadIdx.x == 0) {
     o->lo = band.lo;
     o->hi = band.hi;
@@ -1787,7 +1802,7 @@ __global__ void __launch_bounds__(PT) select_bands_kernel(const BandArgs a) {
 int iq_launch_select_bands(iq_ctx* ctx, const float* maps, const unsigned* mm,
                            const ExactSrc* srcs, int64_t nmaps, int64_t P, int64_t dx,
                            int64_t dxy, const int64_t* seq, int nq, PreBand* out, int32_t* pool,
-                           int64_t cap) {
+                           int64_t cap, int keys_exact) {
   if (nmaps <= 0 || nq <= 0) return IQ_OK;
   if (nq > IQ_PRE_KEYS) return iq_set_error(IQ_ERR_ARG, "too many precomputed selections");
   // per-CTA scratch for a batch of CTAs (38 bytes per position each)
@@ -1814,7 +1829,7 @@ int iq_launch_select_bands(iq_ctx* ctx, const float* maps, const unsigned* mm,
     a.maps = maps; a.mm = mm; a.srcs = srcs; a.m0 = m0; a.nmaps = std::min(mper, nmaps - m0);
     a.P = P; a.dx = dx; a.dxy = dxy; a.nq = nq;
     for (int q = 0; q < IQ_PRE_KEYS; ++q) a.seq[q] = q < nq ? seq[q] : 0;
-    a.out = out; a.pool = pool; a.cap = cap;
+    a.out = out; a.pool = pool; a.cap = cap; a.keys_exact = keys_exact;
     a.rv = rv; a.rr = rr; a.rl = rl; a.list = list; a.k0 = k0; a.v0 = v0; a.k1 = k1; a.v1 = v1;
     iq_timer_start(ctx, "pick");
     select_bands_kernel<<<(unsigned)(a.nmaps * nq), PT, DYN_BYTES, ctx->stream>>>(a);

@@ -693,7 +693,6 @@ int iq_lp_adam(iq_ctx* ctx, float* p, const float* g, float* m, float* v, int n,
 // =============================================================================================
 namespace {
 
-constexpr int TAU_SAMPLES = 8192;  // positions sampled per column for its threshold
 
 __device__ __forceinline__ float bdot64(const __nv_bfloat16* x, const float* e) {
   float acc = 0.f;
@@ -707,37 +706,6 @@ __device__ __forceinline__ float bdot64(const __nv_bfloat16* x, const float* e) 
   return acc;
 }
 
-// One CTA per column: scores of TAU_SAMPLES evenly spaced positions, sorted; tau = the m-th.
-__global__ void __launch_bounds__(1024) lp_tau_kernel(const __nv_bfloat16* __restrict__ W,
-                                                      const float* __restrict__ nW, int64_t P,
-                                                      const __nv_bfloat16* __restrict__ T,
-                                                      const float* __restrict__ nT, int m,
-                                                      float* tau) {
-  __shared__ float sc[TAU_SAMPLES];
-  __shared__ float e[EMB];
-  const int c = blockIdx.x;
-  for (int i = threadIdx.x; i < EMB; i += blockDim.x) e[i] = __bfloat162float(T[(int64_t)c * EMB + i]);
-  __syncthreads();
-  const int64_t stride = (P + TAU_SAMPLES - 1) / TAU_SAMPLES;
-  for (int i = threadIdx.x; i < TAU_SAMPLES; i += blockDim.x) {
-    const int64_t p = (int64_t)i * stride;
-    sc[i] = p < P ? nW[p] + nT[c] - 2.f * bdot64(W + p * EMB, e) : 3.4e38f;
-  }
-  __syncthreads();
-  for (int k = 2; k <= TAU_SAMPLES; k <<= 1)
-    for (int j = k >> 1; j > 0; j >>= 1) {
-      for (int i = threadIdx.x; i < TAU_SAMPLES; i += blockDim.x) {
-        const int l = i ^ j;
-        if (l > i) {
-          const float a = sc[i], b = sc[l];
-          if ((a > b) == ((i & k) == 0)) { sc[i] = b; sc[l] = a; }
-        }
-      }
-      __syncthreads();
-    }
-  if (threadIdx.x == 0) tau[c] = sc[min(m, TAU_SAMPLES) - 1];
-}
-
 __device__ __forceinline__ void mma_bf16(float* d, const uint32_t* a, uint32_t b0, uint32_t b1) {
   asm volatile(
       "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, "
@@ -749,12 +717,15 @@ __device__ __forceinline__ void mma_bf16(float* d, const uint32_t* a, uint32_t b
 // Scores of every position against 64 columns (blockIdx.y) with tensor-core MMAs (BF16 in, FP32
 // accumulation): s = |w|^2 + |e|^2 - 2 w.e; positions with s <= tau[col] are appended to the
 // column's list (cap entries; cnt keeps counting past it so that an overflow is seen).
+// DENSE: every score is written to dense[col * P + row] instead (the sampled rows).
+template <bool DENSE>
 __global__ void __launch_bounds__(256) lp_scan_kernel(const __nv_bfloat16* __restrict__ W,
                                                       const float* __restrict__ nW, int64_t P,
                                                       const __nv_bfloat16* __restrict__ T,
                                                       const float* __restrict__ nT,
                                                       const float* __restrict__ tau, int N,
-                                                      int32_t* list, int32_t* cnt, int cap) {
+                                                      int32_t* list, int32_t* cnt, int cap,
+                                                      float* dense) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int gid = lane >> 2, tig = lane & 3;
   const int n0 = blockIdx.y * 64;
@@ -775,7 +746,7 @@ __global__ void __launch_bounds__(256) lp_scan_kernel(const __nv_bfloat16* __res
     for (int h = 0; h < 2; ++h) {
       const int cc = n0 + nt * 8 + 2 * tig + h;
       ncol[nt][h] = cc < N ? nT[cc] : 0.f;
-      tcol[nt][h] = cc < N ? tau[cc] : -1.f;
+      tcol[nt][h] = DENSE ? 0.f : (cc < N ? tau[cc] : -1.f);
     }
   }
   const int64_t nblk = (P + 15) / 16;
@@ -804,13 +775,65 @@ __global__ void __launch_bounds__(256) lp_scan_kernel(const __nv_bfloat16* __res
         const int h = e & 1;
         const int64_t row = e < 2 ? r0 : r1;
         const float s = (e < 2 ? w0 : w1) + ncol[nt][h] - 2.f * acc[e];
-        if (row < P && s <= tcol[nt][h]) {
+        if (DENSE) {
+          const int c = n0 + nt * 8 + 2 * tig + h;
+          if (row < P && c < N) dense[(int64_t)c * P + row] = s;
+        } else if (row < P && s <= tcol[nt][h]) {
           const int c = n0 + nt * 8 + 2 * tig + h;
           const int idx = atomicAdd(cnt + c, 1);
           if (idx < cap) list[(int64_t)c * cap + idx] = (int32_t)row;
         }
       }
     }
+  }
+}
+
+// Rows i * stride of the window embeddings (the positions the per-column thresholds sample).
+__global__ void lp_sample_rows_kernel(const __nv_bfloat16* __restrict__ W, const float* __restrict__ nW,
+                                      int64_t P, int64_t stride, int S, __nv_bfloat16* Ws,
+                                      float* nWs) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= (int64_t)S * EMB) return;
+  const int64_t row = i / EMB, d = i - row * EMB;
+  const int64_t p = row * stride;
+  Ws[i] = p < P ? W[p * EMB + d] : __float2bfloat16_rn(0.f);
+  if (d == 0) nWs[row] = p < P ? nW[p] : 3.0e38f;
+}
+
+// The m-th smallest of each column's S sampled scores (MSD radix select on order-preserving
+// keys, one CTA per column).
+__global__ void __launch_bounds__(256) lp_select_kernel(const float* __restrict__ dense, int S,
+                                                        int m, float* tau) {
+  __shared__ unsigned hist[256];
+  __shared__ unsigned sel, need;
+  const float* x = dense + (int64_t)blockIdx.x * S;
+  unsigned prefix = 0, pmask = 0;
+  if (threadIdx.x == 0) need = (unsigned)m;
+  for (int shift = 24; shift >= 0; shift -= 8) {
+    hist[threadIdx.x] = 0;
+    __syncthreads();
+    for (int i = threadIdx.x; i < S; i += blockDim.x) {
+      const unsigned b = __float_as_uint(x[i]);
+      const unsigned key = (b & 0x80000000u) ? ~b : (b | 0x80000000u);
+      if ((key & pmask) == prefix) atomicAdd(&hist[(key >> shift) & 255u], 1u);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      unsigned run = 0, d = 0;
+      for (; d < 255; ++d) {
+        if (run + hist[d] >= need) break;
+        run += hist[d];
+      }
+      sel = d;
+      need -= run;
+    }
+    __syncthreads();
+    prefix |= sel << shift;
+    pmask |= 255u << shift;
+  }
+  if (threadIdx.x == 0) {
+    const unsigned b = (prefix & 0x80000000u) ? (prefix & 0x7FFFFFFFu) : ~prefix;
+    tau[blockIdx.x] = __uint_as_float(b);
   }
 }
 
@@ -891,28 +914,45 @@ __global__ void lp_recall_kernel(const float* D, const unsigned* dmin, int64_t P
 
 }  // namespace
 
-int iq_lp_shortlist(iq_ctx* ctx, const __nv_bfloat16* W, const float* nW, int64_t P,
-                    const __nv_bfloat16* T, const float* nT, int N, int64_t k, float* tau,
-                    int32_t* list, int32_t* cnt, int cap) {
-  if (N <= 0) return IQ_OK;
-  const int64_t stride = (P + TAU_SAMPLES - 1) / TAU_SAMPLES;
-  // the m-th smallest sampled score stands for about m * stride positions
-  const int m = (int)std::max<int64_t>(4, std::min<int64_t>(TAU_SAMPLES, (k + stride - 1) / stride));
-  cudaStream_t st = ctx->stream;
-  iq_timer_start(ctx, "lp.scan");
-  lp_tau_kernel<<<(unsigned)N, 1024, 0, st>>>(W, nW, P, T, nT, m, tau);
+int iq_lp_sample_rows(iq_ctx* ctx, const __nv_bfloat16* W, const float* nW, int64_t P,
+                      __nv_bfloat16* Ws, float* nWs) {
+  const int64_t stride = (P + IQ_LP_SAMPLES - 1) / IQ_LP_SAMPLES;
+  const int64_t n = (int64_t)IQ_LP_SAMPLES * EMB;
+  lp_sample_rows_kernel<<<(unsigned)((n + 255) / 256), 256, 0, ctx->stream>>>(W, nW, P, stride,
+                                                                            IQ_LP_SAMPLES, Ws, nWs);
+  iq_count(ctx);
   IQ_CUDA_OK(cudaGetLastError());
-  IQ_CUDA_OK(cudaMemsetAsync(cnt, 0, sizeof(int32_t) * N, st));
+  return IQ_OK;
+}
+
+int iq_lp_shortlist(iq_ctx* ctx, const __nv_bfloat16* W, const float* nW, int64_t P,
+                    const __nv_bfloat16* Ws, const float* nWs, const __nv_bfloat16* T,
+                    const float* nT, int N, int64_t k, float* tau, float* dense, int32_t* list,
+                    int32_t* cnt, int cap) {
+  if (N <= 0) return IQ_OK;
+  const int S = IQ_LP_SAMPLES;
+  const int64_t stride = (P + S - 1) / S;
+  // the m-th smallest sampled score stands for about m * stride positions
+  const int m = (int)std::max<int64_t>(4, std::min<int64_t>(S, (k + stride - 1) / stride));
+  cudaStream_t st = ctx->stream;
   int dev = 0, nsm = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
   const int ncb = (N + 63) / 64;
+  iq_timer_start(ctx, "lp.scan");
+  // per-column thresholds: the sampled rows' scores as one GEMM, then a select per column
+  lp_scan_kernel<true><<<dim3((unsigned)((S / 16 + 7) / 8), (unsigned)ncb), 256, 0, st>>>(
+      Ws, nWs, S, T, nT, nullptr, N, nullptr, nullptr, 0, dense);
+  lp_select_kernel<<<(unsigned)N, 256, 0, st>>>(dense, S, m, tau);
+  IQ_CUDA_OK(cudaGetLastError());
+  IQ_CUDA_OK(cudaMemsetAsync(cnt, 0, sizeof(int32_t) * N, st));
   const int64_t nblk = (P + 15) / 16;
   const int64_t gx = std::max<int64_t>(1, std::min<int64_t>((nblk + 7) / 8, (int64_t)nsm * 8 / ncb + 1));
-  lp_scan_kernel<<<dim3((unsigned)gx, (unsigned)ncb), 256, 0, st>>>(W, nW, P, T, nT, tau, N, list,
-                                                                    cnt, cap);
-  iq_timer_stop(ctx, "lp.scan", 2.0 * (double)P * N * EMB);
-  iq_count(ctx, 2);
+  lp_scan_kernel<false><<<dim3((unsigned)gx, (unsigned)ncb), 256, 0, st>>>(W, nW, P, T, nT, tau,
+                                                                           N, list, cnt, cap,
+                                                                           nullptr);
+  iq_timer_stop(ctx, "lp.scan", 2.0 * (double)(P + S) * N * EMB);
+  iq_count(ctx, 3);
   IQ_CUDA_OK(cudaGetLastError());
   return IQ_OK;
 }

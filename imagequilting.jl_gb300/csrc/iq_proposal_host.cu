@@ -20,6 +20,8 @@ struct LpCache {
   int32_t lohi[6];
   __nv_bfloat16* W = nullptr;  // [P][64]
   float* nW = nullptr;         // [P]
+  __nv_bfloat16* Ws = nullptr; // sampled rows [IQ_LP_SAMPLES][64]
+  float* nWs = nullptr;        // [IQ_LP_SAMPLES]
 };
 
 }  // namespace
@@ -60,6 +62,8 @@ void free_cache(IqLp* lp) {
   for (auto& c : lp->cache) {
     cudaFree(c.W);
     cudaFree(c.nW);
+    cudaFree(c.Ws);
+    cudaFree(c.nWs);
   }
   lp->cache.clear();
 }
@@ -153,14 +157,22 @@ int window_embeddings(iq_ctx* ctx, IqLp* lp, const int32_t* lohi, const LpCache*
   LpCache c;
   memcpy(c.lohi, lohi, sizeof(c.lohi));
   if (cudaMalloc(&c.W, sizeof(__nv_bfloat16) * P * IQ_LP_EMB) != cudaSuccess ||
-      cudaMalloc(&c.nW, sizeof(float) * P) != cudaSuccess) {
+      cudaMalloc(&c.nW, sizeof(float) * P) != cudaSuccess ||
+      cudaMalloc(&c.Ws, sizeof(__nv_bfloat16) * IQ_LP_SAMPLES * IQ_LP_EMB) != cudaSuccess ||
+      cudaMalloc(&c.nWs, sizeof(float) * IQ_LP_SAMPLES) != cudaSuccess) {
     cudaGetLastError();
     cudaFree(c.W);
+    cudaFree(c.nW);
+    cudaFree(c.Ws);
     return iq_set_error(IQ_ERR_ALLOC, "proposal: window embeddings of %lld positions", (long long)P);
   }
   rc = iq_lp_encode_windows(ctx, lp->g, lp->w, lp->ii1, ctx->d_ti2ii, ctx->ti, dist, lohi,
                             lohi + 3, c.W, c.nW);
-  if (rc) return rc;
+  if (!rc) rc = iq_lp_sample_rows(ctx, c.W, c.nW, P, c.Ws, c.nWs);
+  if (rc) {
+    cudaFree(c.W); cudaFree(c.nW); cudaFree(c.Ws); cudaFree(c.nWs);
+    return rc;
+  }
   lp->cache.push_back(c);
   *out = &lp->cache.back();
   return IQ_OK;
@@ -239,6 +251,7 @@ int iq_lp_run_chunk(iq_ctx* ctx, const LpChunk& c, int64_t chunk_index, int* don
   __nv_bfloat16* dT = (__nv_bfloat16*)iq_scratch(ctx, S_LP_T, sizeof(__nv_bfloat16) * N * IQ_LP_EMB);
   float* dnT = (float*)iq_scratch(ctx, S_LP_NT, sizeof(float) * N);
   float* dtau = (float*)iq_scratch(ctx, S_LP_TAU, sizeof(float) * N);
+  float* ddense = (float*)iq_scratch(ctx, S_LP_DENSE, sizeof(float) * (size_t)N * IQ_LP_SAMPLES);
   int32_t* dlist = (int32_t*)iq_scratch(ctx, S_LP_LIST, sizeof(int32_t) * (size_t)N * cap);
   int32_t* dcnt = (int32_t*)iq_scratch(ctx, S_LP_CNT, sizeof(int32_t) * N);
   float* ddl = (float*)iq_scratch(ctx, S_LP_DL, sizeof(float) * (size_t)N * cap);
@@ -247,7 +260,7 @@ int iq_lp_run_chunk(iq_ctx* ctx, const LpChunk& c, int64_t chunk_index, int* don
   int* dtbox = (int*)iq_scratch(ctx, S_LP_TBOX, sizeof(int32_t) * 6 * N);
   int64_t* drind = (int64_t*)iq_scratch(ctx, S_LP_RIND, sizeof(int64_t) * N);
   int64_t* dncand = (int64_t*)iq_scratch(ctx, S_LP_NCAND, sizeof(int64_t) * N);
-  if (!dT || !dnT || !dtau || !dlist || !dcnt || !ddl || !dcols || !dtsrc || !dtbox || !drind || !dncand)
+  if (!dT || !dnT || !dtau || !ddense || !dlist || !dcnt || !ddl || !dcols || !dtsrc || !dtbox || !drind || !dncand)
     return IQ_ERR_ALLOC;
   IQ_CUDA_OK(cudaMemcpyAsync(dtsrc, tsrc.data(), sizeof(int64_t) * N, cudaMemcpyHostToDevice, st));
   IQ_CUDA_OK(cudaMemcpyAsync(dtbox, tbox.data(), sizeof(int32_t) * 6 * N, cudaMemcpyHostToDevice, st));
@@ -261,8 +274,9 @@ int iq_lp_run_chunk(iq_ctx* ctx, const LpChunk& c, int64_t chunk_index, int* don
     const LpCache* wc = nullptr;
     rc = window_embeddings(ctx, lp, c.lohi + 6 * c.cfg[ord[q0]], &wc);
     if (rc) return rc;
-    rc = iq_lp_shortlist(ctx, wc->W, wc->nW, P, dT + (size_t)q0 * IQ_LP_EMB, dnT + q0, q1 - q0,
-                         ctx->lp_k, dtau + q0, dlist + (size_t)q0 * cap, dcnt + q0, cap);
+    rc = iq_lp_shortlist(ctx, wc->W, wc->nW, P, wc->Ws, wc->nWs, dT + (size_t)q0 * IQ_LP_EMB,
+                         dnT + q0, q1 - q0, ctx->lp_k, dtau + q0, ddense, dlist + (size_t)q0 * cap,
+                         dcnt + q0, cap);
     if (rc) return rc;
     q0 = q1;
   }

@@ -50,6 +50,7 @@ __global__ void __launch_bounds__(LP_PT) lp_pick_kernel(const LpPickArgs a) {
   __shared__ float red[32];
   __shared__ unsigned long long ured[32];
   __shared__ int sflag;
+  __shared__ unsigned smin;  // running minimum of the finished sums (bits of a non-negative float)
   const int c = blockIdx.x;
   const LpColumn col = a.cols[c];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -67,7 +68,12 @@ __global__ void __launch_bounds__(LP_PT) lp_pick_kernel(const LpPickArgs a) {
     off[j] = (int32_t)(kx + a.isx * ky + a.isxy * kz);
     tv[j] = col.tmpl[kx + col.tgx * ky + col.tgxy * kz];
   }
+  if (threadIdx.x == 0) smin = 0x7F7FFFFFu;
   __syncthreads();
+  // An entry is abandoned once a partial sum exceeds (1 + tol) * running minimum * (1 + 2e-6):
+  // the terms are non-negative and the sums exact, so its full sum lies above the final
+  // threshold by more than the near-tie band and it neither sets the minimum nor is a candidate.
+  const float pf = (float)((1.0 + a.tol) * (1.0 + 2e-6));
   const int32_t* lst = a.list + (int64_t)c * a.cap;
   float* dl = a.dl + (int64_t)c * a.cap;
   float mloc = 3.4e38f;
@@ -77,21 +83,35 @@ __global__ void __launch_bounds__(LP_PT) lp_pick_kernel(const LpPickArgs a) {
     const float* base = a.img + x + a.isx * y + a.isxy * z;
     float acc = 0.f;
     int j = lane;
-    for (; j + 96 < col.K; j += 128) {
+    bool pruned = false;
+    for (int nx = 0; j + 96 < col.K; j += 128) {
       const float d0 = base[off[j]] - tv[j], d1 = base[off[j + 32]] - tv[j + 32];
       const float d2 = base[off[j + 64]] - tv[j + 64], d3 = base[off[j + 96]] - tv[j + 96];
       acc = fmaf(d0, d0, acc);
       acc = fmaf(d1, d1, acc);
       acc = fmaf(d2, d2, acc);
       acc = fmaf(d3, d3, acc);
+      if (++nx == 4) {  // every 512 terms
+        nx = 0;
+        float part = acc;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
+        const float bound = __uint_as_float(*(volatile unsigned*)&smin) * pf;
+        if (part > bound) { pruned = true; break; }
+      }
     }
-    for (; j < col.K; j += 32) {
-      const float d = base[off[j]] - tv[j];
-      acc = fmaf(d, d, acc);
-    }
+    if (!pruned)
+      for (; j < col.K; j += 32) {
+        const float d = base[off[j]] - tv[j];
+        acc = fmaf(d, d, acc);
+      }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-    if (lane == 0) dl[i] = acc;
+    if (pruned) acc = INFINITY;
+    if (lane == 0) {
+      dl[i] = acc;
+      if (!pruned) atomicMin(&smin, __float_as_uint(acc));
+    }
     mloc = fminf(mloc, acc);
   }
   // minimum

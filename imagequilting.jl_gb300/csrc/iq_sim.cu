@@ -901,6 +901,17 @@ extern "C" int iq_simulate(iq_ctx* ctx, const iq_sim_params* p, const iq_hard_da
     }
   }
 
+  // ---- dbsize selections of the hard-data maps (one per data tile, shared by its
+  // realizations), computed once after the maps below ----
+  std::vector<ExactSrc> hard_x;   // re-evaluation of each hard map (kappa 0: exact)
+  PreBand* d_pbh = nullptr;
+  int32_t* d_pbhpool = nullptr;
+  if (nhs > 0 && npat > 0) {
+    d_pbh = (PreBand*)iq_scratch(ctx, S_PBH_OUT, sizeof(PreBand) * nhs);
+    d_pbhpool = (int32_t*)iq_scratch(ctx, S_PBH_POOL, sizeof(int32_t) * nhs * pb_cap);
+    if (!d_pbh || !d_pbhpool) return IQ_ERR_ALLOC;
+    hard_x.resize(nhs);
+  }
   // ---- task descriptors of every step, uploaded once ----
   // Gather and pick tasks point at per-realization slots: each group has its own copy, whose
   // pointers start at the group's first realization. Cut and paste tasks are shared.
@@ -961,12 +972,17 @@ extern "C" int iq_simulate(iq_ctx* ctx, const iq_sim_params* p, const iq_hard_da
           q.D0 = Dh; q.D0_rs = 0; q.mm0 = mmh; q.mm0_rs = 0;
           const int64_t h0 = hoff[s.tile], hn = hoff[s.tile + 1] - hoff[s.tile];
           const double hk_kappa = iq_map_kappa(ctx->ti_stats, hard_stats, hn, 0);
+          if (d_pbh) {
+            q.x0_pb = d_pbh + (hi - 1);
+            q.x0_pool = d_pbhpool;
+          }
           if (hk_kappa > 0.0) {
             ExactSrc& xh = q.x0;
             xh.img = ctx->d_ti; xh.isx = ctx->ti.x; xh.isxy = ctx->ti.x * ctx->ti.y;
             xh.klist = d_hk + h0; xh.K = (int)hn; xh.kval = d_hkv + h0;
             xh.b2 = Dh == nullptr ? nullptr : d_b2h + (hi - 1); xh.b2_rs = 0;
             xh.kappa = hk_kappa; xh.eabs = 0.0;
+            if (!hard_x.empty()) hard_x[hi - 1] = xh;
           }
           q.aux[na] = D + r0 * P; q.aux_rs[na] = P; q.aux_mm[na] = mm + 2 * r0; q.aux_mm_rs[na] = 2;
           q.xa[na] = xo;
@@ -1039,6 +1055,15 @@ extern "C" int iq_simulate(iq_ctx* ctx, const iq_sim_params* p, const iq_hard_da
     Ch.rpad = 1; Ch.ntmpl = 1; Ch.out_stride = P; Ch.disabled = d_dis;
     Ch.ntask = nb; Ch.tasks = d_hct + h; Ch.flops = 1;
     RET_IF(iq_launch_corr(ctx, Ch));
+  }
+  if (d_pbh) {
+    ExactSrc* d_hx = (ExactSrc*)iq_scratch(ctx, S_PBH_SRC, sizeof(ExactSrc) * nhs);
+    if (!d_hx) return IQ_ERR_ALLOC;
+    IQ_CUDA_OK(cudaMemcpyAsync(d_hx, hard_x.data(), sizeof(ExactSrc) * nhs, cudaMemcpyHostToDevice, st));
+    const int64_t seq1[1] = {dbn};
+    RET_IF(iq_launch_select_bands(ctx, d_Dh, d_mmh, d_hx, nhs, P, distD.x, distD.x * distD.y, seq1,
+                                  1, d_pbh, d_pbhpool, pb_cap, 1));
+    IQ_CUDA_OK(cudaStreamSynchronize(st));  // `hard_x` is a host vector
   }
 
   // ---- the tile loop (src/iqsim.jl:172-285), one dependency level chunk at a time ----
