@@ -108,15 +108,16 @@ extern "C" int iq_profile_get(iq_ctx* ctx, const char* kernel, double* ms_total,
   }
   // "corr.loop", "corr.wait_full", "corr.wait_afull", "corr.wait_done", "corr.producer_wait",
   // "corr.producer_loop", "corr.epilogue" (work = SM cycles summed over CTAs, launches = CTAs)
-  const char* names[23] = {"graphcut.rounds", "graphcut.levels", "pick.iterations",
+  const char* names[27] = {"graphcut.rounds", "graphcut.levels", "pick.iterations",
                            "pick.candidates", "graphcut.max_rounds", "graphcut.max_levels",
                            "corr.loop", "corr.wait_full", "corr.wait_afull", "corr.wait_done",
                            "corr.producer_wait", "corr.producer_loop", "corr.epilogue",
                            "corr.issue", "corr.mma_units", "graphcut.setup_cycles",
                            "graphcut.round_cycles", "graphcut.relabel_cycles",
                            "pick.select_cycles", "pick.weight_cycles", "pick.draw_cycles",
-                           "graphcut.active_nodes", "graphcut.nodes"};
-  const int idx[23][2] = {{ST_CUT_ROUNDS, ST_CUT_CTAS}, {ST_CUT_LEVELS, ST_CUT_CTAS},
+                           "graphcut.active_nodes", "graphcut.nodes", "pick.band_cycles",
+                           "pick.ev1", "pick.ev2", "pick.ev3"};
+  const int idx[27][2] = {{ST_CUT_ROUNDS, ST_CUT_CTAS}, {ST_CUT_LEVELS, ST_CUT_CTAS},
                           {ST_PICK_ITERS, ST_PICK_CTAS}, {ST_PICK_CAND, ST_PICK_CTAS},
                           {ST_CUT_MAXROUNDS, ST_CUT_CTAS}, {ST_CUT_MAXLEVELS, ST_CUT_CTAS},
                           {ST_TC_LOOP, ST_TC_CTAS}, {ST_TC_WFULL, ST_TC_CTAS},
@@ -127,8 +128,10 @@ extern "C" int iq_profile_get(iq_ctx* ctx, const char* kernel, double* ms_total,
                           {ST_CUT_TROUNDS, ST_CUT_CTAS}, {ST_CUT_TGR, ST_CUT_CTAS},
                           {ST_PICK_TSEL, ST_PICK_CTAS}, {ST_PICK_TW, ST_PICK_CTAS},
                           {ST_PICK_TDRAW, ST_PICK_CTAS}, {ST_CUT_ACTIVE, ST_CUT_CTAS},
-                          {ST_CUT_NODES, ST_CUT_CTAS}};
-  for (int i = 0; i < 23; ++i)
+                          {ST_CUT_NODES, ST_CUT_CTAS}, {ST_PICK_TBAND, ST_PICK_CTAS},
+                          {ST_PICK_EV1, ST_PICK_CTAS}, {ST_PICK_EV2, ST_PICK_CTAS},
+                          {ST_PICK_EV3, ST_PICK_CTAS}};
+  for (int i = 0; i < 27; ++i)
     if (!strcmp(kernel, names[i])) {
       unsigned long long h[ST_COUNT];
       IQ_CUDA_OK(cudaMemcpy(h, ctx->d_stats, sizeof(h), cudaMemcpyDeviceToHost));

@@ -110,7 +110,8 @@ enum IqStat { ST_CUT_ROUNDS = 0, ST_CUT_LEVELS, ST_CUT_CTAS, ST_PICK_ITERS, ST_P
               // relabel rounds, global relabels
               ST_CUT_TSETUP, ST_CUT_TROUNDS, ST_CUT_TGR,
               // pick, SM cycles summed over CTAs: selection + compaction, tau-model weights, draw
-              ST_PICK_TSEL, ST_PICK_TW, ST_PICK_TDRAW,
+              ST_PICK_TSEL, ST_PICK_TW, ST_PICK_TDRAW, ST_PICK_TBAND, ST_PICK_EV1, ST_PICK_EV2,
+              ST_PICK_EV3,
               // graph cut: active nodes summed over rounds, node count of the slabs
               ST_CUT_ACTIVE, ST_CUT_NODES, ST_COUNT };
 
@@ -124,7 +125,7 @@ enum IqSlot {
   S_PB_RV, S_PB_RR, S_PB_RL, S_PB_LIST, S_PB_K, S_PB_OUT, S_PB_POOL, S_PB_SRC,
   S_PBH_OUT, S_PBH_POOL, S_PBH_SRC,
   S_LP_T, S_LP_NT, S_LP_TAU, S_LP_LIST, S_LP_CNT, S_LP_DL, S_LP_COLS, S_LP_TSRC, S_LP_TBOX,
-  S_LP_RIND, S_LP_NCAND, S_LP_D, S_LP_BITS, S_LP_ITEMS, S_LP_X, S_LP_E, S_LP_GE, S_LP_FEAT, S_LP_BH1, S_LP_BGZ1, S_LP_BH2, S_LP_DENSE,
+  S_LP_RIND, S_LP_NCAND, S_LP_D, S_LP_BITS, S_LP_ITEMS, S_LP_X, S_LP_E, S_LP_GE, S_LP_FEAT, S_LP_BH1, S_LP_BGZ1, S_LP_BH2, S_LP_DENSE, S_LP_QUAD,
   S_COUNT
 };
 
@@ -522,15 +523,228 @@ int iq_lp_encode_windows(iq_ctx* ctx, const LpGeo& g, const float* w, const doub
                          int64_t npos = 0);
 // One column of the proposal's pick: tile `tile` of global realization `real`, with the mask's
 // offsets and the simulation grid at the tile.
+// Quads of a mask: four consecutive x offsets of one (y, z) row starting at a multiple of 4,
+// for byte-valued images (sums of squared differences with one dp4a per quad).
+struct LpQuad {
+  int32_t off;    // image offset of the quad's first voxel from the window origin
+  int32_t tx;     // template offset of the same voxel
+  uint32_t mask;  // 0xFF in each byte whose voxel is in the mask
+  int32_t pad_;
+};
 struct LpColumn {
   const uint32_t* klist;
   int K;
-  int32_t pad_;
+  int nq;              // quads of the mask (quad)
+  const LpQuad* quad;
   const float* tmpl;
   int64_t tgx, tgxy;
   int64_t tile, real;
+  int32_t lohi[6];     // the mask: the tile minus the box [lo, hi)
+  int32_t tdim[3];     // tile extents
+  int32_t pad2_;
 };
+// The training image as the exact sums of the proposal read it. Plane form (codes 0..3, tiles
+// of x extent <= 32): 2-bit codes in tiles of 32 (x) by 16 (y) voxels, one 64-bit word per tile
+// row (bits 0-31: the low bit of each voxel's code, bits 32-63: the high bit), tiles ordered
+// (x, y, z) with one extra column of zero tiles past the last in x; a window row of 32 voxels
+// is then two words and a funnel shift. Byte form otherwise (quads).
+struct LpImg {
+  const uint8_t* b8;               // bytes, 16 bytes of padding past the end
+  const unsigned long long* b2;    // plane form (nullptr: byte form)
+  int64_t isx, isxy;               // byte image strides
+  int64_t ntx, nty;                // plane tiles per row (x, including the zero column), per slice (y)
+};
+#ifdef __CUDACC__
+// Comparisons of FP32 map values with Float64 bounds, made in FP32 (the FP64 pipe of this part
+// is far narrower than its FP32 pipe): for a float d and a double x,
+//   (double)d <  x  <=>  d <  f_up(x)     (f_up: the smallest float >= x)
+//   (double)d <= x  <=>  d <= f_dn(x)     (f_dn: the largest float <= x)
+__device__ __forceinline__ float f_up(double x) { return __double2float_ru(x); }
+__device__ __forceinline__ float f_dn(double x) { return __double2float_rd(x); }
+
+__device__ __forceinline__ float f_step(float v, bool up) {  // neighbour of a positive float
+  const uint32_t b = __float_as_uint(v);
+  return __uint_as_float(up ? b + 1u : b - 1u);
+}
+
+// FP32 bounds [lo, hi] of the floats v with fabs(rn((double)v - t)) <= w, the near-tie test
+// as the oracle evaluates it (an interval, since rn is monotone); t > 0 finite, 0 <= w < t.
+__device__ inline void tie_window_f(double t, double w, float& lo, float& hi) {
+  lo = f_dn(t - w);
+  hi = f_up(t + w);
+  for (int i = 0; i < 8 && lo >= 0.f && !(__dsub_rn((double)lo, t) >= -w); ++i) lo = f_step(lo, true);
+  for (int i = 0; i < 8 && lo > 0.f; ++i) {
+    const float p = f_step(lo, false);
+    if (p > 0.f && __dsub_rn((double)p, t) >= -w) lo = p; else break;
+  }
+  for (int i = 0; i < 8 && hi > 0.f && !(__dsub_rn((double)hi, t) <= w); ++i) hi = f_step(hi, false);
+  for (int i = 0; i < 8 && hi < 3.0e38f; ++i) {
+    const float p = f_step(hi, true);
+    if (__dsub_rn((double)p, t) <= w) hi = p; else break;
+  }
+}
+
+// The four bytes at image address p (any alignment): two aligned words and a byte permute.
+__device__ __forceinline__ uint32_t iq_ld4(const uint8_t* p) {
+  const uintptr_t u = reinterpret_cast<uintptr_t>(p);
+  const uint32_t sh = (uint32_t)(u & 3u);
+  const uint32_t* w = reinterpret_cast<const uint32_t*>(u - sh);
+  return __byte_perm(__ldg(w), __ldg(w + 1), 0x3210u + 0x1111u * sh);
+}
+
+// Stage a column's quads in shared memory: (image offset, template bytes, byte mask) per quad.
+// Returns false (for the whole block) when a template value in the mask is not a byte value.
+__device__ inline bool iq_stage_quads(const LpColumn& col, uint4* q) {
+  int bad = 0;
+  for (int i = threadIdx.x; i < col.nq; i += blockDim.x) {
+    const LpQuad e = col.quad[i];
+    uint32_t t = 0;
+#pragma unroll
+    for (int b = 0; b < 4; ++b) {
+      if (!(e.mask >> (8 * b) & 0xFFu)) continue;
+      const float v = col.tmpl[e.tx + b];
+      if (!(v >= 0.f && v <= 255.f && v == floorf(v))) bad = 1;
+      t |= ((uint32_t)v & 0xFFu) << (8 * b);
+    }
+    q[i] = make_uint4((uint32_t)e.off, t, e.mask, 0u);
+  }
+  return !__syncthreads_or(bad);
+}
+
+// Warp-collective: sum over the quads [0, nq) of the squared byte differences of the window at
+// `base` (every lane gets the total). With `bound` finite, gives up (returns UINT32_MAX) as soon
+// as a partial sum exceeds bound() -- a lower bound of the total, the terms being non-negative.
+template <typename Bound>
+__device__ __forceinline__ uint32_t iq_quad_ssd(const uint8_t* base, const uint4* q, int nq,
+                                                const Bound& bound) {
+  const int lane = threadIdx.x & 31;
+  uint32_t acc = 0;
+  int i = lane;
+  for (; i + 7 * 32 < nq; i += 8 * 32) {
+    uint32_t v[8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) v[u] = iq_ld4(base + (int32_t)q[i + 32 * u].x);
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      const uint4 e = q[i + 32 * u];
+      const uint32_t d = __vabsdiffu4(v[u], e.y) & e.z;
+      acc = __dp4a(d, d, acc);
+    }
+    uint32_t part = acc;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
+    if ((float)part > bound()) return 0xFFFFFFFFu;
+  }
+  for (; i < nq; i += 32) {
+    const uint4 e = q[i];
+    const uint32_t d = __vabsdiffu4(iq_ld4(base + (int32_t)e.x), e.y) & e.z;
+    acc = __dp4a(d, d, acc);
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+  return acc;
+}
+
+// Plane form: stage a column's template rows (ty, tz) of the tile in shared memory as
+// (low-bit plane, high-bit plane, mask bits, ty | tz << 16). Returns false (for the block) when
+// a template value in the mask is not one of 0, 1, 2, 3.
+__device__ inline bool iq_stage_rows(const LpColumn& col, uint4* rows) {
+  const int R = col.tdim[1] * col.tdim[2];
+  int bad = 0;
+  for (int r = threadIdx.x; r < R; r += blockDim.x) {
+    const int ty = r % col.tdim[1], tz = r / col.tdim[1];
+    const bool rin = ty >= col.lohi[1] && ty < col.lohi[4] && tz >= col.lohi[2] && tz < col.lohi[5];
+    uint32_t p0 = 0, p1 = 0, m = 0;
+    for (int x = 0; x < col.tdim[0]; ++x) {
+      if (rin && x >= col.lohi[0] && x < col.lohi[3]) continue;
+      const float v = col.tmpl[x + col.tgx * ty + col.tgxy * tz];
+      if (!(v == 0.f || v == 1.f || v == 2.f || v == 3.f)) bad = 1;
+      const uint32_t c = (uint32_t)v & 3u;
+      m |= 1u << x;
+      p0 |= (c & 1u) << x;
+      p1 |= (c >> 1) << x;
+    }
+    rows[r] = make_uint4(p0, p1, m, (uint32_t)ty | ((uint32_t)tz << 16));
+  }
+  return !__syncthreads_or(bad);
+}
+
+// Sum of (a - b)^2 over one row of 32 codes given as bit planes (a0, a1), (b0, b1) and mask m:
+// with u = a1 - b1, v = a0 - b0 in {-1, 0, 1}, (a - b)^2 = 4u^2 + 4uv + v^2.
+__device__ __forceinline__ int iq_row_ssd(uint32_t a0, uint32_t a1, const uint4& t) {
+  const uint32_t b0 = t.x, b1 = t.y, m = t.z;
+  const uint32_t up = a1 & ~b1, un = ~a1 & b1, vp = a0 & ~b0, vn = ~a0 & b0;
+  const uint32_t same = ((up & vp) | (un & vn)) & m, opp = ((up & vn) | (un & vp)) & m;
+  return 4 * __popc((a1 ^ b1) & m) + __popc((a0 ^ b0) & m) + 4 * __popc(same) - 4 * __popc(opp);
+}
+
+// Warp-collective, plane form: sum over the R staged rows for the window at (x0, y0, z0), with
+// the early exit of iq_quad_ssd.
+template <typename Bound>
+__device__ __forceinline__ uint32_t iq_plane_ssd(const LpImg& im, int64_t x0, int64_t y0,
+                                                 int64_t z0, const uint4* rows, int R,
+                                                 const Bound& bound) {
+  const int lane = threadIdx.x & 31;
+  const int64_t tx0 = x0 >> 5;
+  const uint32_t s = (uint32_t)(x0 & 31);
+  int acc = 0;
+  int r = lane;
+  for (; r + 3 * 32 < R; r += 4 * 32) {
+    unsigned long long wa[4], wb[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const uint32_t w = rows[r + 32 * u].w;
+      const int64_t yy = y0 + (w & 0xFFFFu), zz = z0 + (w >> 16);
+      const int64_t i0 = (((zz * im.nty + (yy >> 4)) * im.ntx + tx0) << 4) + (yy & 15);
+      wa[u] = __ldg(im.b2 + i0);
+      wb[u] = __ldg(im.b2 + i0 + 16);
+    }
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const uint32_t a0 = __funnelshift_r((uint32_t)wa[u], (uint32_t)wb[u], s);
+      const uint32_t a1 = __funnelshift_r((uint32_t)(wa[u] >> 32), (uint32_t)(wb[u] >> 32), s);
+      acc += iq_row_ssd(a0, a1, rows[r + 32 * u]);
+    }
+    int part = acc;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
+    if ((float)part > bound()) return 0xFFFFFFFFu;
+  }
+  for (; r < R; r += 32) {
+    const uint4 t = rows[r];
+    const int64_t yy = y0 + (t.w & 0xFFFFu), zz = z0 + (t.w >> 16);
+    const int64_t i0 = (((zz * im.nty + (yy >> 4)) * im.ntx + tx0) << 4) + (yy & 15);
+    const unsigned long long a = __ldg(im.b2 + i0), b = __ldg(im.b2 + i0 + 16);
+    acc += iq_row_ssd(__funnelshift_r((uint32_t)a, (uint32_t)b, s),
+                      __funnelshift_r((uint32_t)(a >> 32), (uint32_t)(b >> 32), s), t);
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+  return (uint32_t)acc;
+}
+
+// Stage a column for either form (rows or quads at `stage`); false: the column cannot be summed.
+__device__ inline bool iq_stage(const LpImg& im, const LpColumn& col, uint4* stage) {
+  return im.b2 ? iq_stage_rows(col, stage) : iq_stage_quads(col, stage);
+}
+
+// Exact sum of the column at distance-map position (x, y, z), either form.
+template <typename Bound>
+__device__ __forceinline__ uint32_t iq_lp_ssd(const LpImg& im, const LpColumn& col,
+                                              const uint4* stage, int64_t x, int64_t y,
+                                              int64_t z, const Bound& bound) {
+  if (im.b2) return iq_plane_ssd(im, x, y, z, stage, col.tdim[1] * col.tdim[2], bound);
+  return iq_quad_ssd(im.b8 + x + im.isx * y + im.isxy * z, stage, col.nq, bound);
+}
+#endif
 #define IQ_LP_SAMPLES 8192  // positions sampled per column for its shortlist threshold
+// dst[0, n) = the image as bytes (dst holds n + 16 bytes; the 16 past the end are zeroed);
+// *bad (device) = 1 when a value is not an integer in [0, 255].
+int iq_lp_to_u8(iq_ctx* ctx, const float* src, int64_t n, uint8_t* dst, int* bad);
+// The plane form of an image of codes 0..3 (LpImg; dst: d.z * nty * ntx * 16 words);
+// *bad (device) = 1 when a value is not one of the four codes.
+int iq_lp_to_planes(iq_ctx* ctx, const float* src, Dim3 d, int64_t ntx, int64_t nty,
+                    unsigned long long* dst, int* bad);
 // Rows i * ceil(P / IQ_LP_SAMPLES) of the window embeddings (the sampled positions).
 int iq_lp_sample_rows(iq_ctx* ctx, const __nv_bfloat16* W, const float* nW, int64_t P,
                       __nv_bfloat16* Ws, float* nWs);
@@ -540,12 +754,12 @@ int iq_lp_shortlist(iq_ctx* ctx, const __nv_bfloat16* W, const float* nW, int64_
                     const __nv_bfloat16* Ws, const float* nWs, const __nv_bfloat16* T,
                     const float* nT, int N, int64_t k, float* tau, float* dense, int32_t* list,
                     int32_t* cnt, int cap);
-int iq_lp_pick(iq_ctx* ctx, const float* img, Dim3 imgd, Dim3 dist, const LpColumn* cols, int N,
+int iq_lp_pick(iq_ctx* ctx, const LpImg& im, Dim3 dist, const LpColumn* cols, int N,
                const int32_t* list, const int32_t* cnt, int cap, float* dl, double tol,
                uint64_t seed, int64_t* rind, int64_t* ncand, int maxK);
 int iq_lp_template_features(iq_ctx* ctx, const LpGeo& g, const float* grid, Dim3 gdims,
                             const int64_t* tsrc, const int* tbox, int64_t n, float* out);
-int iq_lp_recall(iq_ctx* ctx, const float* img, Dim3 imgd, Dim3 dist, const LpColumn& col,
+int iq_lp_recall(iq_ctx* ctx, const LpImg& im, Dim3 dist, const LpColumn& col,
                  const int32_t* list, const int32_t* cnt, int cap, double tol, float* Dbuf,
                  unsigned* dmin, uint32_t* bits, unsigned long long* counters);
 void iq_lp_free(iq_ctx* ctx);

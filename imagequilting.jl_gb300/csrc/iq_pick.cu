@@ -260,6 +260,28 @@ __device__ void bitonic_sort(unsigned long long* buf, int n) {
   }
 }
 
+// Bitonic sort of (key, val) pairs by (key, val), n <= 8192 (key/val hold the next power of two).
+__device__ void bitonic_sort_kv(unsigned long long* key, uint32_t* val, int n) {
+  int n2 = 2;
+  while (n2 < n) n2 <<= 1;
+  for (int i = n + threadIdx.x; i < n2; i += PT) { key[i] = ~0ull; val[i] = 0xFFFFFFFFu; }
+  __syncthreads();
+  for (int k = 2; k <= n2; k <<= 1) {
+    for (int j = k >> 1; j > 0; j >>= 1) {
+      for (int i = threadIdx.x; i < n2; i += PT) {
+        const int l = i ^ j;
+        if (l > i) {
+          const unsigned long long a = key[i], b = key[l];
+          const uint32_t va = val[i], vb = val[l];
+          const bool gt = a > b || (a == b && va > vb);
+          if (gt == ((i & k) == 0)) { key[i] = b; key[l] = a; val[i] = vb; val[l] = va; }
+        }
+      }
+      __syncthreads();
+    }
+  }
+}
+
 // Histogram select of the k-th smallest (value, index) key of up to two sources at once.
 // mn/mx: bits of the smallest value and of the largest finite value of each source.
 struct SelReq {
@@ -407,6 +429,8 @@ __device__ __noinline__ void hist_select(Smem& s, uint32_t* hist, unsigned long 
   }
 }
 
+constexpr double TIE_RTOL = 1e-6;                 // relative window of a reported near-tie
+
 // Ordered compaction of {p : pred(p)} into out (if non-null); returns the count.
 template <typename Pred>
 __device__ int64_t compact(Smem& s, const Pred& pred, int64_t P, int32_t* out) {
@@ -429,9 +453,13 @@ __device__ int64_t compact(Smem& s, const Pred& pred, int64_t P, int32_t* out) {
 }
 
 struct ThrPred {
-  const float* D; double thr;
-  double tiew;                        // near-tie window 1e-6 thr (0: none)
-  mutable unsigned long long nt = 0;  // this thread's near-ties |D - thr| <= tiew
+  const float* D;
+  float thr;                          // f_dn of the Float64 threshold
+  float tlo, thi;                     // near-ties |D - thr| <= 1e-6 thr (Float64): tlo <= D <= thi
+  mutable unsigned long long nt = 0;  // this thread's near-ties
+  __device__ ThrPred(const float* d, double t, bool ties) : D(d), thr(f_dn(t)), tlo(1.f), thi(0.f) {
+    if (ties && t > 0.0 && t < 1e300) tie_window_f(t, __dmul_rn(TIE_RTOL, t), tlo, thi);
+  }
   // bit i set when D[p0 + i] <= thr (positions past P excluded)
   __device__ uint32_t eval8(int64_t p0, int64_t P) const {
     float v[CITEMS];
@@ -440,8 +468,8 @@ struct ThrPred {
     uint32_t bits = 0;
 #pragma unroll
     for (int i = 0; i < CITEMS; ++i) {
-      if (p0 + i < P && (double)v[i] <= thr) bits |= 1u << i;
-      if (tiew > 0.0 && p0 + i < P && fabs(__dsub_rn((double)v[i], thr)) <= tiew) nt++;
+      if (p0 + i < P && v[i] <= thr) bits |= 1u << i;
+      if (p0 + i < P && v[i] >= tlo && v[i] <= thi) nt++;
     }
     return bits;
   }
@@ -453,12 +481,16 @@ struct Band {
   double lo, hi;
   int32_t* list;
   int64_t n;
+  float lof, hif;  // f_up(lo), f_dn(hi): the same tests on the FP32 values
 };
 
+__device__ __forceinline__ Band make_band(double lo, double hi, int32_t* list, int64_t n) {
+  return Band{lo, hi, list, n, f_up(lo), f_dn(hi)};
+}
+
 __device__ __forceinline__ bool band_member(const Band& b, int64_t p, float d) {
-  const double dv = (double)d;
-  if (dv < b.lo) return true;
-  if (dv > b.hi) return false;
+  if (d < b.lof) return true;
+  if (d > b.hif) return false;
   int64_t lo = 0, hi = b.n - 1;
   while (lo <= hi) {
     const int64_t mid = (lo + hi) >> 1;
@@ -666,7 +698,6 @@ __device__ __noinline__ unsigned long long dense_ranks(Smem& s, unsigned long lo
 // =============================================================================================
 constexpr double RU32 = 5.9604644775390625e-08;  // 2^-24
 constexpr double RU64 = 1.1102230246251565e-16;  // 2^-53
-constexpr double TIE_RTOL = 1e-6;                 // relative window of a reported near-tie
 constexpr double TINY32 = 1.401298464324817e-45;  // smallest FP32 subnormal
 
 // One map of one realization, as the re-rank reads it.
@@ -766,8 +797,9 @@ __device__ __forceinline__ void ref_term_c(const Ref& f, const RefCache& c, int6
   }
 }
 
-// Warp-collective: value and radius of D[p] at `level` (every lane gets the same result). Each
-// lane keeps four loads in flight (the image is L2-resident; the loop is bound by its latency).
+// Warp-collective: value and radius of D[p] at `level` (every lane gets the same result). The
+// image is L2-resident and the loop is bound by the latency of its loads, so each lane issues
+// sixteen of them (level 1; four at level 2) before it uses the first.
 __device__ __noinline__ void ref_eval(const Ref& f, const RefCache& c, int64_t p, int level,
                                       double& v, double& r) {
   const int lane = threadIdx.x & 31;
@@ -777,18 +809,15 @@ __device__ __noinline__ void ref_eval(const Ref& f, const RefCache& c, int64_t p
   if (level <= 1) {
     float acc = 0.f;
     int j = lane;
-    for (; j + 96 < f.K; j += 128) {
-      float a0, b0, a1, b1, a2, b2, a3, b3;
-      ref_term_c(f, c, base, j, a0, b0);
-      ref_term_c(f, c, base, j + 32, a1, b1);
-      ref_term_c(f, c, base, j + 64, a2, b2);
-      ref_term_c(f, c, base, j + 96, a3, b3);
-      const float d0 = __fsub_rn(a0, b0), d1 = __fsub_rn(a1, b1);
-      const float d2 = __fsub_rn(a2, b2), d3 = __fsub_rn(a3, b3);
-      acc = __fmaf_rn(d0, d0, acc);
-      acc = __fmaf_rn(d1, d1, acc);
-      acc = __fmaf_rn(d2, d2, acc);
-      acc = __fmaf_rn(d3, d3, acc);
+    for (; j + 15 * 32 < f.K; j += 16 * 32) {
+      float ta[16], tb[16];
+#pragma unroll
+      for (int u = 0; u < 16; ++u) ref_term_c(f, c, base, j + 32 * u, ta[u], tb[u]);
+#pragma unroll
+      for (int u = 0; u < 16; ++u) {
+        const float d = __fsub_rn(ta[u], tb[u]);
+        acc = __fmaf_rn(d, d, acc);
+      }
     }
     for (; j < f.K; j += 32) {
       float a, b;
@@ -803,15 +832,17 @@ __device__ __noinline__ void ref_eval(const Ref& f, const RefCache& c, int64_t p
   } else if (level == 2) {
     float h = 0.f, l = 0.f;
     int j = lane;
-    for (; j < f.K; j += 64) {
-      float a0, b0, a1 = 0.f, b1 = 0.f;
-      ref_term_c(f, c, base, j, a0, b0);
-      const bool two = j + 32 < f.K;
-      if (two) ref_term_c(f, c, base, j + 32, a1, b1);
+    for (; j < f.K; j += 128) {
+      float ta[4], tb[4];
 #pragma unroll
-      for (int u = 0; u < 2; ++u) {
-        if (u == 1 && !two) break;
-        const float a = u ? a1 : a0, b = u ? b1 : b0;
+      for (int u = 0; u < 4; ++u) {
+        ta[u] = 0.f; tb[u] = 0.f;
+        if (j + 32 * u < f.K) ref_term_c(f, c, base, j + 32 * u, ta[u], tb[u]);
+      }
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        if (j + 32 * u >= f.K) break;
+        const float a = ta[u], b = tb[u];
         float dh, dl;
         two_sum(a, -b, dh, dl);                               // a - b = dh + dl exactly
         const float p2 = __fmul_rn(dh, dh);
@@ -866,6 +897,7 @@ struct RefArr {
   double* r;
   uint8_t* l;     // level (low 7 bits), 0x80 = to be raised
   uint8_t* link;  // 1 where sorted positions t and t + 1 were re-evaluated together
+  unsigned* ev;   // shared-memory counts of evaluations per level [4] (nullable)
 };
 
 // Level 1 for entries [0, n) of pos (warp per entry).
@@ -875,7 +907,32 @@ __device__ __noinline__ void ref_init(const Ref& f, const int32_t* pos, int64_t 
   for (int64_t i = warp; i < n; i += NW) {
     double v, r;
     ref_eval(f, c, pos[i] & 0x7FFFFFFF, 1, v, r);
-    if (lane == 0) { a.v[i] = v; a.r[i] = r; a.l[i] = 1; }
+    if (lane == 0) {
+      a.v[i] = v; a.r[i] = r; a.l[i] = 1;
+      if (a.ev) atomicAdd(a.ev + 1, 1u);
+    }
+  }
+  __syncthreads();
+}
+
+// Level 0 for entries [0, n) of pos: the map's own FP32 value with its error bound, a radius R
+// with E(v + R) <= R for the increasing bound E(D) of the map at distance D (then |D - v| <= R
+// wherever D - E(D) increases past v + R, checked below); entries without one get R = Inf.
+__device__ __noinline__ void ref_init0(const Ref& f, const float* __restrict__ src, const int32_t* pos,
+                                       int64_t n, RefArr a) {
+  const double sb = sqrt(fmax(f.b2, 0.0));
+  const double dmin = f.kappa < 0.5 ? (f.kappa * sb / (1.0 - f.kappa)) * (f.kappa * sb / (1.0 - f.kappa)) * 1.01 : 1e308;
+  for (int64_t i = threadIdx.x; i < n; i += PT) {
+    const double v = (double)src[pos[i] & 0x7FFFFFFF];
+    double R = 1.5 * tier0_bound(f, v);
+    bool ok = false;
+    for (int it = 0; it < 6; ++it) {
+      const double need = tier0_bound(f, v + R);
+      if (need <= R) { ok = true; break; }
+      R = fmax(need, 1.5 * R);
+    }
+    if (!ok || !(v + R > dmin) || !(v < 1e300)) R = __longlong_as_double(0x7FF0000000000000ll);
+    a.v[i] = v; a.r[i] = R; a.l[i] = 0;
   }
   __syncthreads();
 }
@@ -890,7 +947,10 @@ __device__ __noinline__ void ref_raise(const Ref& f, const int32_t* pos, int64_t
     const int nl = to3 ? 3 : min((l & 0x7F) + 1, 3);
     double v, r;
     ref_eval(f, c, pos[i] & 0x7FFFFFFF, nl, v, r);
-    if (lane == 0) { a.v[i] = v; a.r[i] = r; a.l[i] = (uint8_t)nl; }
+    if (lane == 0) {
+      a.v[i] = v; a.r[i] = r; a.l[i] = (uint8_t)nl;
+      if (a.ev) atomicAdd(a.ev + nl, 1u);
+    }
   }
   __syncthreads();
 }
@@ -951,6 +1011,23 @@ __device__ __noinline__ void ref_resolve(Smem& s, const Ref& f, const int32_t* p
       if (a.link[t]) { ref_mark(a, ord[t]); ref_mark(a, ord[t + 1]); }
     __syncthreads();
     ref_raise(f, pos, n, a, round >= 3);
+    if (n <= SORT_CAP) {
+      // the whole order by (Float64 value, entry) in shared memory (values are >= 0, so their
+      // bits order like the values)
+      extern __shared__ __align__(16) unsigned char dyn[];
+      uint32_t* val = reinterpret_cast<uint32_t*>(dyn);
+      unsigned long long* key = reinterpret_cast<unsigned long long*>(dyn + 2 * NBIN * 4);
+      for (int64_t t = threadIdx.x; t < n; t += PT) {
+        const uint32_t i = ord[t];
+        key[t] = (unsigned long long)__double_as_longlong(a.v[i]);
+        val[t] = i;
+      }
+      __syncthreads();
+      bitonic_sort_kv(key, val, (int)n);
+      for (int64_t t = threadIdx.x; t < n; t += PT) ord[t] = val[t];
+      __syncthreads();
+      continue;
+    }
     // runs of linked neighbours [t, e]: insertion sort by (value, position)
     for (int64_t t = threadIdx.x; t + 1 < n; t += PT) {
       if (!a.link[t] || (t > 0 && a.link[t - 1])) continue;
@@ -1062,15 +1139,16 @@ __device__ __noinline__ int64_t band_collect(Smem& s, const float* __restrict__ 
   int64_t base = 0;
   unsigned long long nb = 0;
   const int64_t tile = (int64_t)PT * CITEMS;
+  const float lof = f_up(lo), hif = f_dn(hi);
   for (int64_t t0 = 0; t0 < P; t0 += tile) {
     const int64_t p0 = t0 + (int64_t)threadIdx.x * CITEMS;
     uint32_t bits = 0;
 #pragma unroll
     for (int i = 0; i < CITEMS; ++i) {
       if (p0 + i >= P) continue;
-      const double d = (double)src[p0 + i];
-      if (d < lo) nb++;
-      else if (d <= hi) bits |= 1u << i;
+      const float d = src[p0 + i];
+      if (d < lof) nb++;
+      else if (d <= hif) bits |= 1u << i;
     }
     uint32_t total;
     const uint32_t off = block_excl_sum(s, (uint32_t)__popc(bits), total);
@@ -1103,6 +1181,8 @@ __device__ __noinline__ long long band_topk(Smem& s, unsigned long long* sbuf, c
   }
   b.lo = v - 2.0 * E;
   b.hi = v + 2.0 * E;
+  b.lof = f_up(b.lo);
+  b.hif = f_dn(b.hi);
   b.list = list;
   int64_t below = 0;
   b.n = band_collect(s, src, P, b.lo, b.hi, list, below);
@@ -1190,10 +1270,11 @@ __device__ __noinline__ unsigned long long count_near(Smem& s, const float* __re
                                          double t) {
   unsigned long long c = 0;
   if (t > 0.0 && t < 1e300) {
-    const double w = __dmul_rn(TIE_RTOL, t);
+    float lo, hi;
+    tie_window_f(t, __dmul_rn(TIE_RTOL, t), lo, hi);
     for (int64_t p = threadIdx.x; p < P; p += PT) {
-      const double d = (double)src[p];
-      if (d < 1e300 && fabs(__dsub_rn(d, t)) <= w) c++;
+      const float d = src[p];
+      if (d >= lo && d <= hi && d < __int_as_float(0x7F800000)) c++;
     }
   }
   return block_sum_u64(s, c);
@@ -1203,10 +1284,11 @@ __device__ __noinline__ unsigned long long count_near(Smem& s, const float* __re
 // returns the sum of (n - rank + 1). Ties of the Float64 distance share a rank.
 // `have`: the intervals of the candidates are in `a` already (the refined threshold pick).
 __device__ __noinline__ unsigned long long dense_ranks_refined(Smem& s, unsigned long long* sbuf, const Ref& f,
+                                                  const float* __restrict__ src,
                                                   const int32_t* cand, int64_t n, RefArr a,
                                                   bool have, uint32_t* k0, uint32_t* v0,
                                                   uint32_t* k1, uint32_t* v1, uint32_t* rank) {
-  if (!have) ref_init(f, cand, n, a);
+  if (!have) ref_init0(f, src, cand, n, a);
   uint32_t* ord = const_cast<uint32_t*>(ref_sort(s, sbuf, n, a, k0, v0, k1, v1));
   ref_resolve(s, f, cand, n, ord, a);
   uint32_t carry = 0;
@@ -1378,6 +1460,12 @@ __global__ void __launch_bounds__(PT) pick_kernel(const PickArgs a) {
   ra.l = a.rl ? a.rl + 2 * b * P : nullptr;
   ra.link = a.rl ? a.rl + 2 * b * P + P : nullptr;
   const bool can_ref = a.rv != nullptr;
+  __shared__ unsigned evc[4];
+  __shared__ long long tband;
+  ra.ev = a.stats ? evc : nullptr;
+  if (threadIdx.x < 4) evc[threadIdx.x] = 0;
+  if (threadIdx.x == 0) tband = 0;
+  __syncthreads();
   __shared__ Band sband[1 + (NAUX > 0 ? NAUX : 1)];
   unsigned long long ties = 0;
 
@@ -1393,7 +1481,7 @@ __global__ void __launch_bounds__(PT) pick_kernel(const PickArgs a) {
       have0 = true;
     } else {
       const double thr = __dmul_rn(__dadd_rn(1.0, a.tol), (double)mn);
-      ThrPred pr{D, thr, (thr > 0.0 && thr < 1e300) ? __dmul_rn(TIE_RTOL, thr) : 0.0};
+      ThrPred pr(D, thr, true);
       n = compact(s, pr, P, cand);
       ties += block_sum_u64(s, pr.nt);
     }
@@ -1439,7 +1527,7 @@ __global__ void __launch_bounds__(PT) pick_kernel(const PickArgs a) {
         pr.kD = Key{(uint32_t)(pb.key >> 32), (uint32_t)pb.key};
         if (pb.ok == 1) {
           if (threadIdx.x == 0)
-            sband[0] = Band{pb.lo, pb.hi, const_cast<int32_t*>(tk.x0_pool) + pb.off, pb.n};
+            sband[0] = make_band(pb.lo, pb.hi, const_cast<int32_t*>(tk.x0_pool) + pb.off, pb.n);
           __syncthreads();
           pr.bD = &sband[0];
           tiesD = pb.ties;
@@ -1459,8 +1547,10 @@ __global__ void __launch_bounds__(PT) pick_kernel(const PickArgs a) {
         }
         pr.kD = res[0];
         if (ref0 && !allzero && dbsize < P) {
+          const long long tb0 = prof ? clock64() : 0;
           const long long t = band_topk(s, sbuf, f0, D, P, dbsize, pr.kD, blist, ra, k0, v0, k1,
                                         v1, sband[0]);
+          if (prof) tband += clock64() - tb0;
           if (t >= 0) {
             pr.bD = &sband[0];
             boff = sband[0].n;
@@ -1479,7 +1569,7 @@ __global__ void __launch_bounds__(PT) pick_kernel(const PickArgs a) {
           const PreBand& pb = tk.aux_pb[j][q];
           pr.ka[j] = Key{(uint32_t)(pb.key >> 32), (uint32_t)pb.key};
           if (threadIdx.x == 0)
-            sband[1 + j] = Band{pb.lo, pb.hi, const_cast<int32_t*>(tk.pb_pool) + pb.off, pb.n};
+            sband[1 + j] = make_band(pb.lo, pb.hi, const_cast<int32_t*>(tk.pb_pool) + pb.off, pb.n);
           __syncthreads();
           pr.ba[j] = &sband[1 + j];
           tiesA[j] = pb.ties;
@@ -1505,8 +1595,10 @@ __global__ void __launch_bounds__(PT) pick_kernel(const PickArgs a) {
             continue;
           }
           const Ref fa = make_ref(tk.xa[j], r, a.dx, a.dxy);
+          const long long tb0 = prof ? clock64() : 0;
           const long long t = band_topk(s, sbuf, fa, aux[j], P, sz, pr.ka[j], blist + aoff, ra,
                                         k0, v0, k1, v1, sband[1 + j]);
+          if (prof) tband += clock64() - tb0;
           if (t >= 0) {
             pr.ba[j] = &sband[1 + j];
             aoff += sband[1 + j].n;
@@ -1570,7 +1662,7 @@ __global__ void __launch_bounds__(PT) pick_kernel(const PickArgs a) {
     unsigned long long S;
     if (can_ref && ref_on(xs)) {
       const Ref f = make_ref(xs, r, a.dx, a.dxy);
-      S = dense_ranks_refined(s, sbuf, f, cand, n, ra, j == 0 && have0, k0, v0, k1, v1, rankbuf);
+      S = dense_ranks_refined(s, sbuf, f, src, cand, n, ra, j == 0 && have0, k0, v0, k1, v1, rankbuf);
     } else {
       S = dense_ranks(s, sbuf, src, cand, n, k0, v0, k1, v1, rankbuf);
     }
@@ -1587,7 +1679,11 @@ __global__ void __launch_bounds__(PT) pick_kernel(const PickArgs a) {
   __syncthreads();
 
   const long long t2 = prof ? clock64() : 0;
-  if (prof) atomicAdd(a.stats + ST_PICK_TW, (unsigned long long)(t2 - t1));
+  if (prof) {
+    atomicAdd(a.stats + ST_PICK_TW, (unsigned long long)(t2 - t1));
+    atomicAdd(a.stats + ST_PICK_TBAND, (unsigned long long)tband);
+    for (int l = 1; l < 4; ++l) atomicAdd(a.stats + ST_PICK_EV1 + l - 1, (unsigned long long)evc[l]);
+  }
   // ---- weighted draw ----
   const int64_t nch = (n + IQ_DRAW_CHUNK - 1) / IQ_DRAW_CHUNK;
   double* csum = prod;  // reuse
@@ -1776,6 +1872,7 @@ __global__ void __launch_bounds__(PT) select_bands_kernel(const BandArgs a) {
     ra.r = a.rr + b * P;
     ra.l = a.rl + 2 * b * P;
     ra.link = ra.l + P;
+    ra.ev = nullptr;
     int32_t* list = a.list + b * P;
     ties = band_topk(s, sbuf, f, src, P, k, key, list, ra, a.k0 + b * P, a.v0 + b * P,
                      a.k1 + b * P, a.v1 + b * P, band);

@@ -851,33 +851,20 @@ __global__ void lp_template_features_kernel(LpGeo g, const float* grid, const in
   }
 }
 
-// Exact (integer data) distance of one column at every position, and its minimum (the monitor).
-__global__ void __launch_bounds__(256) lp_full_kernel(const float* __restrict__ img, int64_t isx,
-                                                      int64_t isxy, int64_t dx, int64_t dxy,
+// Exact distance (byte-valued image, integer sums) of one column at every position, and its
+// minimum (the monitor). A column whose template values are not bytes leaves dmin at +Inf.
+__global__ void __launch_bounds__(256) lp_full_kernel(const LpImg im, int64_t dx, int64_t dxy,
                                                       int64_t P, LpColumn col, float* D,
                                                       unsigned* dmin) {
   extern __shared__ __align__(16) unsigned char dyn[];
-  int32_t* off = reinterpret_cast<int32_t*>(dyn);
-  float* tv = reinterpret_cast<float*>(dyn + 4 * (size_t)col.K);
-  for (int j = threadIdx.x; j < col.K; j += blockDim.x) {
-    const uint32_t k = col.klist[j];
-    const int kx = kx_of(k), ky = ky_of(k), kz = kz_of(k);
-    off[j] = (int32_t)(kx + isx * ky + isxy * kz);
-    tv[j] = col.tmpl[kx + col.tgx * ky + col.tgxy * kz];
-  }
-  __syncthreads();
+  uint4* qd = reinterpret_cast<uint4*>(dyn);
+  if (!iq_stage(im, col, qd)) return;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   unsigned mn = 0x7F800000u;
   for (int64_t p = (int64_t)blockIdx.x * 8 + warp; p < P; p += (int64_t)gridDim.x * 8) {
     const int64_t z = p / dxy, r = p - z * dxy, y = r / dx, x = r - y * dx;
-    const float* base = img + x + isx * y + isxy * z;
-    float acc = 0.f;
-    for (int j = lane; j < col.K; j += 32) {
-      const float d = base[off[j]] - tv[j];
-      acc = fmaf(d, d, acc);
-    }
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    const uint32_t s = iq_lp_ssd(im, col, qd, x, y, z, [] { return INFINITY; });
+    const float acc = (float)s;
     if (lane == 0) D[p] = acc;
     mn = min(mn, __float_as_uint(acc));
   }
@@ -893,11 +880,12 @@ __global__ void lp_mark_kernel(const int32_t* list, const int32_t* cnt, int cap,
 // counters[0] += |{D <= (1 + tol) min D}|, counters[1] += those in the shortlist
 __global__ void lp_recall_kernel(const float* D, const unsigned* dmin, int64_t P, double tol,
                                  const uint32_t* bits, unsigned long long* counters) {
-  const double thr = __dmul_rn(__dadd_rn(1.0, tol), (double)__uint_as_float(*dmin));
+  if (*dmin >= 0x7F800000u) return;  // the column was not evaluated
+  const float thr = f_dn(__dmul_rn(__dadd_rn(1.0, tol), (double)__uint_as_float(*dmin)));
   unsigned long long t = 0, h = 0;
   for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < P;
        p += (int64_t)gridDim.x * blockDim.x) {
-    if ((double)D[p] <= thr) {
+    if (D[p] <= thr) {
       t++;
       if (bits[p >> 5] >> (p & 31) & 1u) h++;
     }
@@ -913,6 +901,71 @@ __global__ void lp_recall_kernel(const float* D, const unsigned* dmin, int64_t P
 }
 
 }  // namespace
+
+namespace {
+// The image as bytes; *bad = 1 when a value is not an integer in [0, 255].
+__global__ void lp_to_u8_kernel(const float* __restrict__ src, int64_t n, uint8_t* dst, int* bad) {
+  int b = 0;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const float v = src[i];
+    const bool ok = v >= 0.f && v <= 255.f && v == floorf(v);
+    dst[i] = ok ? (uint8_t)v : 0;
+    b |= !ok;
+  }
+  if (__syncthreads_or(b) && threadIdx.x == 0) atomicOr(bad, 1);
+}
+}  // namespace
+
+namespace {
+// Plane form of an image of codes 0..3 (see LpImg); *bad = 1 for any other value.
+__global__ void lp_to_planes_kernel(const float* __restrict__ src, Dim3 d, int64_t ntx, int64_t nty,
+                                    unsigned long long* dst, int* bad) {
+  const int64_t nw = d.z * nty * ntx * 16;
+  int b = 0;
+  for (int64_t w = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; w < nw;
+       w += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t yr = w & 15, t = w >> 4;
+    const int64_t tx = t % ntx, ty = (t / ntx) % nty, z = t / (ntx * nty);
+    const int64_t y = ty * 16 + yr;
+    uint32_t p0 = 0, p1 = 0;
+    if (y < d.y) {
+      for (int i = 0; i < 32; ++i) {
+        const int64_t x = tx * 32 + i;
+        if (x >= d.x) break;
+        const float v = src[x + d.x * y + d.x * d.y * z];
+        if (!(v == 0.f || v == 1.f || v == 2.f || v == 3.f)) b = 1;
+        const uint32_t c = (uint32_t)v & 3u;
+        p0 |= (c & 1u) << i;
+        p1 |= (c >> 1) << i;
+      }
+    }
+    dst[w] = (unsigned long long)p0 | ((unsigned long long)p1 << 32);
+  }
+  if (__syncthreads_or(b) && threadIdx.x == 0) atomicOr(bad, 1);
+}
+}  // namespace
+
+int iq_lp_to_planes(iq_ctx* ctx, const float* src, Dim3 d, int64_t ntx, int64_t nty,
+                    unsigned long long* dst, int* bad) {
+  IQ_CUDA_OK(cudaMemsetAsync(bad, 0, sizeof(int), ctx->stream));
+  const int64_t nw = d.z * nty * ntx * 16;
+  lp_to_planes_kernel<<<(unsigned)std::min<int64_t>((nw + 255) / 256, 4096), 256, 0, ctx->stream>>>(
+      src, d, ntx, nty, dst, bad);
+  iq_count(ctx);
+  IQ_CUDA_OK(cudaGetLastError());
+  return IQ_OK;
+}
+
+int iq_lp_to_u8(iq_ctx* ctx, const float* src, int64_t n, uint8_t* dst, int* bad) {
+  IQ_CUDA_OK(cudaMemsetAsync(bad, 0, sizeof(int), ctx->stream));
+  IQ_CUDA_OK(cudaMemsetAsync(dst + n, 0, 16, ctx->stream));
+  lp_to_u8_kernel<<<(unsigned)std::min<int64_t>((n + 255) / 256, 4096), 256, 0, ctx->stream>>>(
+      src, n, dst, bad);
+  iq_count(ctx);
+  IQ_CUDA_OK(cudaGetLastError());
+  return IQ_OK;
+}
 
 int iq_lp_sample_rows(iq_ctx* ctx, const __nv_bfloat16* W, const float* nW, int64_t P,
                       __nv_bfloat16* Ws, float* nWs) {
@@ -967,11 +1020,11 @@ int iq_lp_template_features(iq_ctx* ctx, const LpGeo& g, const float* grid, Dim3
   return IQ_OK;
 }
 
-int iq_lp_recall(iq_ctx* ctx, const float* img, Dim3 imgd, Dim3 dist, const LpColumn& col,
+int iq_lp_recall(iq_ctx* ctx, const LpImg& im, Dim3 dist, const LpColumn& col,
                  const int32_t* list, const int32_t* cnt, int cap, double tol, float* Dbuf,
                  unsigned* dmin, uint32_t* bits, unsigned long long* counters) {
   const int64_t P = dist.vol();
-  const size_t sm = (size_t)8 * col.K + 16;
+  const size_t sm = (size_t)16 * (im.b2 ? (size_t)col.tdim[1] * col.tdim[2] : (size_t)col.nq) + 16;
   if (sm > 227 * 1024) return iq_set_error(IQ_ERR_LIMIT, "recall check: mask too large");
   IQ_CUDA_OK(cudaFuncSetAttribute(lp_full_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
   const unsigned inf = 0x7F800000u;
@@ -979,7 +1032,7 @@ int iq_lp_recall(iq_ctx* ctx, const float* img, Dim3 imgd, Dim3 dist, const LpCo
   IQ_CUDA_OK(cudaMemsetAsync(bits, 0, sizeof(uint32_t) * ((P + 31) / 32), ctx->stream));
   iq_timer_start(ctx, "lp.monitor");
   lp_full_kernel<<<(unsigned)std::min<int64_t>((P + 7) / 8, 152 * 8), 256, sm, ctx->stream>>>(
-      img, imgd.x, imgd.x * imgd.y, dist.x, dist.x * dist.y, P, col, Dbuf, dmin);
+      im, dist.x, dist.x * dist.y, P, col, Dbuf, dmin);
   lp_mark_kernel<<<64, 256, 0, ctx->stream>>>(list, cnt, cap, bits);
   lp_recall_kernel<<<(unsigned)std::min<int64_t>((P + 255) / 256, 1024), 256, 0, ctx->stream>>>(
       Dbuf, dmin, P, tol, bits, counters);

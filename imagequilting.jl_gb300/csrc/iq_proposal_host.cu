@@ -15,6 +15,7 @@
 namespace {
 
 constexpr int NPOS = 8;  // positives kept per captured pair (candidates of its pick)
+constexpr double kMonMinTrue = 1000;  // sampled candidates before the recall decides a fallback
 
 struct LpCache {
   int32_t lohi[6];
@@ -40,6 +41,15 @@ struct IqLp {
   double* ii1 = nullptr;  // Float64 integral image of the values
   size_t ii1_bytes = 0;
   int64_t ii1_ti = -1;
+  uint8_t* ti8 = nullptr;  // the image as bytes (the exact sums of the shortlist pick)
+  size_t ti8_bytes = 0;
+  int64_t ti8_ti = -1;
+  bool ti8_ok = false;
+  unsigned long long* ti2 = nullptr;  // plane form (codes 0..3)
+  size_t ti2_words = 0;
+  int64_t ti2_ntx = 0, ti2_nty = 0;
+  bool ti2_ok = false;
+  int* d_bad = nullptr;
   std::vector<LpCache> cache;
   int64_t cache_ti = -1, cache_w = -1;
   // captured pairs: features of the template, its mask box, NPOS candidate positions
@@ -136,6 +146,94 @@ int ensure_ii1(iq_ctx* ctx, IqLp* lp) {
   return IQ_OK;
 }
 
+// The image as bytes, when every value is an integer in [0, 255] (categorical codes).
+int ensure_ti8(iq_ctx* ctx, IqLp* lp) {
+  if (lp->ti8_ti == ctx->ti_version) return IQ_OK;
+  const int64_t n = ctx->ti.vol();
+  const size_t bytes = (size_t)n + 16;
+  if (lp->ti8_bytes < bytes || !lp->d_bad) {
+    cudaFree(lp->ti8);
+    lp->ti8 = nullptr;
+    lp->ti8_bytes = 0;
+    if (cudaMalloc(&lp->ti8, bytes) != cudaSuccess ||
+        (!lp->d_bad && cudaMalloc(&lp->d_bad, sizeof(int)) != cudaSuccess)) {
+      cudaGetLastError();
+      return iq_set_error(IQ_ERR_ALLOC, "proposal: byte image allocation failed");
+    }
+    lp->ti8_bytes = bytes;
+  }
+  int rc = iq_lp_to_u8(ctx, ctx->d_ti, n, lp->ti8, lp->d_bad);
+  if (rc) return rc;
+  int bad = 1;
+  IQ_CUDA_OK(cudaMemcpyAsync(&bad, lp->d_bad, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  IQ_CUDA_OK(cudaStreamSynchronize(ctx->stream));
+  lp->ti8_ok = bad == 0;
+  // plane form when the codes are 0..3
+  lp->ti2_ok = false;
+  if (lp->ti8_ok) {
+    const int64_t ntx = (ctx->ti.x + 31) / 32 + 1, nty = (ctx->ti.y + 15) / 16;
+    const size_t words = (size_t)(ctx->ti.z * nty * ntx * 16);
+    if (lp->ti2_words < words) {
+      cudaFree(lp->ti2);
+      lp->ti2 = nullptr;
+      lp->ti2_words = 0;
+      if (cudaMalloc(&lp->ti2, sizeof(unsigned long long) * words) != cudaSuccess) {
+        cudaGetLastError();
+        return iq_set_error(IQ_ERR_ALLOC, "proposal: plane image allocation failed");
+      }
+      lp->ti2_words = words;
+    }
+    rc = iq_lp_to_planes(ctx, ctx->d_ti, ctx->ti, ntx, nty, lp->ti2, lp->d_bad);
+    if (rc) return rc;
+    IQ_CUDA_OK(cudaMemcpyAsync(&bad, lp->d_bad, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    IQ_CUDA_OK(cudaStreamSynchronize(ctx->stream));
+    lp->ti2_ok = bad == 0;
+    lp->ti2_ntx = ntx;
+    lp->ti2_nty = nty;
+  }
+  lp->ti8_ti = ctx->ti_version;
+  return IQ_OK;
+}
+
+// The form the exact sums read: planes for codes 0..3 and tiles of x extent <= 32, else bytes.
+LpImg lp_image(iq_ctx* ctx, IqLp* lp, Dim3 tile) {
+  LpImg im{};
+  im.b8 = lp->ti8;
+  im.isx = ctx->ti.x;
+  im.isxy = ctx->ti.x * ctx->ti.y;
+  if (lp->ti2_ok && tile.x <= 32) {
+    im.b2 = lp->ti2;
+    im.ntx = lp->ti2_ntx;
+    im.nty = lp->ti2_nty;
+  }
+  return im;
+}
+
+// Quads of the mask "tile minus box [lo, hi)": rows in (z, y, x) order, four x offsets from a
+// multiple of 4, image strides (isx, isxy), template strides (tgx, tgxy).
+void make_quads(Dim3 tile, const int32_t* lohi, int64_t isx, int64_t isxy, int64_t tgx,
+                int64_t tgxy, std::vector<LpQuad>& out) {
+  for (int64_t z = 0; z < tile.z; ++z)
+    for (int64_t y = 0; y < tile.y; ++y)
+      for (int64_t x4 = 0; x4 < tile.x; x4 += 4) {
+        uint32_t m = 0;
+        for (int b = 0; b < 4; ++b) {
+          const int64_t x = x4 + b;
+          if (x >= tile.x) break;
+          const bool inner = x >= lohi[0] && x < lohi[3] && y >= lohi[1] && y < lohi[4] &&
+                             z >= lohi[2] && z < lohi[5];
+          if (!inner) m |= 0xFFu << (8 * b);
+        }
+        if (!m) continue;
+        LpQuad q;
+        q.off = (int32_t)(x4 + isx * y + isxy * z);
+        q.tx = (int32_t)(x4 + tgx * y + tgxy * z);
+        q.mask = m;
+        q.pad_ = 0;
+        out.push_back(q);
+      }
+}
+
 Dim3 dist_of(iq_ctx* ctx, Dim3 tile) {
   return Dim3{ctx->ti.x - tile.x + 1, ctx->ti.y - tile.y + 1, ctx->ti.z - tile.z + 1};
 }
@@ -184,6 +282,7 @@ void iq_lp_free(iq_ctx* ctx) {
   IqLp* lp = ctx->lp;
   if (!lp) return;
   free_cache(lp);
+  cudaFree(lp->ti8); cudaFree(lp->ti2); cudaFree(lp->d_bad);
   cudaFree(lp->w); cudaFree(lp->m); cudaFree(lp->v); cudaFree(lp->grad); cudaFree(lp->loss);
   cudaFree(lp->ii1);
   cudaFree(lp->cap_feat); cudaFree(lp->cap_box); cudaFree(lp->cap_pos);
@@ -209,7 +308,9 @@ bool iq_lp_applies(iq_ctx* ctx, Dim3 tile, int64_t maxK, bool data) {
   if (!s.narrow || s.lsbexp < 0) return false;
   const double m = (double)maxK * (double)s.amax * (double)s.amax * 4.0;
   if (!(m < 16777216.0)) return false;
-  return 8 * maxK <= 200 * 1024;
+  // byte-valued image (categorical codes): the exact sums read it as bytes
+  if (ensure_ti8(ctx, lp) || !lp->ti8_ok) return false;
+  return 16 * (maxK / 4 + 2 * tile.y * tile.z) <= 200 * 1024;
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -232,7 +333,22 @@ int iq_lp_run_chunk(iq_ctx* ctx, const LpChunk& c, int64_t chunk_index, int* don
   std::vector<int64_t> tsrc(N);
   std::vector<int32_t> tbox(6 * (size_t)N);
   std::vector<LpColumn> cols(N);
-  int maxK = 0;
+  // quad tables of the configurations present, one after another
+  std::vector<LpQuad> quads;
+  std::map<int, std::pair<size_t, int>> qcfg;  // configuration -> (first quad, count)
+  for (int i = 0; i < N; ++i) {
+    const int cf = c.cfg[i];
+    if (qcfg.count(cf)) continue;
+    const size_t q0 = quads.size();
+    make_quads(c.tile_dims, c.lohi + 6 * cf, ctx->ti.x, ctx->ti.x * ctx->ti.y, c.sim_dims.x,
+               c.sim_dims.x * c.sim_dims.y, quads);
+    qcfg[cf] = {q0, (int)(quads.size() - q0)};
+  }
+  LpQuad* dquad = (LpQuad*)iq_scratch(ctx, S_LP_QUAD, sizeof(LpQuad) * std::max<size_t>(1, quads.size()));
+  if (!dquad) return IQ_ERR_ALLOC;
+  IQ_CUDA_OK(cudaMemcpyAsync(dquad, quads.data(), sizeof(LpQuad) * quads.size(),
+                             cudaMemcpyHostToDevice, st));
+  int maxQ = 0;
   for (int q = 0; q < N; ++q) {
     const int i = ord[q];
     const int cf = c.cfg[i];
@@ -241,12 +357,18 @@ int iq_lp_run_chunk(iq_ctx* ctx, const LpChunk& c, int64_t chunk_index, int* don
     LpColumn& col = cols[q];
     col.klist = c.d_klist + (size_t)cf * c.T;
     col.K = c.cfgK[cf];
+    col.quad = dquad + qcfg[cf].first;
+    col.nq = qcfg[cf].second;
+    for (int d = 0; d < 6; ++d) col.lohi[d] = c.lohi[6 * cf + d];
+    col.tdim[0] = (int32_t)c.tile_dims.x;
+    col.tdim[1] = (int32_t)c.tile_dims.y;
+    col.tdim[2] = (int32_t)c.tile_dims.z;
+    maxQ = std::max<int>(maxQ, (int)std::max<int64_t>(col.nq, c.tile_dims.y * c.tile_dims.z));
     col.tmpl = c.sim + tsrc[q];
     col.tgx = c.sim_dims.x;
     col.tgxy = c.sim_dims.x * c.sim_dims.y;
     col.tile = c.tile[i];
     col.real = c.real[i];
-    maxK = std::max(maxK, col.K);
   }
   __nv_bfloat16* dT = (__nv_bfloat16*)iq_scratch(ctx, S_LP_T, sizeof(__nv_bfloat16) * N * IQ_LP_EMB);
   float* dnT = (float*)iq_scratch(ctx, S_LP_NT, sizeof(float) * N);
@@ -280,8 +402,9 @@ int iq_lp_run_chunk(iq_ctx* ctx, const LpChunk& c, int64_t chunk_index, int* don
     if (rc) return rc;
     q0 = q1;
   }
-  rc = iq_lp_pick(ctx, ctx->d_ti, ctx->ti, c.dist, dcols, N, dlist, dcnt, cap, ddl, c.tol, c.seed,
-                  drind, dncand, maxK);
+  const LpImg im = lp_image(ctx, lp, c.tile_dims);
+  rc = iq_lp_pick(ctx, im, c.dist, dcols, N, dlist, dcnt, cap, ddl, c.tol, c.seed,
+                  drind, dncand, maxQ);
   if (rc) return rc;
   // recall of the first column against the full exact scan, every lp_monitor-th chunk
   const bool mon = ctx->lp_monitor > 0 && chunk_index % ctx->lp_monitor == 0;
@@ -297,7 +420,7 @@ int iq_lp_run_chunk(iq_ctx* ctx, const LpChunk& c, int64_t chunk_index, int* don
       }
     }
     IQ_CUDA_OK(cudaMemsetAsync(lp->d_counters, 0, 2 * sizeof(unsigned long long), st));
-    rc = iq_lp_recall(ctx, ctx->d_ti, ctx->ti, c.dist, cols[0], dlist, dcnt, cap, c.tol, dD,
+    rc = iq_lp_recall(ctx, im, c.dist, cols[0], dlist, dcnt, cap, c.tol, dD,
                       lp->d_dmin, dbits, lp->d_counters);
     if (rc) return rc;
   }
@@ -313,7 +436,10 @@ int iq_lp_run_chunk(iq_ctx* ctx, const LpChunk& c, int64_t chunk_index, int* don
     lp->mon_cols += 1;
     lp->mon_true += (double)hcnt[0];
     lp->mon_hit += (double)hcnt[1];
-    if (ctx->lp_fallback && lp->mon_true > 0 && lp->mon_hit < 0.99 * lp->mon_true) lp->off = true;
+    // the sampled recall decides once it rests on enough candidates (a standard error of
+    // about 0.003 at recall 0.99)
+    if (ctx->lp_fallback && lp->mon_true >= kMonMinTrue && lp->mon_hit < 0.99 * lp->mon_true)
+      lp->off = true;
   }
   for (int q = 0; q < N; ++q)
     if (hr[q] < 0) return IQ_OK;  // a shortlist overflowed: the full scan takes this chunk

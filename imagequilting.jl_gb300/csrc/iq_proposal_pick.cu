@@ -4,6 +4,10 @@
 // full pick (iq_pick.cu). The distances are FP32 direct sums, exact for the integer-valued
 // (categorical) data the proposal serves; whenever the shortlist holds the full candidate set
 // the result equals the full scan's.
+//
+// Byte-valued images: the training image is read as bytes and a mask as quads of four
+// consecutive x offsets of one row; a lane forms the four differences of a quad with one
+// __vabsdiffu4 and adds their squares with one __dp4a (integer arithmetic: exact).
 #include "iq_internal.h"
 
 namespace {
@@ -12,8 +16,7 @@ constexpr int LP_PT = 1024;
 constexpr int LP_SORT = 8192;  // candidates a column's pick sorts in shared memory
 
 struct LpPickArgs {
-  const float* img;            // training image
-  int64_t isx, isxy;
+  LpImg im;                    // training image (plane or byte form)
   int64_t dx, dxy;             // distance-map strides
   const LpColumn* cols;        // per column: mask offsets, template, tile, realization
   const int32_t* list;         // shortlists [N][cap]
@@ -59,17 +62,13 @@ __global__ void __launch_bounds__(LP_PT) lp_pick_kernel(const LpPickArgs a) {
     if (threadIdx.x == 0) { a.rind[c] = -1; a.ncand[c] = 0; }
     return;
   }
-  // terms of the column's mask in shared memory
-  int32_t* off = reinterpret_cast<int32_t*>(dyn);
-  float* tv = reinterpret_cast<float*>(dyn + 4 * (size_t)col.K);
-  for (int j = threadIdx.x; j < col.K; j += LP_PT) {
-    const uint32_t k = col.klist[j];
-    const int kx = kx_of(k), ky = ky_of(k), kz = kz_of(k);
-    off[j] = (int32_t)(kx + a.isx * ky + a.isxy * kz);
-    tv[j] = col.tmpl[kx + col.tgx * ky + col.tgxy * kz];
-  }
+  // the column's rows (plane form) or quads (byte form) in shared memory
+  uint4* qd = reinterpret_cast<uint4*>(dyn);
   if (threadIdx.x == 0) smin = 0x7F7FFFFFu;
-  __syncthreads();
+  if (!iq_stage(a.im, col, qd)) {  // template values outside the form: the column falls back
+    if (threadIdx.x == 0) { a.rind[c] = -1; a.ncand[c] = 0; }
+    return;
+  }
   // An entry is abandoned once a partial sum exceeds (1 + tol) * running minimum * (1 + 2e-6):
   // the terms are non-negative and the sums exact, so its full sum lies above the final
   // threshold by more than the near-tie band and it neither sets the minimum nor is a candidate.
@@ -80,34 +79,11 @@ __global__ void __launch_bounds__(LP_PT) lp_pick_kernel(const LpPickArgs a) {
   for (int i = warp; i < n; i += LP_PT / 32) {
     const int64_t p = lst[i];
     const int64_t z = p / a.dxy, r = p - z * a.dxy, y = r / a.dx, x = r - y * a.dx;
-    const float* base = a.img + x + a.isx * y + a.isxy * z;
-    float acc = 0.f;
-    int j = lane;
-    bool pruned = false;
-    for (int nx = 0; j + 96 < col.K; j += 128) {
-      const float d0 = base[off[j]] - tv[j], d1 = base[off[j + 32]] - tv[j + 32];
-      const float d2 = base[off[j + 64]] - tv[j + 64], d3 = base[off[j + 96]] - tv[j + 96];
-      acc = fmaf(d0, d0, acc);
-      acc = fmaf(d1, d1, acc);
-      acc = fmaf(d2, d2, acc);
-      acc = fmaf(d3, d3, acc);
-      if (++nx == 4) {  // every 512 terms
-        nx = 0;
-        float part = acc;
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
-        const float bound = __uint_as_float(*(volatile unsigned*)&smin) * pf;
-        if (part > bound) { pruned = true; break; }
-      }
-    }
-    if (!pruned)
-      for (; j < col.K; j += 32) {
-        const float d = base[off[j]] - tv[j];
-        acc = fmaf(d, d, acc);
-      }
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-    if (pruned) acc = INFINITY;
+    const uint32_t s = iq_lp_ssd(a.im, col, qd, x, y, z, [&] {
+      return __uint_as_float(*(volatile unsigned*)&smin) * pf;
+    });
+    const bool pruned = s == 0xFFFFFFFFu;
+    const float acc = pruned ? INFINITY : (float)s;
     if (lane == 0) {
       dl[i] = acc;
       if (!pruned) atomicMin(&smin, __float_as_uint(acc));
@@ -129,11 +105,14 @@ __global__ void __launch_bounds__(LP_PT) lp_pick_kernel(const LpPickArgs a) {
   // candidates (position, value) and near-ties
   unsigned long long* keys = reinterpret_cast<unsigned long long*>(dyn);
   unsigned long long nt = 0;
-  const double tw = thr > 0.0 ? __dmul_rn(1e-6, thr) : -1.0;
+  // the Float64 tests d <= thr and |d - thr| <= 1e-6 thr as FP32 comparisons
+  const float thr_f = f_dn(thr);
+  float tlo = 1.f, thi = 0.f;
+  if (thr > 0.0 && thr < 1e300) tie_window_f(thr, __dmul_rn(1e-6, thr), tlo, thi);
   for (int i = threadIdx.x; i < n; i += LP_PT) {
-    const double d = (double)dl[i];
-    if (fabs(__dsub_rn(d, thr)) <= tw) nt++;
-    if (d <= thr) {
+    const float d = dl[i];
+    if (d >= tlo && d <= thi) nt++;
+    if (d <= thr_f) {
       const int at = atomicAdd(&sflag, 1);
       if (at < LP_SORT) keys[at] = ((unsigned long long)(uint32_t)lst[i] << 32) | __float_as_uint(dl[i]);
     }
@@ -222,20 +201,21 @@ __global__ void __launch_bounds__(LP_PT) lp_pick_kernel(const LpPickArgs a) {
 
 }  // namespace
 
-int iq_lp_pick(iq_ctx* ctx, const float* img, Dim3 imgd, Dim3 dist, const LpColumn* cols, int N,
+int iq_lp_pick(iq_ctx* ctx, const LpImg& im, Dim3 dist, const LpColumn* cols, int N,
                const int32_t* list, const int32_t* cnt, int cap, float* dl, double tol,
-               uint64_t seed, int64_t* rind, int64_t* ncand, int maxK) {
+               uint64_t seed, int64_t* rind, int64_t* ncand, int maxQ) {
   if (N <= 0) return IQ_OK;
   LpPickArgs a{};
-  a.img = img; a.isx = imgd.x; a.isxy = imgd.x * imgd.y; a.dx = dist.x; a.dxy = dist.x * dist.y;
+  a.im = im; a.dx = dist.x; a.dxy = dist.x * dist.y;
   a.cols = cols; a.list = list; a.cnt = cnt; a.cap = cap; a.dl = dl; a.tol = tol; a.seed = seed;
   a.rind = rind; a.ncand = ncand; a.ties = ctx->d_ties;
-  // shared memory: the mask's terms (8 bytes each), later the sort buffers, weights and sums
-  const size_t sm = std::max<size_t>((size_t)8 * maxK,
+  // shared memory: the mask's rows or quads (16 bytes each; maxQ: the most of either), later
+  // the sort buffers, weights and sums
+  const size_t sm = std::max<size_t>((size_t)16 * maxQ,
                                      (size_t)LP_SORT * (8 + 8 + 8 + 4) +
                                          8 * ((LP_SORT + IQ_DRAW_CHUNK - 1) / IQ_DRAW_CHUNK)) + 64;
   if (sm > 227 * 1024)
-    return iq_set_error(IQ_ERR_LIMIT, "proposal pick: a mask of %d offsets is too large", maxK);
+    return iq_set_error(IQ_ERR_LIMIT, "proposal pick: a mask of %d quads is too large", maxQ);
   IQ_CUDA_OK(cudaFuncSetAttribute(lp_pick_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
   iq_timer_start(ctx, "lp.pick");
   lp_pick_kernel<<<(unsigned)N, LP_PT, sm, ctx->stream>>>(a);

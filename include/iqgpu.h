@@ -217,10 +217,12 @@ int iq_set_option(iq_ctx* ctx, const char* name, int64_t value);
  * for every tile, src/iqsim.jl:206). A small 3-D convolutional encoder embeds a tile's masked
  * overlap and every training-image window under the same mask in 64 dimensions; iq_simulate
  * then evaluates the exact distance only at the ~lp.k positions whose embeddings lie nearest
- * the tile's, and picks among them. It applies to integer-valued (categorical) training images
+ * the tile's, and picks among them. It applies to training images of integer codes in [0, 255]
+ * (categorical facies; codes 0..3 are read as 2-bit planes)
  * without hard or soft data, for the tile shape the encoder was made for. Every lp.monitor-th
  * chunk compares one shortlist with the full exact scan; once the sampled recall of the true
- * candidate set falls below 0.99 the call continues with the full scan. Options:
+ * candidate set, over at least 1000 sampled candidates of the call, falls below 0.99 the call
+ * continues with the full scan. Options:
  *   "lp.enable"   1: use the proposal where it applies (default 0)
  *   "lp.k"        shortlist length aimed at (default 4096)
  *   "lp.monitor"  chunks between recall checks (default 16; 0: none)

@@ -52,11 +52,11 @@ def _mask(tile, box):
     return m
 
 
-def _cat_ti(shape, seed):
+def _cat_ti(shape, seed, ncodes=4):
     import scipy.ndimage as ndi
     rng = np.random.default_rng(seed)
     f = np.stack([ndi.gaussian_filter(rng.standard_normal(shape), (4, 4, 2), mode="wrap")
-                  for _ in range(4)])
+                  for _ in range(ncodes)])
     return np.argmax(f, axis=0).astype(np.float32)
 
 
@@ -108,10 +108,12 @@ def test_encoder_gradients_vs_oracle(iq, ctx):
         assert num <= 2e-3 * den + 1e-6, (k, num, den)
 
 
-def test_shortlist_of_every_position_equals_full_scan(iq, ctx):
+@pytest.mark.parametrize("ncodes", [4, 6])
+def test_shortlist_of_every_position_equals_full_scan(iq, ctx, ncodes):
     """With a shortlist that holds every position the proposal's pick sees the full candidate
-    set, so the realizations equal the full scan's; capture and training run on the way."""
-    ti = _cat_ti((30, 28, 14), 3)
+    set, so the realizations equal the full scan's; capture and training run on the way. Four
+    codes are summed from the 2-bit plane form of the image, six from its byte form."""
+    ti = _cat_ti((30, 28, 14), 3, ncodes)
     tile, simsize = (8, 8, 6), (30, 28, 14)
     kw = dict(overlap=(0.25, 0.25, 0.34), nreal=3, rng=9, ctx=ctx)
     ctx.set_ti(ti)
