@@ -332,13 +332,18 @@ def proposal_roofline(dom, prof, lp_kernels, W, peaks, peak_kind, st, args):
     ovl = [math.ceil(o * t) for o, t in zip(W["overlap"], W["tilesize"])]
     K = int(np.prod(W["tilesize"])) - int(np.prod([t - o for t, o in zip(W["tilesize"], ovl)]))
     cols = st["cols_shortlist"] if st else 0
-    byts = cols * (st["mean_shortlist"] if st else 0) * K * 4.0
+    planes = bool(np.isin(W["ti"], (0, 1, 2, 3)).all()) and W["tilesize"][0] <= 32
+    per = 0.25 if planes else 1.0
+    byts = cols * (st["mean_shortlist"] if st else 0) * K * per
     ach = byts / (ms / 1e3) / 1e9 if ms else None
     return {"bound": "hbm", "kernel": dom, "achieved": ach, "unit": "GB/s",
             "peak": peaks.get("hbm_gbs"), "peak_kind": "%s (copy)" % peak_kind,
-            "frac": ach / peaks.get("hbm_gbs") if ach else None, "traffic": None,
-            "bytes_note": "algorithmic bytes = shortlisted positions x interior mask offsets x 4 "
-                          "(the training-image values the direct sums read; L2-resident)"}
+            "frac": ach / peaks.get("hbm_gbs") if ach else None,
+            "traffic": profile_traffic("lp_pick_kernel", W["name"]),
+            "bytes_note": "algorithmic bytes = shortlisted positions x interior mask offsets x "
+                          "%s B (the %s the exact sums read; the image is L2-resident and the "
+                          "kernel is bound by L1 line lookups and integer issue, not by HBM)" % (
+                              per, "2-bit codes" if planes else "byte codes")}
 
 
 def run_ours(args, W, dist, rank, world):
@@ -430,6 +435,7 @@ def run_ours(args, W, dist, rank, world):
         lp_info = train_proposal(args, W, ctx, lib, _lib, p, hd_dev, sd_dev, out_d)
         ctx.set_option("lp.enable", 1)
         ctx.set_option("lp.k", args.lp_k)
+        ctx.set_option("lp.kmax", args.lp_kmax)
     for i in range(args.warmup):
         step_resident(i)
     torch.cuda.synchronize()
@@ -610,11 +616,14 @@ def main():
     ap.add_argument("--form", default=None, choices=["plain", "proposal"],
                     help="plain full scan, or the learned proposal (default: the proposal for "
                          "the categorical configurations 3 and 4, plain otherwise)")
-    ap.add_argument("--lp-k", type=int, default=16384, help="shortlist length of the proposal")
-    ap.add_argument("--lp-pairs", type=int, default=200000, help="training pairs to capture")
+    ap.add_argument("--lp-k", type=int, default=16384,
+                    help="shortlist length a call starts with (lp.k)")
+    ap.add_argument("--lp-kmax", type=int, default=65536,
+                    help="longest shortlist the recall monitor may raise it to (lp.kmax)")
+    ap.add_argument("--lp-pairs", type=int, default=60000, help="training pairs to capture")
     ap.add_argument("--lp-seeds", type=int, default=50)
     ap.add_argument("--lp-capture-steps", type=int, default=1500)
-    ap.add_argument("--lp-capture-reals", type=int, default=8)
+    ap.add_argument("--lp-capture-reals", type=int, default=2)
     ap.add_argument("--lp-train-steps", type=int, default=3000)
     ap.add_argument("--plain-steps", type=int, default=1)
     ap.add_argument("--no-plain", action="store_true", help="skip the full-scan comparison step")

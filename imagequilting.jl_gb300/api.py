@@ -157,10 +157,11 @@ class Context:
 
     def lp_stats(self):
         """Statistics of the last iqsim call (see include/iqgpu.h, iq_lp_stats)."""
-        out = np.zeros(9)
-        check(load().iq_lp_stats(self.h, out.ctypes.data, 9))
+        out = np.zeros(12)
+        check(load().iq_lp_stats(self.h, out.ctypes.data, 12))
         keys = ("cols_shortlist", "cols_full", "monitored", "true_candidates", "shortlisted",
-                "recall", "fell_back", "mean_shortlist", "captured")
+                "recall", "fell_back", "mean_shortlist", "captured", "k_final",
+                "recall_final", "sampled_final")
         return dict(zip(keys, out.tolist()))
 
     @property

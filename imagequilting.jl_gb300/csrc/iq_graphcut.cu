@@ -314,6 +314,72 @@ __global__ void __launch_bounds__(CUT_MAX_THREADS, 1) cut_kernel(const CutArgs a
   auto list_once = [&](int v) {  // append v to Nl unless it is there already
     if (cas_height(&flag[v], 0, 1)) Nl[atomicAdd(&s_wl[1], 1)] = (HT)v;
   };
+  // push phase over L[0, A): every listed node pushes along its admissible arcs while it has
+  // excess; the receivers' excesses are updated with integer atomics (exact in any order). Two
+  // ends of one edge never push on it in the same round (that would need h(u) = h(v) + 1 and
+  // h(v) = h(u) + 1), so each residual has one writer.
+  auto push_phase = [&](int A, int t0, int step) {
+    for (int i = t0; i < A; i += step) {
+      const int u = L[i];
+      const int hu = hc[u];
+      long long e = g.ex[u];
+      const long long e0 = e;
+#pragma unroll
+      for (int dir = 0; dir < 6; ++dir) {
+        if (e <= 0) break;
+        int v;
+        if (!g.nbr(u, dir, v)) continue;
+        if (hu != g.height(hc, v) + 1) continue;
+        long long *ruv, *rvu;
+        g.arc(u, v, dir, ruv, rvu);
+        const long long rr = *ruv;
+        if (rr <= 0) continue;
+        const long long delta = e < rr ? e : rr;
+        *ruv = rr - delta;
+        *rvu += delta;
+        e -= delta;
+        if (g.kind(v) == 0) {
+          atomicAdd(reinterpret_cast<unsigned long long*>(&g.ex[v]), (unsigned long long)delta);
+          list_once(v);
+        }
+      }
+      if (e != e0)
+        atomicAdd(reinterpret_cast<unsigned long long*>(&g.ex[u]), (unsigned long long)(e - e0));
+      if (e > 0) list_once(u);
+    }
+  };
+  // relabel phase over Nl[0, B): a node left with excess and no admissible arc moves to 1 + the
+  // lowest neighbour it still has residual capacity to; the nodes that stay active form the
+  // next round's list
+  auto relabel_phase = [&](int B, int t0, int step) {
+    for (int i = t0; i < B; i += step) {
+      const int u = Nl[i];
+      flag[u] = 0;
+      const long long e = g.ex[u];
+      int hu = hc[u];
+      if (e > 0 && hu < g.NH) {
+        bool adm = false;
+        int mh = 0x7fffffff;
+#pragma unroll
+        for (int dir = 0; dir < 6; ++dir) {
+          int v;
+          if (!g.nbr(u, dir, v)) continue;
+          long long *ruv, *rvu;
+          g.arc(u, v, dir, ruv, rvu);
+          if (!g.open(ruv, rvu)) continue;
+          const int hv = g.height(hc, v);
+          if (hu == hv + 1) { adm = true; break; }
+          mh = min(mh, hv);
+        }
+        if (!adm) {
+          hu = mh >= g.NH - 1 ? g.NH : mh + 1;
+          hc[u] = (HT)hu;
+        }
+        if (hu < g.NH) L[atomicAdd(&s_wl[0], 1)] = (HT)u;
+      }
+    }
+  };
+  __shared__ int s_round;
   if (g.L > 2) {
     relabel_all();
     rebuild();
@@ -321,77 +387,47 @@ __global__ void __launch_bounds__(CUT_MAX_THREADS, 1) cut_kernel(const CutArgs a
     for (;;) {
       const int A = s_wl[0];
       if (A == 0) break;
-      nactive += A;
-      if (threadIdx.x == 0) s_wl[1] = 0;
-      __syncthreads();
-      // push phase: every listed node pushes along its admissible arcs while it has excess;
-      // the receivers' excesses are updated with integer atomics (exact in any order). Two
-      // ends of one edge never push on it in the same round (that would need
-      // h(u) = h(v) + 1 and h(v) = h(u) + 1), so each residual has one writer.
-      for (int i = threadIdx.x; i < A; i += blockDim.x) {
-        const int u = L[i];
-        const int hu = hc[u];
-        long long e = g.ex[u];
-        const long long e0 = e;
-#pragma unroll
-        for (int dir = 0; dir < 6; ++dir) {
-          if (e <= 0) break;
-          int v;
-          if (!g.nbr(u, dir, v)) continue;
-          if (hu != g.height(hc, v) + 1) continue;
-          long long *ruv, *rvu;
-          g.arc(u, v, dir, ruv, rvu);
-          const long long rr = *ruv;
-          if (rr <= 0) continue;
-          const long long delta = e < rr ? e : rr;
-          *ruv = rr - delta;
-          *rvu += delta;
-          e -= delta;
-          if (g.kind(v) == 0) {
-            atomicAdd(reinterpret_cast<unsigned long long*>(&g.ex[v]), (unsigned long long)delta);
-            list_once(v);
+      if (A <= 32) {
+        // Rounds with at most 32 active nodes run on warp 0 alone, synchronised by __syncwarp,
+        // until the list grows past 32 or empties, or the round cap or a global relabel is due
+        // (the same rounds as the block form, without its barriers).
+        if (threadIdx.x < 32) {
+          const int lane = threadIdx.x;
+          int Aw = A;
+          for (;;) {
+            nactive += Aw;
+            if (lane == 0) s_wl[1] = 0;
+            __syncwarp();
+            push_phase(Aw, lane, 32);
+            __syncwarp();
+            const int B = s_wl[1];
+            __syncwarp();
+            if (lane == 0) s_wl[0] = 0;
+            __syncwarp();
+            relabel_phase(B, lane, 32);
+            __syncwarp();
+            ++round;
+            Aw = s_wl[0];
+            if (Aw == 0 || Aw > 32 || round >= a.round_cap || round % a.gr_period == 0) break;
           }
+          if (lane == 0) s_round = round;
         }
-        if (e != e0)
-          atomicAdd(reinterpret_cast<unsigned long long*>(&g.ex[u]), (unsigned long long)(e - e0));
-        if (e > 0) list_once(u);
+        __syncthreads();
+        round = s_round;
+      } else {
+        nactive += A;
+        if (threadIdx.x == 0) s_wl[1] = 0;
+        __syncthreads();
+        push_phase(A, threadIdx.x, blockDim.x);
+        __syncthreads();
+        const int B = s_wl[1];
+        __syncthreads();
+        if (threadIdx.x == 0) s_wl[0] = 0;
+        __syncthreads();
+        relabel_phase(B, threadIdx.x, blockDim.x);
+        __syncthreads();
+        ++round;
       }
-      __syncthreads();
-      // relabel phase over Nl: a node left with excess and no admissible arc moves to 1 + the
-      // lowest neighbour it still has residual capacity to; the nodes that stay active form
-      // the next round's list
-      const int B = s_wl[1];
-      __syncthreads();
-      if (threadIdx.x == 0) s_wl[0] = 0;
-      __syncthreads();
-      for (int i = threadIdx.x; i < B; i += blockDim.x) {
-        const int u = Nl[i];
-        flag[u] = 0;
-        const long long e = g.ex[u];
-        int hu = hc[u];
-        if (e > 0 && hu < g.NH) {
-          bool adm = false;
-          int mh = 0x7fffffff;
-#pragma unroll
-          for (int dir = 0; dir < 6; ++dir) {
-            int v;
-            if (!g.nbr(u, dir, v)) continue;
-            long long *ruv, *rvu;
-            g.arc(u, v, dir, ruv, rvu);
-            if (!g.open(ruv, rvu)) continue;
-            const int hv = g.height(hc, v);
-            if (hu == hv + 1) { adm = true; break; }
-            mh = min(mh, hv);
-          }
-          if (!adm) {
-            hu = mh >= g.NH - 1 ? g.NH : mh + 1;
-            hc[u] = (HT)hu;
-          }
-          if (hu < g.NH) L[atomicAdd(&s_wl[0], 1)] = (HT)u;
-        }
-      }
-      __syncthreads();
-      ++round;
       if (round >= a.round_cap && s_wl[0] > 0) { capped = true; break; }
       if (round % a.gr_period == 0) {
         relabel_all();

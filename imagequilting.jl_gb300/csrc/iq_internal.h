@@ -89,7 +89,8 @@ struct iq_ctx {
   cudaStream_t stream2 = nullptr;  // stream of the second realization group (made on first use)
   struct IqLp* lp = nullptr;       // learned proposal state (iq_proposal_host.cu)
   int lp_enable = 0;               // iq_simulate shortlists with the proposal where it applies
-  int64_t lp_k = 4096;             // shortlist size the proposal aims at
+  int64_t lp_k = 16384;            // shortlist size the proposal starts a call with
+  int64_t lp_kmax = 65536;         // largest size the recall monitor may raise it to
   int64_t lp_capture = 0;          // training pairs iq_simulate records (0: none)
   int lp_monitor = 16;             // every lp_monitor-th proposal chunk checks its recall
   int lp_fallback = 1;             // 0: keep the shortlists even below 0.99 recall (measuring)
@@ -646,17 +647,30 @@ __device__ __forceinline__ uint32_t iq_quad_ssd(const uint8_t* base, const uint4
 }
 
 // Plane form: stage a column's template rows (ty, tz) of the tile in shared memory as
-// (low-bit plane, high-bit plane, mask bits, ty | tz << 16). Returns false (for the block) when
-// a template value in the mask is not one of 0, 1, 2, 3.
-__device__ inline bool iq_stage_rows(const LpColumn& col, uint4* rows) {
+// (low-bit plane, high-bit plane, mask bits, ty | tz << 16): the rows outside the box's (y, z)
+// range (every x in the mask) first, then the rows through the box (x outside it only; left out
+// when the box spans every x), so that partial sums grow fast for the early exit. Returns the
+// number of rows staged, or -1 (for the whole block) when a template value in the mask is not
+// one of 0, 1, 2, 3.
+__device__ inline int iq_stage_rows(const LpColumn& col, uint4* rows) {
   const int R = col.tdim[1] * col.tdim[2];
+  const int* lh = col.lohi;
+  const int iy0 = max(lh[1], 0), iy1 = max(min(lh[4], col.tdim[1]), iy0);
+  const int iz0 = max(lh[2], 0), iz1 = max(min(lh[5], col.tdim[2]), iz0);
+  const int ny = iy1 - iy0, nz = iz1 - iz0;
+  const int nouter = R - ny * nz;
+  const bool inner_empty = lh[0] <= 0 && lh[3] >= col.tdim[0];
   int bad = 0;
   for (int r = threadIdx.x; r < R; r += blockDim.x) {
     const int ty = r % col.tdim[1], tz = r / col.tdim[1];
-    const bool rin = ty >= col.lohi[1] && ty < col.lohi[4] && tz >= col.lohi[2] && tz < col.lohi[5];
+    const bool rin = ty >= iy0 && ty < iy1 && tz >= iz0 && tz < iz1;
+    // box rows before r in (tz, ty) order
+    const int before = (min(max(tz, iz0), iz1) - iz0) * ny +
+                       (tz >= iz0 && tz < iz1 ? min(max(ty, iy0), iy1) - iy0 : 0);
+    if (rin && inner_empty) continue;
     uint32_t p0 = 0, p1 = 0, m = 0;
     for (int x = 0; x < col.tdim[0]; ++x) {
-      if (rin && x >= col.lohi[0] && x < col.lohi[3]) continue;
+      if (rin && x >= lh[0] && x < lh[3]) continue;
       const float v = col.tmpl[x + col.tgx * ty + col.tgxy * tz];
       if (!(v == 0.f || v == 1.f || v == 2.f || v == 3.f)) bad = 1;
       const uint32_t c = (uint32_t)v & 3u;
@@ -664,9 +678,9 @@ __device__ inline bool iq_stage_rows(const LpColumn& col, uint4* rows) {
       p0 |= (c & 1u) << x;
       p1 |= (c >> 1) << x;
     }
-    rows[r] = make_uint4(p0, p1, m, (uint32_t)ty | ((uint32_t)tz << 16));
+    rows[rin ? nouter + before : r - before] = make_uint4(p0, p1, m, (uint32_t)ty | ((uint32_t)tz << 16));
   }
-  return !__syncthreads_or(bad);
+  return __syncthreads_or(bad) ? -1 : (inner_empty ? nouter : R);
 }
 
 // Sum of (a - b)^2 over one row of 32 codes given as bit planes (a0, a1), (b0, b1) and mask m:
@@ -680,22 +694,26 @@ __device__ __forceinline__ int iq_row_ssd(uint32_t a0, uint32_t a1, const uint4&
 
 // Warp-collective, plane form: sum over the R staged rows for the window at (x0, y0, z0), with
 // the early exit of iq_quad_ssd.
+// (The plane image has fewer than 2^31 words: 32-bit index arithmetic.)
 template <typename Bound>
 __device__ __forceinline__ uint32_t iq_plane_ssd(const LpImg& im, int64_t x0, int64_t y0,
                                                  int64_t z0, const uint4* rows, int R,
                                                  const Bound& bound) {
   const int lane = threadIdx.x & 31;
-  const int64_t tx0 = x0 >> 5;
   const uint32_t s = (uint32_t)(x0 & 31);
+  const uint32_t ntx16 = (uint32_t)im.ntx * 16u, zs = (uint32_t)im.nty * ntx16;
+  const uint32_t base = (uint32_t)z0 * zs + ((uint32_t)x0 >> 5) * 16u;
+  const uint32_t y0u = (uint32_t)y0;
   int acc = 0;
   int r = lane;
   for (; r + 3 * 32 < R; r += 4 * 32) {
     unsigned long long wa[4], wb[4];
+    uint4 t[4];
 #pragma unroll
     for (int u = 0; u < 4; ++u) {
-      const uint32_t w = rows[r + 32 * u].w;
-      const int64_t yy = y0 + (w & 0xFFFFu), zz = z0 + (w >> 16);
-      const int64_t i0 = (((zz * im.nty + (yy >> 4)) * im.ntx + tx0) << 4) + (yy & 15);
+      t[u] = rows[r + 32 * u];
+      const uint32_t yy = y0u + (t[u].w & 0xFFFFu);
+      const uint32_t i0 = base + (t[u].w >> 16) * zs + (yy >> 4) * ntx16 + (yy & 15u);
       wa[u] = __ldg(im.b2 + i0);
       wb[u] = __ldg(im.b2 + i0 + 16);
     }
@@ -703,7 +721,7 @@ __device__ __forceinline__ uint32_t iq_plane_ssd(const LpImg& im, int64_t x0, in
     for (int u = 0; u < 4; ++u) {
       const uint32_t a0 = __funnelshift_r((uint32_t)wa[u], (uint32_t)wb[u], s);
       const uint32_t a1 = __funnelshift_r((uint32_t)(wa[u] >> 32), (uint32_t)(wb[u] >> 32), s);
-      acc += iq_row_ssd(a0, a1, rows[r + 32 * u]);
+      acc += iq_row_ssd(a0, a1, t[u]);
     }
     int part = acc;
 #pragma unroll
@@ -712,8 +730,8 @@ __device__ __forceinline__ uint32_t iq_plane_ssd(const LpImg& im, int64_t x0, in
   }
   for (; r < R; r += 32) {
     const uint4 t = rows[r];
-    const int64_t yy = y0 + (t.w & 0xFFFFu), zz = z0 + (t.w >> 16);
-    const int64_t i0 = (((zz * im.nty + (yy >> 4)) * im.ntx + tx0) << 4) + (yy & 15);
+    const uint32_t yy = y0u + (t.w & 0xFFFFu);
+    const uint32_t i0 = base + (t.w >> 16) * zs + (yy >> 4) * ntx16 + (yy & 15u);
     const unsigned long long a = __ldg(im.b2 + i0), b = __ldg(im.b2 + i0 + 16);
     acc += iq_row_ssd(__funnelshift_r((uint32_t)a, (uint32_t)b, s),
                       __funnelshift_r((uint32_t)(a >> 32), (uint32_t)(b >> 32), s), t);
@@ -723,18 +741,19 @@ __device__ __forceinline__ uint32_t iq_plane_ssd(const LpImg& im, int64_t x0, in
   return (uint32_t)acc;
 }
 
-// Stage a column for either form (rows or quads at `stage`); false: the column cannot be summed.
-__device__ inline bool iq_stage(const LpImg& im, const LpColumn& col, uint4* stage) {
-  return im.b2 ? iq_stage_rows(col, stage) : iq_stage_quads(col, stage);
+// Stage a column for either form (rows or quads at `stage`): the number of staged items, or -1
+// when the column cannot be summed in that form.
+__device__ inline int iq_stage(const LpImg& im, const LpColumn& col, uint4* stage) {
+  if (im.b2) return iq_stage_rows(col, stage);
+  return iq_stage_quads(col, stage) ? col.nq : -1;
 }
 
-// Exact sum of the column at distance-map position (x, y, z), either form.
+// Exact sum of the column at distance-map position (x, y, z), either form; n: staged items.
 template <typename Bound>
-__device__ __forceinline__ uint32_t iq_lp_ssd(const LpImg& im, const LpColumn& col,
-                                              const uint4* stage, int64_t x, int64_t y,
-                                              int64_t z, const Bound& bound) {
-  if (im.b2) return iq_plane_ssd(im, x, y, z, stage, col.tdim[1] * col.tdim[2], bound);
-  return iq_quad_ssd(im.b8 + x + im.isx * y + im.isxy * z, stage, col.nq, bound);
+__device__ __forceinline__ uint32_t iq_lp_ssd(const LpImg& im, const uint4* stage, int n,
+                                              int64_t x, int64_t y, int64_t z, const Bound& bound) {
+  if (im.b2) return iq_plane_ssd(im, x, y, z, stage, n, bound);
+  return iq_quad_ssd(im.b8 + x + im.isx * y + im.isxy * z, stage, n, bound);
 }
 #endif
 #define IQ_LP_SAMPLES 8192  // positions sampled per column for its shortlist threshold

@@ -714,10 +714,16 @@ __device__ __forceinline__ void mma_bf16(float* d, const uint32_t* a, uint32_t b
       : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
 }
 
-// Scores of every position against 64 columns (blockIdx.y) with tensor-core MMAs (BF16 in, FP32
-// accumulation): s = |w|^2 + |e|^2 - 2 w.e; positions with s <= tau[col] are appended to the
-// column's list (cap entries; cnt keeps counting past it so that an overflow is seen).
+// Scores of every position against every column with tensor-core MMAs (mma.sync m16n8k16, BF16
+// in, FP32 accumulation): s = |w|^2 + |e|^2 - 2 w.e; positions with s <= tau[col] are appended
+// to the column's list (cap entries; cnt keeps counting past it so that an overflow is seen).
+// The columns are staged in shared memory in chunks of LP_SCAN_COLS (rows padded to 36 words,
+// conflict-free fragment loads); a warp keeps the A fragments of its 16 positions in registers
+// and sweeps the chunk's columns, so the window embeddings are read once per chunk.
 // DENSE: every score is written to dense[col * P + row] instead (the sampled rows).
+constexpr int LP_SCAN_COLS = 512;
+constexpr int LP_SCAN_LD = 36;  // words per staged column (32 + 4 of padding)
+
 template <bool DENSE>
 __global__ void __launch_bounds__(256) lp_scan_kernel(const __nv_bfloat16* __restrict__ W,
                                                       const float* __restrict__ nW, int64_t P,
@@ -726,62 +732,65 @@ __global__ void __launch_bounds__(256) lp_scan_kernel(const __nv_bfloat16* __res
                                                       const float* __restrict__ tau, int N,
                                                       int32_t* list, int32_t* cnt, int cap,
                                                       float* dense) {
+  extern __shared__ __align__(16) uint32_t sT[];
+  float* sN = reinterpret_cast<float*>(sT + LP_SCAN_COLS * LP_SCAN_LD);
+  float* sTau = sN + LP_SCAN_COLS;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int gid = lane >> 2, tig = lane & 3;
-  const int n0 = blockIdx.y * 64;
-  uint32_t bf[8][4][2];
-  float ncol[8][2], tcol[8][2];
-#pragma unroll
-  for (int nt = 0; nt < 8; ++nt) {
-    const int c = n0 + nt * 8 + gid;
-    const bool ok = c < N;
-#pragma unroll
-    for (int ks = 0; ks < 4; ++ks) {
-      const uint32_t* src =
-          reinterpret_cast<const uint32_t*>(T + (int64_t)(ok ? c : 0) * EMB + ks * 16 + 2 * tig);
-      bf[nt][ks][0] = ok ? src[0] : 0u;
-      bf[nt][ks][1] = ok ? src[4] : 0u;
-    }
-#pragma unroll
-    for (int h = 0; h < 2; ++h) {
-      const int cc = n0 + nt * 8 + 2 * tig + h;
-      ncol[nt][h] = cc < N ? nT[cc] : 0.f;
-      tcol[nt][h] = DENSE ? 0.f : (cc < N ? tau[cc] : -1.f);
-    }
-  }
+  const uint32_t* T32 = reinterpret_cast<const uint32_t*>(T);
   const int64_t nblk = (P + 15) / 16;
-  for (int64_t blk = (int64_t)blockIdx.x * 8 + warp; blk < nblk; blk += (int64_t)gridDim.x * 8) {
-    const int64_t p0 = blk * 16;
-    const int64_t r0 = p0 + gid, r1 = p0 + gid + 8;
-    const int64_t q0 = r0 < P ? r0 : P - 1, q1 = r1 < P ? r1 : P - 1;
-    uint32_t af[4][4];
-#pragma unroll
-    for (int ks = 0; ks < 4; ++ks) {
-      const uint32_t* x0 = reinterpret_cast<const uint32_t*>(W + q0 * EMB + ks * 16 + 2 * tig);
-      const uint32_t* x1 = reinterpret_cast<const uint32_t*>(W + q1 * EMB + ks * 16 + 2 * tig);
-      af[ks][0] = x0[0];
-      af[ks][1] = x1[0];
-      af[ks][2] = x0[4];
-      af[ks][3] = x1[4];
+  for (int c0 = 0; c0 < N; c0 += LP_SCAN_COLS) {
+    const int nc = min(LP_SCAN_COLS, N - c0);
+    __syncthreads();  // the previous chunk's readers are done
+    for (int i = threadIdx.x; i < nc * 32; i += blockDim.x)
+      sT[(i >> 5) * LP_SCAN_LD + (i & 31)] = T32[(int64_t)(c0 + (i >> 5)) * 32 + (i & 31)];
+    for (int i = threadIdx.x; i < nc; i += blockDim.x) {
+      sN[i] = nT[c0 + i];
+      sTau[i] = DENSE ? 0.f : tau[c0 + i];
     }
-    const float w0 = nW[q0], w1 = nW[q1];
+    __syncthreads();
+    for (int64_t blk = (int64_t)blockIdx.x * 8 + warp; blk < nblk; blk += (int64_t)gridDim.x * 8) {
+      const int64_t p0 = blk * 16;
+      const int64_t r0 = p0 + gid, r1 = p0 + gid + 8;
+      const int64_t q0 = r0 < P ? r0 : P - 1, q1 = r1 < P ? r1 : P - 1;
+      uint32_t af[4][4];
 #pragma unroll
-    for (int nt = 0; nt < 8; ++nt) {
-      float acc[4] = {0.f, 0.f, 0.f, 0.f};
+      for (int ks = 0; ks < 4; ++ks) {
+        const uint32_t* x0 = reinterpret_cast<const uint32_t*>(W + q0 * EMB + ks * 16 + 2 * tig);
+        const uint32_t* x1 = reinterpret_cast<const uint32_t*>(W + q1 * EMB + ks * 16 + 2 * tig);
+        af[ks][0] = x0[0];
+        af[ks][1] = x1[0];
+        af[ks][2] = x0[4];
+        af[ks][3] = x1[4];
+      }
+      const float w0 = nW[q0], w1 = nW[q1];
+      for (int cb = 0; cb < nc; cb += 64) {
+#pragma unroll 2
+        for (int nt = 0; nt < 8; ++nt) {
+          const int cl = cb + nt * 8 + gid;
+          // word ks * 8 + tig holds dims ks * 16 + 2 tig, +1 (b0); +4 words: dims + 8 (b1)
+          const uint32_t* src = sT + (cl < nc ? cl : 0) * LP_SCAN_LD + tig;
+          float acc[4] = {0.f, 0.f, 0.f, 0.f};
 #pragma unroll
-      for (int ks = 0; ks < 4; ++ks) mma_bf16(acc, af[ks], bf[nt][ks][0], bf[nt][ks][1]);
+          for (int ks = 0; ks < 4; ++ks) {
+            const uint32_t b0 = cl < nc ? src[ks * 8] : 0u, b1 = cl < nc ? src[ks * 8 + 4] : 0u;
+            mma_bf16(acc, af[ks], b0, b1);
+          }
 #pragma unroll
-      for (int e = 0; e < 4; ++e) {
-        const int h = e & 1;
-        const int64_t row = e < 2 ? r0 : r1;
-        const float s = (e < 2 ? w0 : w1) + ncol[nt][h] - 2.f * acc[e];
-        if (DENSE) {
-          const int c = n0 + nt * 8 + 2 * tig + h;
-          if (row < P && c < N) dense[(int64_t)c * P + row] = s;
-        } else if (row < P && s <= tcol[nt][h]) {
-          const int c = n0 + nt * 8 + 2 * tig + h;
-          const int idx = atomicAdd(cnt + c, 1);
-          if (idx < cap) list[(int64_t)c * cap + idx] = (int32_t)row;
+          for (int e = 0; e < 4; ++e) {
+            const int h = e & 1;
+            const int cc = cb + nt * 8 + 2 * tig + h;  // column within the chunk
+            if (cc >= nc) continue;
+            const int64_t row = e < 2 ? r0 : r1;
+            if (row >= P) continue;
+            const float s = (e < 2 ? w0 : w1) + sN[cc] - 2.f * acc[e];
+            if (DENSE) {
+              dense[(int64_t)(c0 + cc) * P + row] = s;
+            } else if (s <= sTau[cc]) {
+              const int idx = atomicAdd(cnt + c0 + cc, 1);
+              if (idx < cap) list[(int64_t)(c0 + cc) * cap + idx] = (int32_t)row;
+            }
+          }
         }
       }
     }
@@ -858,12 +867,13 @@ __global__ void __launch_bounds__(256) lp_full_kernel(const LpImg im, int64_t dx
                                                       unsigned* dmin) {
   extern __shared__ __align__(16) unsigned char dyn[];
   uint4* qd = reinterpret_cast<uint4*>(dyn);
-  if (!iq_stage(im, col, qd)) return;
+  const int nst = iq_stage(im, col, qd);
+  if (nst < 0) return;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   unsigned mn = 0x7F800000u;
   for (int64_t p = (int64_t)blockIdx.x * 8 + warp; p < P; p += (int64_t)gridDim.x * 8) {
     const int64_t z = p / dxy, r = p - z * dxy, y = r / dx, x = r - y * dx;
-    const uint32_t s = iq_lp_ssd(im, col, qd, x, y, z, [] { return INFINITY; });
+    const uint32_t s = iq_lp_ssd(im, qd, nst, x, y, z, [] { return INFINITY; });
     const float acc = (float)s;
     if (lane == 0) D[p] = acc;
     mn = min(mn, __float_as_uint(acc));
@@ -991,19 +1001,20 @@ int iq_lp_shortlist(iq_ctx* ctx, const __nv_bfloat16* W, const float* nW, int64_
   int dev = 0, nsm = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-  const int ncb = (N + 63) / 64;
   iq_timer_start(ctx, "lp.scan");
   // per-column thresholds: the sampled rows' scores as one GEMM, then a select per column
-  lp_scan_kernel<true><<<dim3((unsigned)((S / 16 + 7) / 8), (unsigned)ncb), 256, 0, st>>>(
+  const size_t sm = sizeof(uint32_t) * LP_SCAN_COLS * LP_SCAN_LD + 2 * sizeof(float) * LP_SCAN_COLS;
+  IQ_CUDA_OK(cudaFuncSetAttribute(lp_scan_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+  IQ_CUDA_OK(cudaFuncSetAttribute(lp_scan_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+  lp_scan_kernel<true><<<(unsigned)((S / 16 + 7) / 8), 256, sm, st>>>(
       Ws, nWs, S, T, nT, nullptr, N, nullptr, nullptr, 0, dense);
   lp_select_kernel<<<(unsigned)N, 256, 0, st>>>(dense, S, m, tau);
   IQ_CUDA_OK(cudaGetLastError());
   IQ_CUDA_OK(cudaMemsetAsync(cnt, 0, sizeof(int32_t) * N, st));
   const int64_t nblk = (P + 15) / 16;
-  const int64_t gx = std::max<int64_t>(1, std::min<int64_t>((nblk + 7) / 8, (int64_t)nsm * 8 / ncb + 1));
-  lp_scan_kernel<false><<<dim3((unsigned)gx, (unsigned)ncb), 256, 0, st>>>(W, nW, P, T, nT, tau,
-                                                                           N, list, cnt, cap,
-                                                                           nullptr);
+  const int64_t gx = std::max<int64_t>(1, std::min<int64_t>((nblk + 7) / 8, (int64_t)nsm * 2));
+  lp_scan_kernel<false><<<(unsigned)gx, 256, sm, st>>>(W, nW, P, T, nT, tau, N, list, cnt, cap,
+                                                       nullptr);
   iq_timer_stop(ctx, "lp.scan", 2.0 * (double)(P + S) * N * EMB);
   iq_count(ctx, 3);
   IQ_CUDA_OK(cudaGetLastError());

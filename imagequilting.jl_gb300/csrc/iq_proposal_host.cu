@@ -61,6 +61,8 @@ struct IqLp {
   // statistics of the current call
   int64_t cols_lp = 0, cols_full = 0, mon_cols = 0, short_total = 0;
   double mon_true = 0, mon_hit = 0;
+  int64_t k_cur = 0;                  // shortlist length of the current phase of the call
+  double ph_true = 0, ph_hit = 0;     // sampled candidates since k_cur was set
   bool off = false;       // sampled recall fell below 0.99: full scan for the rest of the call
   unsigned long long* d_counters = nullptr;
   unsigned* d_dmin = nullptr;
@@ -187,7 +189,7 @@ int ensure_ti8(iq_ctx* ctx, IqLp* lp) {
     if (rc) return rc;
     IQ_CUDA_OK(cudaMemcpyAsync(&bad, lp->d_bad, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
     IQ_CUDA_OK(cudaStreamSynchronize(ctx->stream));
-    lp->ti2_ok = bad == 0;
+    lp->ti2_ok = bad == 0 && words < ((size_t)1 << 31);
     lp->ti2_ntx = ntx;
     lp->ti2_nty = nty;
   }
@@ -296,6 +298,8 @@ void iq_lp_begin_call(iq_ctx* ctx) {
   IqLp* lp = ctx->lp;
   lp->cols_lp = lp->cols_full = lp->mon_cols = lp->short_total = 0;
   lp->mon_true = lp->mon_hit = 0;
+  lp->ph_true = lp->ph_hit = 0;
+  lp->k_cur = ctx->lp_k;
   lp->off = false;
 }
 
@@ -325,7 +329,8 @@ int iq_lp_run_chunk(iq_ctx* ctx, const LpChunk& c, int64_t chunk_index, int* don
   cudaStream_t st = ctx->stream;
   const int N = c.ncol;
   const int64_t P = c.dist.vol();
-  const int cap = (int)std::min<int64_t>(std::max<int64_t>(16384, 4 * ctx->lp_k), P);
+  const int64_t kk = lp->k_cur > 0 ? lp->k_cur : ctx->lp_k;
+  const int cap = (int)std::min<int64_t>(std::max<int64_t>(16384, 4 * kk), P);
   // columns in the order of their mask configuration
   std::vector<int> ord(N);
   for (int i = 0; i < N; ++i) ord[i] = i;
@@ -397,7 +402,7 @@ int iq_lp_run_chunk(iq_ctx* ctx, const LpChunk& c, int64_t chunk_index, int* don
     rc = window_embeddings(ctx, lp, c.lohi + 6 * c.cfg[ord[q0]], &wc);
     if (rc) return rc;
     rc = iq_lp_shortlist(ctx, wc->W, wc->nW, P, wc->Ws, wc->nWs, dT + (size_t)q0 * IQ_LP_EMB,
-                         dnT + q0, q1 - q0, ctx->lp_k, dtau + q0, ddense, dlist + (size_t)q0 * cap,
+                         dnT + q0, q1 - q0, kk, dtau + q0, ddense, dlist + (size_t)q0 * cap,
                          dcnt + q0, cap);
     if (rc) return rc;
     q0 = q1;
@@ -436,10 +441,19 @@ int iq_lp_run_chunk(iq_ctx* ctx, const LpChunk& c, int64_t chunk_index, int* don
     lp->mon_cols += 1;
     lp->mon_true += (double)hcnt[0];
     lp->mon_hit += (double)hcnt[1];
-    // the sampled recall decides once it rests on enough candidates (a standard error of
-    // about 0.003 at recall 0.99)
-    if (ctx->lp_fallback && lp->mon_true >= kMonMinTrue && lp->mon_hit < 0.99 * lp->mon_true)
-      lp->off = true;
+    lp->ph_true += (double)hcnt[0];
+    lp->ph_hit += (double)hcnt[1];
+    // the sampled recall of the current shortlist length decides once it rests on enough
+    // candidates (a standard error of about 0.003 at recall 0.99): below 0.99 the length
+    // doubles (up to lp.kmax) and is judged afresh; at lp.kmax the call takes the full scan
+    if (ctx->lp_fallback && lp->ph_true >= kMonMinTrue && lp->ph_hit < 0.99 * lp->ph_true) {
+      if (2 * lp->k_cur <= ctx->lp_kmax) {
+        lp->k_cur *= 2;
+        lp->ph_true = lp->ph_hit = 0;
+      } else {
+        lp->off = true;
+      }
+    }
   }
   for (int q = 0; q < N; ++q)
     if (hr[q] < 0) return IQ_OK;  // a shortlist overflowed: the full scan takes this chunk
@@ -738,12 +752,18 @@ int iq_lp_capture_reserve(iq_ctx* ctx, int64_t n) {
 // Statistics of the last iq_simulate call: [0] columns picked from a shortlist, [1] columns of
 // the full scan, [2] monitored columns, [3] their exact candidates, [4] of those shortlisted,
 // [5] sampled recall (-1: none sampled), [6] 1 when the recall fell below 0.99 and the call
-// fell back to the full scan, [7] mean shortlist length, [8] captured training pairs.
+// fell back to the full scan, [7] mean shortlist length, [8] captured training pairs; with
+// n >= 12 also [9] the shortlist length the call ended with, [10] the sampled recall at that
+// length (-1: none sampled), [11] its sampled candidates.
 extern "C" int iq_lp_stats(iq_ctx* ctx, double* out, int32_t n) {
   if (!ctx || !out || n < 9) return iq_set_error(IQ_ERR_ARG, "invalid argument");
   IqLp* lp = ctx->lp;
   for (int i = 0; i < n; ++i) out[i] = 0.0;
-  if (!lp) { out[5] = -1.0; return IQ_OK; }
+  if (!lp) {
+    out[5] = -1.0;
+    if (n >= 12) out[10] = -1.0;
+    return IQ_OK;
+  }
   out[0] = (double)lp->cols_lp;
   out[1] = (double)lp->cols_full;
   out[2] = (double)lp->mon_cols;
@@ -753,6 +773,11 @@ extern "C" int iq_lp_stats(iq_ctx* ctx, double* out, int32_t n) {
   out[6] = lp->off ? 1.0 : 0.0;
   out[7] = lp->cols_lp > 0 ? (double)lp->short_total / (double)lp->cols_lp : 0.0;
   out[8] = (double)lp->cap_n;
+  if (n >= 12) {
+    out[9] = (double)(lp->k_cur > 0 ? lp->k_cur : ctx->lp_k);
+    out[10] = lp->ph_true > 0 ? lp->ph_hit / lp->ph_true : -1.0;
+    out[11] = lp->ph_true;
+  }
   return IQ_OK;
 }
 

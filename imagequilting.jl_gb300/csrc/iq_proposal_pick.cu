@@ -65,7 +65,8 @@ __global__ void __launch_bounds__(LP_PT) lp_pick_kernel(const LpPickArgs a) {
   // the column's rows (plane form) or quads (byte form) in shared memory
   uint4* qd = reinterpret_cast<uint4*>(dyn);
   if (threadIdx.x == 0) smin = 0x7F7FFFFFu;
-  if (!iq_stage(a.im, col, qd)) {  // template values outside the form: the column falls back
+  const int nst = iq_stage(a.im, col, qd);
+  if (nst < 0) {  // template values outside the form: the column falls back
     if (threadIdx.x == 0) { a.rind[c] = -1; a.ncand[c] = 0; }
     return;
   }
@@ -79,7 +80,7 @@ __global__ void __launch_bounds__(LP_PT) lp_pick_kernel(const LpPickArgs a) {
   for (int i = warp; i < n; i += LP_PT / 32) {
     const int64_t p = lst[i];
     const int64_t z = p / a.dxy, r = p - z * a.dxy, y = r / a.dx, x = r - y * a.dx;
-    const uint32_t s = iq_lp_ssd(a.im, col, qd, x, y, z, [&] {
+    const uint32_t s = iq_lp_ssd(a.im, qd, nst, x, y, z, [&] {
       return __uint_as_float(*(volatile unsigned*)&smin) * pf;
     });
     const bool pruned = s == 0xFFFFFFFFu;

@@ -221,13 +221,15 @@ int iq_set_option(iq_ctx* ctx, const char* name, int64_t value);
  * (categorical facies; codes 0..3 are read as 2-bit planes)
  * without hard or soft data, for the tile shape the encoder was made for. Every lp.monitor-th
  * chunk compares one shortlist with the full exact scan; once the sampled recall of the true
- * candidate set, over at least 1000 sampled candidates of the call, falls below 0.99 the call
- * continues with the full scan. Options:
+ * candidate set, over at least 1000 sampled candidates, falls below 0.99 the shortlist length
+ * doubles (and is judged afresh), and at lp.kmax the call continues with the full scan. Options:
  *   "lp.enable"   1: use the proposal where it applies (default 0)
- *   "lp.k"        shortlist length aimed at (default 4096)
+ *   "lp.k"        shortlist length a call starts with (default 16384)
+ *   "lp.kmax"     the recall monitor doubles the length while the sampled recall of the current
+ *                 length is below 0.99, up to this (default 65536), then falls back
  *   "lp.monitor"  chunks between recall checks (default 16; 0: none)
- *   "lp.fallback" 1 (default): switch to the full scan below 0.99 sampled recall; 0: keep the
- *                 shortlists (to measure the recall of an encoder)
+ *   "lp.fallback" 1 (default): longer shortlists, then the full scan, below 0.99 sampled
+ *                 recall; 0: keep the shortlists of lp.k (to measure the recall of an encoder)
  *   "lp.capture"  capacity of training pairs recorded by iq_simulate's full-scan picks
  *                 (template features + 8 of its exact candidates); setting it clears them
  */
@@ -252,7 +254,9 @@ int iq_lp_train(iq_ctx* ctx, int32_t steps, int32_t batch, int32_t nneg, double 
                 uint64_t seed, double* loss_first, double* loss_last);
 /* Statistics of the last iq_simulate (n >= 9): columns from shortlists, columns of the full
  * scan, monitored columns, their exact candidates, those shortlisted, sampled recall (-1: none),
- * fell back (1/0), mean shortlist length, captured training pairs. */
+ * fell back (1/0), mean shortlist length, captured training pairs; n >= 12 adds the shortlist
+ * length the call ended with, the sampled recall at that length (-1: none) and its sampled
+ * candidates. */
 int iq_lp_stats(iq_ctx* ctx, double* out, int32_t n);
 
 #ifdef __cplusplus
