@@ -432,7 +432,14 @@ def run_ours(args, W, dist, rank, world):
     _lib.check(lib.iq_set_ti(ctx.h, ti_h.ctypes.data, ti_dt, N, size))
     lp_info = None
     if args.form == "proposal":
-        lp_info = train_proposal(args, W, ctx, lib, _lib, p, hd_dev, sd_dev, out_d)
+        if args.lp_load:
+            # parameters trained by an earlier run of this bench (--lp-save), for profiling runs
+            ctx.lp_set_params(W["tilesize"], np.load(args.lp_load))
+            lp_info = {"loaded": os.path.basename(args.lp_load)}
+        else:
+            lp_info = train_proposal(args, W, ctx, lib, _lib, p, hd_dev, sd_dev, out_d)
+            if args.lp_save:
+                np.save(args.lp_save, ctx.lp_params())
         ctx.set_option("lp.enable", 1)
         ctx.set_option("lp.k", args.lp_k)
         ctx.set_option("lp.kmax", args.lp_kmax)
@@ -616,11 +623,14 @@ def main():
     ap.add_argument("--form", default=None, choices=["plain", "proposal"],
                     help="plain full scan, or the learned proposal (default: the proposal for "
                          "the categorical configurations 3 and 4, plain otherwise)")
-    ap.add_argument("--lp-k", type=int, default=16384,
+    ap.add_argument("--lp-k", type=int, default=8192,
                     help="shortlist length a call starts with (lp.k)")
     ap.add_argument("--lp-kmax", type=int, default=65536,
                     help="longest shortlist the recall monitor may raise it to (lp.kmax)")
     ap.add_argument("--lp-pairs", type=int, default=60000, help="training pairs to capture")
+    ap.add_argument("--lp-save", default=None, help="save the trained encoder parameters (.npy)")
+    ap.add_argument("--lp-load", default=None,
+                    help="use saved encoder parameters instead of capturing and training")
     ap.add_argument("--lp-seeds", type=int, default=50)
     ap.add_argument("--lp-capture-steps", type=int, default=1500)
     ap.add_argument("--lp-capture-reals", type=int, default=2)

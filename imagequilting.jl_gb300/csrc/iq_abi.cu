@@ -284,6 +284,11 @@ extern "C" int iq_set_option(iq_ctx* ctx, const char* name, int64_t value) {
     ctx->lp_k = value;
     return IQ_OK;
   }
+  if (!strcmp(name, "lp.train_near")) {
+    if (value < 0 || value > 4096) return iq_set_error(IQ_ERR_ARG, "lp.train_near out of range");
+    ctx->lp_train_near = (int)value;
+    return IQ_OK;
+  }
   if (!strcmp(name, "lp.kmax")) {
     if (value < 16 || value > (1 << 22)) return iq_set_error(IQ_ERR_ARG, "lp.kmax out of range");
     ctx->lp_kmax = value;

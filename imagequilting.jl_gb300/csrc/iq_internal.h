@@ -89,8 +89,9 @@ struct iq_ctx {
   cudaStream_t stream2 = nullptr;  // stream of the second realization group (made on first use)
   struct IqLp* lp = nullptr;       // learned proposal state (iq_proposal_host.cu)
   int lp_enable = 0;               // iq_simulate shortlists with the proposal where it applies
-  int64_t lp_k = 16384;            // shortlist size the proposal starts a call with
+  int64_t lp_k = 8192;             // shortlist size the proposal starts a call with
   int64_t lp_kmax = 65536;         // largest size the recall monitor may raise it to
+  int lp_train_near = 16;          // training negatives per anchor drawn next to its positive
   int64_t lp_capture = 0;          // training pairs iq_simulate records (0: none)
   int lp_monitor = 16;             // every lp_monitor-th proposal chunk checks its recall
   int lp_fallback = 1;             // 0: keep the shortlists even below 0.99 recall (measuring)

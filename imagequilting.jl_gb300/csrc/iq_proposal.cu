@@ -724,8 +724,10 @@ __device__ __forceinline__ void mma_bf16(float* d, const uint32_t* a, uint32_t b
 constexpr int LP_SCAN_COLS = 512;
 constexpr int LP_SCAN_LD = 36;  // words per staged column (32 + 4 of padding)
 
+constexpr int LP_SCAN_THREADS = 512;  // 16 warps: two CTAs fill half an SM's warp slots
+
 template <bool DENSE>
-__global__ void __launch_bounds__(256) lp_scan_kernel(const __nv_bfloat16* __restrict__ W,
+__global__ void __launch_bounds__(LP_SCAN_THREADS) lp_scan_kernel(const __nv_bfloat16* __restrict__ W,
                                                       const float* __restrict__ nW, int64_t P,
                                                       const __nv_bfloat16* __restrict__ T,
                                                       const float* __restrict__ nT,
@@ -749,7 +751,8 @@ __global__ void __launch_bounds__(256) lp_scan_kernel(const __nv_bfloat16* __res
       sTau[i] = DENSE ? 0.f : tau[c0 + i];
     }
     __syncthreads();
-    for (int64_t blk = (int64_t)blockIdx.x * 8 + warp; blk < nblk; blk += (int64_t)gridDim.x * 8) {
+    const int nw = blockDim.x >> 5;
+    for (int64_t blk = (int64_t)blockIdx.x * nw + warp; blk < nblk; blk += (int64_t)gridDim.x * nw) {
       const int64_t p0 = blk * 16;
       const int64_t r0 = p0 + gid, r1 = p0 + gid + 8;
       const int64_t q0 = r0 < P ? r0 : P - 1, q1 = r1 < P ? r1 : P - 1;
@@ -1006,15 +1009,15 @@ int iq_lp_shortlist(iq_ctx* ctx, const __nv_bfloat16* W, const float* nW, int64_
   const size_t sm = sizeof(uint32_t) * LP_SCAN_COLS * LP_SCAN_LD + 2 * sizeof(float) * LP_SCAN_COLS;
   IQ_CUDA_OK(cudaFuncSetAttribute(lp_scan_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
   IQ_CUDA_OK(cudaFuncSetAttribute(lp_scan_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-  lp_scan_kernel<true><<<(unsigned)((S / 16 + 7) / 8), 256, sm, st>>>(
+  lp_scan_kernel<true><<<(unsigned)((S / 16 + 15) / 16), LP_SCAN_THREADS, sm, st>>>(
       Ws, nWs, S, T, nT, nullptr, N, nullptr, nullptr, 0, dense);
   lp_select_kernel<<<(unsigned)N, 256, 0, st>>>(dense, S, m, tau);
   IQ_CUDA_OK(cudaGetLastError());
   IQ_CUDA_OK(cudaMemsetAsync(cnt, 0, sizeof(int32_t) * N, st));
   const int64_t nblk = (P + 15) / 16;
-  const int64_t gx = std::max<int64_t>(1, std::min<int64_t>((nblk + 7) / 8, (int64_t)nsm * 2));
-  lp_scan_kernel<false><<<(unsigned)gx, 256, sm, st>>>(W, nW, P, T, nT, tau, N, list, cnt, cap,
-                                                       nullptr);
+  const int64_t gx = std::max<int64_t>(1, std::min<int64_t>((nblk + 15) / 16, (int64_t)nsm * 2));
+  lp_scan_kernel<false><<<(unsigned)gx, LP_SCAN_THREADS, sm, st>>>(W, nW, P, T, nT, tau, N, list,
+                                                                   cnt, cap, nullptr);
   iq_timer_stop(ctx, "lp.scan", 2.0 * (double)(P + S) * N * EMB);
   iq_count(ctx, 3);
   IQ_CUDA_OK(cudaGetLastError());

@@ -710,9 +710,28 @@ extern "C" int iq_lp_train(iq_ctx* ctx, int32_t steps, int32_t batch, int32_t nn
     }
     for (int b = 0; b < batch; ++b) { items.push_back(rows[b]); items.push_back(-1); items.push_back(rows[b]); items.push_back(0); }
     for (int b = 0; b < batch; ++b) { items.push_back(-1); items.push_back(pos[b]); items.push_back(rows[b]); items.push_back(0); }
+    // negatives: random windows, and (lp.train_near of them) windows a few voxels from the
+    // positive, which look alike but are rarely candidates: the ranking near the top
+    const Dim3 dm = lp->cap_dist;
+    const int nnear = std::min(nneg, ctx->lp_train_near);
     for (int b = 0; b < batch; ++b)
       for (int k = 0; k < nneg; ++k) {
-        items.push_back(-1); items.push_back((int32_t)rnd((uint64_t)P)); items.push_back(rows[b]); items.push_back(0);
+        int64_t q = (int64_t)rnd((uint64_t)P);
+        if (k < nnear) {
+          const int64_t p = pos[b];
+          const int64_t x = p % dm.x, y = (p / dm.x) % dm.y, z = p / (dm.x * dm.y);
+          int64_t dx = 0, dy = 0, dz = 0;
+          while (dx == 0 && dy == 0 && dz == 0) {
+            dx = (int64_t)rnd(7) - 3;
+            dy = (int64_t)rnd(7) - 3;
+            dz = dm.z > 1 ? (int64_t)rnd(3) - 1 : 0;
+          }
+          const int64_t nx = std::min(std::max<int64_t>(x + dx, 0), dm.x - 1);
+          const int64_t ny = std::min(std::max<int64_t>(y + dy, 0), dm.y - 1);
+          const int64_t nz = std::min(std::max<int64_t>(z + dz, 0), dm.z - 1);
+          q = nx + dm.x * (ny + dm.y * nz);
+        }
+        items.push_back(-1); items.push_back((int32_t)q); items.push_back(rows[b]); items.push_back(0);
       }
     double l = 0.0;
     const bool want = s == 0 || s == steps - 1;

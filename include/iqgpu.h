@@ -224,12 +224,14 @@ int iq_set_option(iq_ctx* ctx, const char* name, int64_t value);
  * candidate set, over at least 1000 sampled candidates, falls below 0.99 the shortlist length
  * doubles (and is judged afresh), and at lp.kmax the call continues with the full scan. Options:
  *   "lp.enable"   1: use the proposal where it applies (default 0)
- *   "lp.k"        shortlist length a call starts with (default 16384)
+ *   "lp.k"        shortlist length a call starts with (default 8192)
  *   "lp.kmax"     the recall monitor doubles the length while the sampled recall of the current
  *                 length is below 0.99, up to this (default 65536), then falls back
  *   "lp.monitor"  chunks between recall checks (default 16; 0: none)
  *   "lp.fallback" 1 (default): longer shortlists, then the full scan, below 0.99 sampled
  *                 recall; 0: keep the shortlists of lp.k (to measure the recall of an encoder)
+ *   "lp.train_near" of the nneg negatives of iq_lp_train, how many are windows within 3 voxels
+ *                 (x, y) and 1 (z) of the positive instead of random ones (default 16)
  *   "lp.capture"  capacity of training pairs recorded by iq_simulate's full-scan picks
  *                 (template features + 8 of its exact candidates); setting it clears them
  */

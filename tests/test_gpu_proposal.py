@@ -132,7 +132,7 @@ def test_shortlist_of_every_position_equals_full_scan(iq, ctx, ncodes):
         st = ctx.lp_stats()
     finally:
         ctx.set_option("lp.enable", 0)
-        ctx.set_option("lp.k", 16384)
+        ctx.set_option("lp.k", 8192)
         ctx.set_option("lp.monitor", 16)
     assert st["cols_shortlist"] > 0 and st["recall"] == 1.0 and st["fell_back"] == 0
     for a, b in zip(full, lp):
@@ -166,7 +166,7 @@ def test_training_gains_recall(iq, ctx):
             ctx.set_option("lp.enable", 0)
             ctx.set_option("lp.fallback", 1)
             ctx.set_option("lp.monitor", 16)
-            ctx.set_option("lp.k", 16384)
+            ctx.set_option("lp.k", 8192)
 
     r0 = recall(untrained)
     ctx.set_option("lp.capture", 20000)
