@@ -346,6 +346,23 @@ def proposal_roofline(dom, prof, lp_kernels, W, peaks, peak_kind, st, args):
                               per, "2-bit codes" if planes else "byte codes")}
 
 
+def cut_roofline(prof, cut_nodes, peaks, peak_kind, W):
+    """Roofline of the graph cut: the slab values it must read (A and B, 4 bytes each per node)
+    and the mask it writes (1 byte per node), over its time, against HBM; the kernel itself is
+    bound by barrier and atomic latency (push-relabel rounds), not by bandwidth."""
+    ms, n, _ = prof["graphcut"]
+    nodes = cut_nodes[2]
+    byts = 9.0 * nodes
+    ach = byts / (ms / 1e3) / 1e9 if ms else None
+    return {"bound": "hbm", "kernel": "graphcut", "achieved": ach, "unit": "GB/s",
+            "peak": peaks.get("hbm_gbs"), "peak_kind": "%s (copy)" % peak_kind,
+            "frac": ach / peaks.get("hbm_gbs") if ach else None,
+            "traffic": profile_traffic("cut_kernel", W["name"]),
+            "bytes_note": "algorithmic bytes = 9 per slab node (A and B read, mask written); "
+                          "%d slabs of %.0f nodes on average; latency-bound rounds" % (
+                              cut_nodes[1], nodes / cut_nodes[1] if cut_nodes[1] else 0)}
+
+
 def run_ours(args, W, dist, rank, world):
     import ctypes
 
@@ -486,6 +503,7 @@ def run_ours(args, W, dist, rank, world):
     pk = {k: ctx.profile_get("pick." + k) for k in ("select_cycles", "weight_cycles", "draw_cycles",
                                                    "band_cycles", "ev1", "ev2", "ev3")}
     counters["pick_cycles_per_cta"] = {k: (v[2] / v[1]) if v[1] else None for k, v in pk.items()}
+    cut_nodes = ctx.profile_get("graphcut.nodes")  # (ms, CTAs, nodes)
     lp_stats = ctx.lp_stats() if args.form == "proposal" else None
     lp_kernels = {k: ctx.profile_get(k) for k in ("lp.encode", "lp.scan", "lp.pick", "lp.monitor")} \
         if args.form == "proposal" else {}
@@ -608,6 +626,12 @@ def run_ours(args, W, dist, rank, world):
             line["roofline"] = proposal_roofline(dom, prof, lp_kernels, W, peaks, peak_kind,
                                                  lp_stats, args)
             line["dominant_kernel"] = dom
+        elif dom == "graphcut":
+            line["roofline"] = cut_roofline(prof, cut_nodes, peaks, peak_kind, W)
+        # the proposal's own kernels, whichever dominates
+        line["proposal"]["kernel_rooflines"] = {
+            k: proposal_roofline(k, prof, lp_kernels, W, peaks, peak_kind, lp_stats, args)
+            for k in ("lp.pick", "lp.scan") if k in prof}
     print(json.dumps(line), flush=True)
     ctx.close()
 

@@ -149,10 +149,12 @@ __device__ __forceinline__ int global_relabel(const Graph& g, HT* hc, HT* fa, HT
   return level;
 }
 
-// GS: the slab lives in global scratch (too large for shared memory). The shared-memory form
-// derives every array from the shared window itself, so its loads, stores and atomics are
-// shared-memory instructions rather than generic ones.
-template <typename HT, bool GS>
+// MODE 0: the slab lives in shared memory; the form derives every array from the shared window
+// itself, so its loads, stores and atomics are shared-memory instructions rather than generic
+// ones. MODE 1: everything in global scratch (too large for shared memory). MODE 2: the
+// residuals, heights and node info (what every push and relabel reads) in shared memory, the
+// excesses and the BFS frontiers in global scratch (slabs of 8 x 32 x 16 nodes, configs 3-4).
+template <typename HT, int MODE>
 __global__ void __launch_bounds__(CUT_MAX_THREADS, 1) cut_kernel(const CutArgs a) {
   extern __shared__ __align__(16) char smem[];
   const int s_id = blockIdx.x;
@@ -175,19 +177,31 @@ __global__ void __launch_bounds__(CUT_MAX_THREADS, 1) cut_kernel(const CutArgs a
   const int n = g.n;
 
   char* base = smem;
-  if constexpr (GS) base = a.scratch + (int64_t)(blockIdx.y * gridDim.x + blockIdx.x) * a.scratch_per_cta;
+  char* gbase = a.scratch + (int64_t)(blockIdx.y * gridDim.x + blockIdx.x) * a.scratch_per_cta;
+  if constexpr (MODE == 1) base = gbase;
   long long* dp = reinterpret_cast<long long*>(base);
+  HT *h0, *h1, *fa, *fb;
   g.R = dp;
-  g.ex = dp + 6 * n;
-  HT* ip = reinterpret_cast<HT*>(dp + 7 * n);
-  HT* const h0 = ip;          // heights, double-buffered
-  HT* const h1 = ip + n;
-  HT* const fa = ip + 2 * n;  // BFS frontier lists
-  HT* const fb = ip + 3 * n;
+  if constexpr (MODE == 2) {
+    HT* ip = reinterpret_cast<HT*>(dp + 6 * n);
+    h0 = ip;        // heights, double-buffered
+    h1 = ip + n;
+    g.info = reinterpret_cast<uint8_t*>(ip + 2 * n);
+    g.ex = reinterpret_cast<long long*>(gbase);
+    fa = reinterpret_cast<HT*>(g.ex + n);  // BFS frontier lists
+    fb = fa + n;
+  } else {
+    g.ex = dp + 6 * n;
+    HT* ip = reinterpret_cast<HT*>(dp + 7 * n);
+    h0 = ip;
+    h1 = ip + n;
+    fa = ip + 2 * n;
+    fb = ip + 3 * n;
+    g.info = reinterpret_cast<uint8_t*>(ip + 4 * n);
+  }
   __shared__ int s_cnt[2];
   __shared__ unsigned long long s_cmax;  // bits of the largest capacity
   if (threadIdx.x == 0) s_cmax = 0ull;
-  g.info = reinterpret_cast<uint8_t*>(ip + 4 * n);
   float* Av = reinterpret_cast<float*>(g.ex);  // A and B alias the excesses (8n bytes), which
   float* Bv = Av + n;                          // are first written after the capacities
 
@@ -470,6 +484,13 @@ size_t cut_bytes(int64_t nodes, int hbytes) {
   size_t b = (size_t)nodes * (7 * 8 + 4 * hbytes + 1);
   return (b + 255) & ~(size_t)255;
 }
+// MODE 2: shared part (residuals, two heights, node info) and global part (excess, frontiers)
+size_t cut_bytes_shared2(int64_t nodes, int hbytes) {
+  return ((size_t)nodes * (6 * 8 + 2 * hbytes + 1) + 255) & ~(size_t)255;
+}
+size_t cut_bytes_global2(int64_t nodes, int hbytes) {
+  return ((size_t)nodes * (8 + 2 * hbytes) + 255) & ~(size_t)255;
+}
 constexpr int64_t CUT_SHORT_MAX = 32767;  // largest slab with 16-bit heights and indices
 }  // namespace
 
@@ -497,22 +518,25 @@ int iq_launch_cut(iq_ctx* ctx, const CutLaunch& L) {
   const int64_t nmax = L.slabmax;
   const size_t need = iq_cut_scratch_bytes(nmax);
   const bool narrow = nmax <= CUT_SHORT_MAX;
-  auto kern = narrow ? cut_kernel<short, false> : cut_kernel<int, false>;
-  int smem_limit = 0;
-  {
-    // dynamic shared memory may use the opt-in maximum minus the kernel's static part
+  const int hb = narrow ? 2 : 4;
+  // dynamic shared memory may use the opt-in maximum minus the kernel's static part
+  auto limit_of = [&](void (*k)(CutArgs), int& lim) -> int {
     int dev = 0, v = 0;
     IQ_CUDA_OK(cudaGetDevice(&dev));
     IQ_CUDA_OK(cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
     cudaFuncAttributes fa;
-    IQ_CUDA_OK(cudaFuncGetAttributes(&fa, kern));
-    smem_limit = v - (int)fa.sharedSizeBytes;
-    IQ_CUDA_OK(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_limit));
-  }
+    IQ_CUDA_OK(cudaFuncGetAttributes(&fa, k));
+    lim = v - (int)fa.sharedSizeBytes;
+    IQ_CUDA_OK(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, lim));
+    return IQ_OK;
+  };
+  void (*kern)(CutArgs) = narrow ? cut_kernel<short, 0> : cut_kernel<int, 0>;
+  int smem_limit = 0;
+  if (int rc = limit_of(kern, smem_limit)) return rc;
   size_t dyn = 0;
+  a.scratch = nullptr;
+  a.scratch_per_cta = 0;
   if ((int64_t)need <= smem_limit) {
-    a.scratch = nullptr;
-    a.scratch_per_cta = 0;
     dyn = need;
   } else {
     if (!L.scratch || L.scratch_per_cta < (int64_t)need)
@@ -520,7 +544,16 @@ int iq_launch_cut(iq_ctx* ctx, const CutLaunch& L) {
                           (long long)nmax);
     a.scratch = (char*)L.scratch;
     a.scratch_per_cta = L.scratch_per_cta;
-    kern = narrow ? cut_kernel<short, true> : cut_kernel<int, true>;
+    void (*k2)(CutArgs) = narrow ? cut_kernel<short, 2> : cut_kernel<int, 2>;
+    int lim2 = 0;
+    if (int rc = limit_of(k2, lim2)) return rc;
+    if ((int64_t)cut_bytes_shared2(nmax, hb) <= lim2 &&
+        (int64_t)cut_bytes_global2(nmax, hb) <= L.scratch_per_cta) {
+      kern = k2;
+      dyn = cut_bytes_shared2(nmax, hb);
+    } else {
+      kern = narrow ? cut_kernel<short, 1> : cut_kernel<int, 1>;
+    }
   }
   const int threads = (L.threads == 256 || L.threads == 1024) ? L.threads : 512;
   dim3 grid((unsigned)nslab_max, (unsigned)(L.ntask * L.nreal));
