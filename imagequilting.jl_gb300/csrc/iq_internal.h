@@ -685,12 +685,15 @@ __device__ inline int iq_stage_rows(const LpColumn& col, uint4* rows) {
 }
 
 // Sum of (a - b)^2 over one row of 32 codes given as bit planes (a0, a1), (b0, b1) and mask m:
-// with u = a1 - b1, v = a0 - b0 in {-1, 0, 1}, (a - b)^2 = 4u^2 + 4uv + v^2.
+// with u = a1 - b1, v = a0 - b0 in {-1, 0, 1}, (a - b)^2 = 4u^2 + 4uv + v^2, u^2 = a1 ^ b1,
+// v^2 = a0 ^ b0, and where both are nonzero uv = +1 exactly when a1 == a0 (then u and v have
+// the sign of a1 - b1 = a0 - b0), so sum 4uv = 4 popc(y) - 8 popc(y & (a1 ^ a0)) with
+// y = (a1 ^ b1) & (a0 ^ b0).
 __device__ __forceinline__ int iq_row_ssd(uint32_t a0, uint32_t a1, const uint4& t) {
-  const uint32_t b0 = t.x, b1 = t.y, m = t.z;
-  const uint32_t up = a1 & ~b1, un = ~a1 & b1, vp = a0 & ~b0, vn = ~a0 & b0;
-  const uint32_t same = ((up & vp) | (un & vn)) & m, opp = ((up & vn) | (un & vp)) & m;
-  return 4 * __popc((a1 ^ b1) & m) + __popc((a0 ^ b0) & m) + 4 * __popc(same) - 4 * __popc(opp);
+  const uint32_t m = t.z;
+  const uint32_t x1 = (a1 ^ t.y) & m, x0 = (a0 ^ t.x) & m;
+  const uint32_t y = x1 & x0;
+  return __popc(x0) + 4 * (__popc(x1) + __popc(y)) - 8 * __popc(y & (a1 ^ a0));
 }
 
 // Warp-collective, plane form: sum over the R staged rows for the window at (x0, y0, z0), with

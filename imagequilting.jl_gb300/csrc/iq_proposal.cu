@@ -746,9 +746,10 @@ __global__ void __launch_bounds__(LP_SCAN_THREADS) lp_scan_kernel(const __nv_bfl
     __syncthreads();  // the previous chunk's readers are done
     for (int i = threadIdx.x; i < nc * 32; i += blockDim.x)
       sT[(i >> 5) * LP_SCAN_LD + (i & 31)] = T32[(int64_t)(c0 + (i >> 5)) * 32 + (i & 31)];
+    // scan: |w|^2 - 2 w.e <= tau - |e|^2 (one FMA and a compare per pair)
     for (int i = threadIdx.x; i < nc; i += blockDim.x) {
       sN[i] = nT[c0 + i];
-      sTau[i] = DENSE ? 0.f : tau[c0 + i];
+      sTau[i] = DENSE ? 0.f : tau[c0 + i] - nT[c0 + i];
     }
     __syncthreads();
     const int nw = blockDim.x >> 5;
@@ -786,10 +787,9 @@ __global__ void __launch_bounds__(LP_SCAN_THREADS) lp_scan_kernel(const __nv_bfl
             if (cc >= nc) continue;
             const int64_t row = e < 2 ? r0 : r1;
             if (row >= P) continue;
-            const float s = (e < 2 ? w0 : w1) + sN[cc] - 2.f * acc[e];
             if (DENSE) {
-              dense[(int64_t)(c0 + cc) * P + row] = s;
-            } else if (s <= sTau[cc]) {
+              dense[(int64_t)(c0 + cc) * P + row] = (e < 2 ? w0 : w1) + sN[cc] - 2.f * acc[e];
+            } else if (fmaf(-2.f, acc[e], e < 2 ? w0 : w1) <= sTau[cc]) {
               const int idx = atomicAdd(cnt + c0 + cc, 1);
               if (idx < cap) list[(int64_t)(c0 + cc) * cap + idx] = (int32_t)row;
             }
