@@ -661,6 +661,8 @@ def main():
     ap.add_argument("--lp-train-steps", type=int, default=3000)
     ap.add_argument("--plain-steps", type=int, default=1)
     ap.add_argument("--no-plain", action="store_true", help="skip the full-scan comparison step")
+    ap.add_argument("--nreal", type=int, default=0,
+                    help="realizations per call (default: the workload's; for profiling captures)")
     ap.add_argument("--cpu-budget", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer arm")
@@ -671,6 +673,9 @@ def main():
     args = ap.parse_args()
     dist, rank, world = dist_setup()
     W = workload(args.workload)
+    if args.nreal:
+        W["nreal"] = args.nreal  # smaller device footprint for profiling captures
+        W["desc"] += " (nreal set to %d)" % args.nreal
     if args.form is None:
         args.form = "proposal" if args.workload in ("cfg3", "cfg4") else "plain"
     if args.impl == "reference":
