@@ -915,28 +915,6 @@ __device__ __noinline__ void ref_init(const Ref& f, const int32_t* pos, int64_t 
   __syncthreads();
 }
 
-// Level 0 for entries [0, n) of pos: the map's own FP32 value with its error bound, a radius R
-// with E(v + R) <= R for the increasing bound E(D) of the map at distance D (then |D - v| <= R
-// wherever D - E(D) increases past v + R, checked below); entries without one get R = Inf.
-__device__ __noinline__ void ref_init0(const Ref& f, const float* __restrict__ src, const int32_t* pos,
-                                       int64_t n, RefArr a) {
-  const double sb = sqrt(fmax(f.b2, 0.0));
-  const double dmin = f.kappa < 0.5 ? (f.kappa * sb / (1.0 - f.kappa)) * (f.kappa * sb / (1.0 - f.kappa)) * 1.01 : 1e308;
-  for (int64_t i = threadIdx.x; i < n; i += PT) {
-    const double v = (double)src[pos[i] & 0x7FFFFFFF];
-    double R = 1.5 * tier0_bound(f, v);
-    bool ok = false;
-    for (int it = 0; it < 6; ++it) {
-      const double need = tier0_bound(f, v + R);
-      if (need <= R) { ok = true; break; }
-      R = fmax(need, 1.5 * R);
-    }
-    if (!ok || !(v + R > dmin) || !(v < 1e300)) R = __longlong_as_double(0x7FF0000000000000ll);
-    a.v[i] = v; a.r[i] = R; a.l[i] = 0;
-  }
-  __syncthreads();
-}
-
 // Raise every marked entry by one level, or to level 3 when `to3`.
 __device__ __noinline__ void ref_raise(const Ref& f, const int32_t* pos, int64_t n, RefArr a, bool to3) {
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -1284,11 +1262,10 @@ __device__ __noinline__ unsigned long long count_near(Smem& s, const float* __re
 // returns the sum of (n - rank + 1). Ties of the Float64 distance share a rank.
 // `have`: the intervals of the candidates are in `a` already (the refined threshold pick).
 __device__ __noinline__ unsigned long long dense_ranks_refined(Smem& s, unsigned long long* sbuf, const Ref& f,
-                                                  const float* __restrict__ src,
                                                   const int32_t* cand, int64_t n, RefArr a,
                                                   bool have, uint32_t* k0, uint32_t* v0,
                                                   uint32_t* k1, uint32_t* v1, uint32_t* rank) {
-  if (!have) ref_init0(f, src, cand, n, a);
+  if (!have) ref_init(f, cand, n, a);
   uint32_t* ord = const_cast<uint32_t*>(ref_sort(s, sbuf, n, a, k0, v0, k1, v1));
   ref_resolve(s, f, cand, n, ord, a);
   uint32_t carry = 0;
@@ -1662,7 +1639,7 @@ __global__ void __launch_bounds__(PT) pick_kernel(const PickArgs a) {
     unsigned long long S;
     if (can_ref && ref_on(xs)) {
       const Ref f = make_ref(xs, r, a.dx, a.dxy);
-      S = dense_ranks_refined(s, sbuf, f, src, cand, n, ra, j == 0 && have0, k0, v0, k1, v1, rankbuf);
+      S = dense_ranks_refined(s, sbuf, f, cand, n, ra, j == 0 && have0, k0, v0, k1, v1, rankbuf);
     } else {
       S = dense_ranks(s, sbuf, src, cand, n, k0, v0, k1, v1, rankbuf);
     }
