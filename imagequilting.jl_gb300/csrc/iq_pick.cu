@@ -799,7 +799,8 @@ __device__ __forceinline__ void ref_term_c(const Ref& f, const RefCache& c, int6
 
 // Warp-collective: value and radius of D[p] at `level` (every lane gets the same result). The
 // image is L2-resident and the loop is bound by the latency of its loads, so each lane issues
-// sixteen of them (level 1; four at level 2) before it uses the first.
+// four of them before it uses the first (sixteen measured slower on config 2: more registers,
+// fewer resident warps).
 __device__ __noinline__ void ref_eval(const Ref& f, const RefCache& c, int64_t p, int level,
                                       double& v, double& r) {
   const int lane = threadIdx.x & 31;
@@ -809,12 +810,12 @@ __device__ __noinline__ void ref_eval(const Ref& f, const RefCache& c, int64_t p
   if (level <= 1) {
     float acc = 0.f;
     int j = lane;
-    for (; j + 15 * 32 < f.K; j += 16 * 32) {
-      float ta[16], tb[16];
+    for (; j + 3 * 32 < f.K; j += 4 * 32) {
+      float ta[4], tb[4];
 #pragma unroll
-      for (int u = 0; u < 16; ++u) ref_term_c(f, c, base, j + 32 * u, ta[u], tb[u]);
+      for (int u = 0; u < 4; ++u) ref_term_c(f, c, base, j + 32 * u, ta[u], tb[u]);
 #pragma unroll
-      for (int u = 0; u < 16; ++u) {
+      for (int u = 0; u < 4; ++u) {
         const float d = __fsub_rn(ta[u], tb[u]);
         acc = __fmaf_rn(d, d, acc);
       }
