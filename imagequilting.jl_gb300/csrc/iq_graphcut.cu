@@ -306,7 +306,12 @@ __global__ void __launch_bounds__(CUT_MAX_THREADS, 1) cut_kernel(const CutArgs a
   HT* const L = fa;     // nodes with excess and height below NH (pushed this round)
   HT* const Nl = fb;    // nodes to relabel: the pushers left with excess and the receivers
   HT* const flag = h1;  // 1 while a node is in Nl
-  __shared__ int s_wl[2];  // |L|, |Nl|
+  // list lengths, double-buffered by round parity `par`: a round reads |L| = s_cl[par] and
+  // appends the receivers to Nl through s_cn[par], the next round's L through s_cl[par ^ 1];
+  // the counters of the other parity are zeroed while nobody uses them, so a round needs only
+  // a barrier after its push phase and one after its relabel phase
+  __shared__ int s_cl[2], s_cn[2];
+  int par = 0;
   int round = 0, levels = 0;
   long long nactive = 0;
   const long long t_setup = prof ? clock64() : 0;
@@ -317,16 +322,17 @@ __global__ void __launch_bounds__(CUT_MAX_THREADS, 1) cut_kernel(const CutArgs a
   };
   // the active list from scratch (after a global relabel, which used the lists as frontiers)
   auto rebuild = [&]() {
-    if (threadIdx.x == 0) s_wl[0] = 0;
+    par = 0;
+    if (threadIdx.x == 0) { s_cl[0] = 0; s_cl[1] = 0; s_cn[0] = 0; s_cn[1] = 0; }
     __syncthreads();
     for (int u = threadIdx.x; u < n; u += blockDim.x) {
       flag[u] = 0;
-      if (g.kind(u) == 0 && g.ex[u] > 0 && (int)hc[u] < g.NH) L[atomicAdd(&s_wl[0], 1)] = (HT)u;
+      if (g.kind(u) == 0 && g.ex[u] > 0 && (int)hc[u] < g.NH) L[atomicAdd(&s_cl[0], 1)] = (HT)u;
     }
     __syncthreads();
   };
   auto list_once = [&](int v) {  // append v to Nl unless it is there already
-    if (cas_height(&flag[v], 0, 1)) Nl[atomicAdd(&s_wl[1], 1)] = (HT)v;
+    if (cas_height(&flag[v], 0, 1)) Nl[atomicAdd(&s_cn[par], 1)] = (HT)v;
   };
   // push phase over L[0, A): every listed node pushes along its admissible arcs while it has
   // excess; the receivers' excesses are updated with integer atomics (exact in any order). Two
@@ -389,60 +395,58 @@ __global__ void __launch_bounds__(CUT_MAX_THREADS, 1) cut_kernel(const CutArgs a
           hu = mh >= g.NH - 1 ? g.NH : mh + 1;
           hc[u] = (HT)hu;
         }
-        if (hu < g.NH) L[atomicAdd(&s_wl[0], 1)] = (HT)u;
+        if (hu < g.NH) L[atomicAdd(&s_cl[par ^ 1], 1)] = (HT)u;
       }
     }
   };
-  __shared__ int s_round;
+  __shared__ int s_round, s_par;
   if (g.L > 2) {
     relabel_all();
     rebuild();
     bool capped = false;
     for (;;) {
-      const int A = s_wl[0];
+      const int A = s_cl[par];
       if (A == 0) break;
       if (A <= 32) {
         // Rounds with at most 32 active nodes run on warp 0 alone, synchronised by __syncwarp,
         // until the list grows past 32 or empties, or the round cap or a global relabel is due
         // (the same rounds as the block form, without its barriers).
+        __syncthreads();  // every thread has read A before warp 0 moves the counters on
         if (threadIdx.x < 32) {
           const int lane = threadIdx.x;
           int Aw = A;
           for (;;) {
             nactive += Aw;
-            if (lane == 0) s_wl[1] = 0;
-            __syncwarp();
+            if (lane == 0) s_cn[par ^ 1] = 0;
             push_phase(Aw, lane, 32);
             __syncwarp();
-            const int B = s_wl[1];
-            __syncwarp();
-            if (lane == 0) s_wl[0] = 0;
-            __syncwarp();
+            const int B = s_cn[par];
+            if (lane == 0) s_cl[par] = 0;
             relabel_phase(B, lane, 32);
             __syncwarp();
             ++round;
-            Aw = s_wl[0];
+            par ^= 1;
+            Aw = s_cl[par];
             if (Aw == 0 || Aw > 32 || round >= a.round_cap || round % a.gr_period == 0) break;
           }
-          if (lane == 0) s_round = round;
+          if (lane == 0) { s_round = round; s_par = par; }
         }
         __syncthreads();
         round = s_round;
+        par = s_par;
       } else {
         nactive += A;
-        if (threadIdx.x == 0) s_wl[1] = 0;
-        __syncthreads();
+        if (threadIdx.x == 0) s_cn[par ^ 1] = 0;
         push_phase(A, threadIdx.x, blockDim.x);
         __syncthreads();
-        const int B = s_wl[1];
-        __syncthreads();
-        if (threadIdx.x == 0) s_wl[0] = 0;
-        __syncthreads();
+        const int B = s_cn[par];
+        if (threadIdx.x == 0) s_cl[par] = 0;
         relabel_phase(B, threadIdx.x, blockDim.x);
         __syncthreads();
         ++round;
+        par ^= 1;
       }
-      if (round >= a.round_cap && s_wl[0] > 0) { capped = true; break; }
+      if (round >= a.round_cap && s_cl[par] > 0) { capped = true; break; }
       if (round % a.gr_period == 0) {
         relabel_all();
         rebuild();
