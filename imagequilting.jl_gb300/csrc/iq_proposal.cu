@@ -89,20 +89,28 @@ __device__ void template_cell(const LpGeo& g, const float* __restrict__ src, int
                               int64_t gxy, const int* lo, const int* hi, int cell, float* out) {
   int c3[3];
   cell_of(g, cell, c3[0], c3[1], c3[2]);
-  double s1 = 0.0, s2 = 0.0, cnt = 0.0;
+  // rows summed in FP32, rows added in Float64 (exact for integer codes, the proposal's data;
+  // GB300's FP64 pipe is narrow, so FP64 work per row rather than per voxel)
+  double s1 = 0.0, s2 = 0.0;
+  int cnt = 0;
   const int a0 = c3[0] * g.c[0], a1 = c3[1] * g.c[1], a2 = c3[2] * g.c[2];
   const int b0 = min(a0 + g.c[0], g.t[0]), b1 = min(a1 + g.c[1], g.t[1]), b2 = min(a2 + g.c[2], g.t[2]);
   for (int z = a2; z < b2; ++z)
-    for (int y = a1; y < b1; ++y)
+    for (int y = a1; y < b1; ++y) {
+      const bool rin = y >= lo[1] && y < hi[1] && z >= lo[2] && z < hi[2];
+      float r1 = 0.f, r2 = 0.f;
       for (int x = a0; x < b0; ++x) {
-        if (x >= lo[0] && x < hi[0] && y >= lo[1] && y < hi[1] && z >= lo[2] && z < hi[2]) continue;
-        const double v = (double)src[x + gx * y + gxy * z];
-        s1 += v;
-        s2 += v * v;
-        cnt += 1.0;
+        if (rin && x >= lo[0] && x < hi[0]) continue;
+        const float v = src[x + gx * y + gxy * z];
+        r1 += v;
+        r2 = fmaf(v, v, r2);
+        ++cnt;
       }
+      s1 += (double)r1;
+      s2 += (double)r2;
+    }
   const double vol = (double)g.c[0] * g.c[1] * g.c[2];
-  out[0] = (float)(cnt / vol);
+  out[0] = (float)((double)cnt / vol);
   out[1] = (float)(s1 / vol);
   out[2] = (float)(s2 / vol);
 }
