@@ -701,19 +701,6 @@ int iq_lp_adam(iq_ctx* ctx, float* p, const float* g, float* m, float* v, int n,
 // =============================================================================================
 namespace {
 
-
-__device__ __forceinline__ float bdot64(const __nv_bfloat16* x, const float* e) {
-  float acc = 0.f;
-  const __nv_bfloat162* x2 = reinterpret_cast<const __nv_bfloat162*>(x);
-#pragma unroll 8
-  for (int i = 0; i < EMB / 2; ++i) {
-    const float2 f = __bfloat1622float2(x2[i]);
-    acc = fmaf(f.x, e[2 * i], acc);
-    acc = fmaf(f.y, e[2 * i + 1], acc);
-  }
-  return acc;
-}
-
 __device__ __forceinline__ void mma_bf16(float* d, const uint32_t* a, uint32_t b0, uint32_t b1) {
   asm volatile(
       "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, "
