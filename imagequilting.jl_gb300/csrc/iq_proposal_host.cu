@@ -2,7 +2,7 @@
 // and Adam state, the cached window embeddings of the resident training image (one set per mask
 // configuration), training pairs captured from full-scan simulations, the training loop, and the
 // per-chunk path of iq_simulate -- template embeddings, shortlists, the shortlist pick, the
-// recall monitor and the fall-back to the full scan.
+// recall monitor with its shortlist doubling, and the fall-back to the full scan.
 #include <cuda_bf16.h>
 
 #include <algorithm>

@@ -1,13 +1,15 @@
 // The pick of the learned proposal: exact distances at a column's shortlisted positions, then the
 // pick of src/iqsim.jl:236-246 on them -- threshold (1 + tol) min D, tau-model weights
 // (src/taumodel.jl:5-45, one source) and the StatsBase draw in the fixed summation order of the
-// full pick (iq_pick.cu). The distances are FP32 direct sums, exact for the integer-valued
-// (categorical) data the proposal serves; whenever the shortlist holds the full candidate set
-// the result equals the full scan's.
+// full pick (iq_pick.cu). The distances are integer sums (exact) over the categorical codes the
+// proposal serves; whenever the shortlist holds the full candidate set the result equals the
+// full scan's.
 //
-// Byte-valued images: the training image is read as bytes and a mask as quads of four
-// consecutive x offsets of one row; a lane forms the four differences of a quad with one
-// __vabsdiffu4 and adds their squares with one __dp4a (integer arithmetic: exact).
+// Codes 0..3 with tiles of x extent <= 32: the training image as 2-bit planes and the template
+// as staged rows, one row of 32 codes per lane step (iq_plane_ssd in iq_internal.h). Other byte
+// codes: the image as bytes and the mask as quads of four consecutive x offsets of one row; a
+// lane forms the four differences of a quad with one __vabsdiffu4 and adds their squares with
+// one __dp4a. A sum stops early once it exceeds (1 + tol) x the running minimum x (1 + 2e-6).
 #include "iq_internal.h"
 
 namespace {
